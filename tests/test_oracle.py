@@ -1,0 +1,114 @@
+"""The FP64 oracle against golden vectors produced by the reference itself."""
+
+import os
+
+import numpy as np
+import pytest
+
+from oracle import kirchhoff_oracle as ko
+from tests.conftest import GOLDEN
+
+CASES = ["k2d_kin", "k2d_dyn_ap", "k2d_dyn_noap", "k3d_kin", "k3d_dyn", "k2d_dyn_byot", "k2d_kin_f32"]
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz"), allow_pickle=False))
+
+
+def build(g):
+    y = g.get("y")
+    kw = dict(y=y)
+    if "vel_model" in g:
+        vel = g["vel_model"]
+        kw.update(mode="byot", trav=(g["trav_in_srcs"], g["trav_in_recs"]),
+                  amp=(g["amp_in_srcs"], g["amp_in_recs"]))
+    else:
+        vel = float(g["vel_scalar"])
+        kw.update(mode="analytic")
+    if "aperture_in" in g:
+        kw["aperture"] = float(g["aperture_in"])
+    if "angleaperture_in" in g:
+        kw["angleaperture"] = float(g["angleaperture_in"])
+    elif bool(g["dynamic"]):
+        kw["angleaperture"] = None if np.allclose(g["angleaperture"], np.deg2rad([0.0, 1000.0])) else 90.0
+    return ko.KirchhoffOracle(g["z"], g["x"], g["t"], g["srcs"], g["recs"], vel, g["wav"],
+                              int(g["wavc"]), dynamic=bool(g["dynamic"]), **kw)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a, np.float64) - np.asarray(b, np.float64)) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_tables_match_reference(name):
+    g = load(name)
+    K = build(g)
+    np.testing.assert_allclose(K.trav_srcs, g["trav_srcs"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(K.trav_recs, g["trav_recs"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(K.aperture, g["aperture"])
+    np.testing.assert_allclose(K.angleaperture, g["angleaperture"])
+    np.testing.assert_allclose(K.aperturetap, g["aperturetap"], rtol=0, atol=1e-15)
+    if K.dynamic:
+        for k in ("amp_srcs", "amp_recs", "angle_srcs", "angle_recs", "vel"):
+            np.testing.assert_allclose(getattr(K, k), g[k], rtol=1e-12, atol=1e-14, err_msg=k)
+        np.testing.assert_array_equal(K.six, g["six"])
+        np.testing.assert_array_equal(K.rix, g["rix"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_spread_gather_match_reference(name):
+    g = load(name)
+    K = build(g)
+    tol = 1e-6 if g["fwd"].dtype == np.float32 or g["spread"].dtype == np.float32 else 1e-12
+    assert rel(K.spread(g["m_in"]), g["spread"]) < tol
+    assert rel(K.gather(g["d_in"]), g["gather"]) < max(tol, 1e-12)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_matvec_rmatvec_match_reference(name):
+    g = load(name)
+    K = build(g)
+    tol = 1e-6 if g["adj"].dtype == np.float32 else 1e-11
+    assert rel(K.matvec(g["m_in"]), g["fwd"]) < tol
+    assert rel(K.rmatvec(g["d_in"]), g["adj"]) < tol
+
+
+def test_convolve1d_matches_reference():
+    g = load("convolve1d")
+    keys = sorted(k[2:] for k in g if k.startswith("h_"))
+    assert len(keys) == 6
+    for key in keys:
+        nh, off = map(int, key.split("_"))
+        h = ko.pad_wavelet(g["h_" + key], off)
+        x = g["x_" + key]
+        np.testing.assert_allclose(ko.conv_same(x, h), g["fwd_" + key], rtol=1e-9, atol=1e-10, err_msg=key)
+        np.testing.assert_allclose(ko.conv_same(x, h[::-1].copy()), g["adj_" + key], rtol=1e-9, atol=1e-10, err_msg=key)
+
+
+def test_solvers_match_reference():
+    g = load("solvers")
+    K = build(load("k2d_dyn_noap"))
+    d = g["d"]
+    out = ko.lsqr(K.matvec, K.rmatvec, d, K.ni, niter=12)
+    assert out[1] == int(g["lsqr_istop"]) and out[2] == int(g["lsqr_iiter"])
+    np.testing.assert_allclose(out[9], g["lsqr_cost"], rtol=1e-8)
+    np.testing.assert_allclose(np.array(out[10]), g["lsqr_iterates"].reshape(len(out[10]), -1), rtol=1e-7, atol=1e-9)
+    for k, i in (("lsqr_r1", 3), ("lsqr_r2", 4), ("lsqr_anorm", 5), ("lsqr_acond", 6), ("lsqr_arnorm", 7), ("lsqr_xnorm", 8)):
+        np.testing.assert_allclose(out[i], g[k], rtol=1e-7, err_msg=k)
+    out = ko.cgls(K.matvec, K.rmatvec, d, K.ni, niter=12, tol=1e-10)
+    np.testing.assert_allclose(out[5], g["cgls_cost"], rtol=1e-8)
+    np.testing.assert_allclose(np.array(out[6]), g["cgls_iterates"].reshape(len(out[6]), -1), rtol=1e-7, atol=1e-9)
+    out = ko.lsqr(K.matvec, K.rmatvec, d, K.ni, niter=6, damp=0.1)
+    np.testing.assert_allclose(out[9], g["lsqrd_cost"], rtol=1e-8)
+    np.testing.assert_allclose(out[0], g["lsqrd_x"].ravel(), rtol=1e-7, atol=1e-9)
+    out = ko.cgls(K.matvec, K.rmatvec, d, K.ni, niter=6, damp=0.1, tol=1e-10, x0=0.1 * np.ones(K.ni))
+    np.testing.assert_allclose(out[5], g["cglsd_cost"], rtol=1e-8)
+    np.testing.assert_allclose(out[0], g["cglsd_x"].ravel(), rtol=1e-7, atol=1e-9)
+
+
+def test_traveltime_known_answer():
+    g = load("traveltime_ana")
+    src = np.array([100, 0])[:, np.newaxis]
+    ts, tr, ds, dr, _, _ = ko.traveltime_table_analytic(np.arange(0, 200, 1), np.arange(0, 200, 1), src, src, 500.0)
+    assert ts[0, 0] == 100 / 500.0 == float(g["trav00"])
+    assert ds[0, 0] + dr[0, 0] == 200 == float(g["dist00"])
