@@ -1,0 +1,453 @@
+"""Kirchhoff forward+adjoint throughput on one GB300.
+
+Workload (the headline configuration that fits one GPU): 2-D Kirchhoff,
+mode='eikonal', dynamic=True, angleaperture=60 deg, float32; v(z)=1500+0.5 z
+m/s plus 5 seeded Gaussian anomalies (+-200 m/s, sigma 40 m); grid nz=300,
+nx=800, dz=dx=5 m; nt=1501, dt=2 ms, 15 Hz Ricker; 64 sources and 400
+receivers at the surface; reflectivity of 12 random-dip layers plus sparse
+spikes.  Synthetic, seeded inputs of those shapes.
+
+A step is one forward (spreading + wavelet) and one adjoint (correlation +
+gathering) over the whole data volume.  ``value`` is compulsory GB moved per
+step / step time (GB/s), the metric's HBM-roofline view; ``e2e`` is the same
+metric through the public API with host numpy buffers (copies inside).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``--impl reference`` times the CPU restatement of the reference's numba loop
+nest (oracle/kirch_oracle.c, all host threads) on a bounded sample.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "kirchhoff2d_eikonal_dynamic_300x800_64x400_nt1501"
+METRIC = "Kirchhoff fwd+adj GB/s vs HBM peak"
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_workload(seed: int = 1):
+    from pylops_gb300.utils.wavelets import ricker
+
+    nz, nx, dz, dx = 300, 800, 5.0, 5.0
+    nt, dt = 1501, 0.002
+    ns, nr = 64, 400
+    z = np.arange(nz) * dz
+    x = np.arange(nx) * dx
+    t = np.arange(nt) * dt
+    rng = np.random.default_rng(seed)
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    vel = 1500.0 + 0.5 * Z
+    for _ in range(5):
+        cx, cz = rng.uniform(x[0], x[-1]), rng.uniform(z[0] + 200, z[-1])
+        amp = rng.choice([-200.0, 200.0])
+        vel += amp * np.exp(-((X - cx) ** 2 + (Z - cz) ** 2) / (2 * 40.0 ** 2))
+    srcs = np.vstack((np.linspace(x[0], x[-1], ns), np.zeros(ns)))
+    recs = np.vstack((np.linspace(x[0], x[-1], nr), np.zeros(nr)))
+    wav, _, wc = ricker(t[:41], f0=15)
+    refl = np.zeros((nx, nz))
+    for _ in range(12):
+        z0 = rng.uniform(20, nz - 20)
+        dip = np.tan(np.deg2rad(rng.uniform(-15, 15)))
+        a = rng.standard_normal()
+        for ix in range(nx):
+            iz = int(round(z0 + dip * (ix - nx / 2)))
+            if 0 <= iz < nz:
+                refl[ix, iz] += a
+    spikes = rng.random((nx, nz)) < 1e-3
+    refl[spikes] += rng.standard_normal(int(spikes.sum()))
+    return dict(z=z, x=x, t=t, srcs=srcs, recs=recs, vel=vel, wav=wav, wc=wc, refl=refl,
+                ns=ns, nr=nr, nt=nt, nz=nz, nx=nx)
+
+
+def compulsory_bytes(ni, ns, nr, nt, s_tab=12):
+    """Compulsory HBM bytes of one forward + one adjoint: each table entry,
+    the model and the data read or written once per application."""
+    return 2 * (s_tab * ni * (ns + nr) + 4 * ni + 4 * ns * nr * nt)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.lines = []
+        self.idx = device_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [s.strip() for s in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: C restatement of the numba loop nest on the host cores
+# ---------------------------------------------------------------------------
+def cpu_baseline(K, m, d, target_s=10.0):
+    """Time the oracle on a bounded sample of sources (all host threads) and
+    scale to one full forward + adjoint.  Returns the baseline record, the
+    number of sampled sources and the oracle's forward rows / adjoint image
+    for that sample (for the parity check of the same run)."""
+    from oracle.kirch_oracle_c import COracle, build
+
+    build()
+    C = COracle(K, _padded_wavelet(K))
+    t0 = time.perf_counter()
+    _cpu_step(C, m, d, 0, 1)
+    t1 = time.perf_counter() - t0
+    nsamp = int(max(1, min(K.ns, target_s / max(t1, 1e-3))))
+    t0 = time.perf_counter()
+    yc, xc = _cpu_step(C, m, d, 0, nsamp)
+    dt_s = time.perf_counter() - t0
+    full_s = dt_s * K.ns / nsamp
+    B = compulsory_bytes(K.ni, K.ns, K.nr, K.nt)
+    res = {"value": round(B / full_s / 1e9, 4), "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+           "sample": f"{nsamp} of {K.ns} sources ({nsamp * K.nr} of {K.nsnr} traces), forward+adjoint in "
+                     f"float64 with all host threads, {dt_s:.1f} s, scaled by {K.ns / nsamp:.1f} to one full step"}
+    return res, nsamp, yc, xc
+
+
+def _padded_wavelet(K):
+    from oracle.kirchhoff_oracle import pad_wavelet
+
+    return pad_wavelet(np.asarray(K.wav), K.wavcenter)
+
+
+def _cpu_step(C, m, d, s0, s1):
+    y = C.spread(m, s0, s1)
+    rows = slice(s0 * C.nr, s1 * C.nr)
+    yc = np.zeros_like(y)
+    yc[rows] = C.conv(y[rows])
+    dc = np.zeros((C.ns * C.nr, C.nt))
+    dc[rows] = C.conv(np.asarray(d, np.float64).reshape(-1, C.nt)[rows], adjoint=True)
+    x = C.gather(dc, s0, s1)
+    return yc, x
+
+
+# ---------------------------------------------------------------------------
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def build_operator(w):
+    from pylops_gb300.waveeqprocessing import Kirchhoff
+
+    t0 = time.perf_counter()
+    K = Kirchhoff(w["z"], w["x"], w["t"], w["srcs"], w["recs"], w["vel"], w["wav"], w["wc"], mode="eikonal",
+                  dynamic=True, angleaperture=60.0, engine="cuda", dtype="float32")
+    return K, time.perf_counter() - t0
+
+
+def run_gpu(args):
+    import torch
+
+    from pylops_gb300 import _native
+
+    rank, ws, dist = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    w = make_workload()
+    K, t_setup = build_operator(w)
+    L = _native.lib()
+    rng = np.random.default_rng(7)
+    m_host = w["refl"].ravel().astype(np.float32)
+    d_host = rng.standard_normal(K.nsnr * K.nt).astype(np.float32)
+    m = torch.as_tensor(m_host, device="cuda")
+    d = torch.as_tensor(d_host, device="cuda")
+    y = torch.empty(K.nsnr * K.nt, dtype=torch.float32, device="cuda")
+    dcorr = torch.empty_like(y)
+    img = torch.empty(K.ni, dtype=torch.float32, device="cuda")
+    h = K.native_handle
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step(evs=None):
+        if evs:
+            evs[0].record(stream)
+        _native.check(L.kgb_kirchhoff_forward(h, m.data_ptr(), y.data_ptr(), sp))
+        if evs:
+            evs[1].record(stream)
+        _native.check(L.kgb_kirchhoff_wavelet(h, d.data_ptr(), dcorr.data_ptr(), 1, sp))
+        if evs:
+            evs[2].record(stream)
+        _native.check(L.kgb_kirchhoff_gather(h, dcorr.data_ptr(), img.data_ptr(), sp))
+        if evs:
+            evs[3].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(events[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    fwd_ms = [e[0].elapsed_time(e[1]) for e in events]
+    cor_ms = [e[1].elapsed_time(e[2]) for e in events]
+    gat_ms = [e[2].elapsed_time(e[3]) for e in events]
+    ms_step = total_ms / args.steps
+    if dist:
+        tt = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_step = float(tt.item())
+
+    y_dev = y.cpu().numpy().astype(np.float64)
+
+    # e2e: public API, host numpy buffers (pinned), copies inside the timed region
+    m_pin = torch.empty(K.ni, dtype=torch.float32, pin_memory=True).numpy()
+    d_pin = torch.empty(K.nsnr * K.nt, dtype=torch.float32, pin_memory=True).numpy()
+    m_pin[:] = m_host
+    d_pin[:] = d_host
+    for _ in range(max(1, args.warmup)):
+        K @ m_pin
+        K.H @ d_pin
+    torch.cuda.synchronize()
+    te = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        yy = K @ m_pin
+        xx = K.H @ d_pin
+        te.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(te)
+    del yy
+
+    B = compulsory_bytes(K.ni, K.ns, K.nr, K.nt)
+    ngpu = ws
+    value = ngpu * B / (ms_step * 1e-3) / 1e9
+    peaks = _peaks()
+    hbm = peaks.get("hbm_gbs")
+    # dominant kernel: by measured time
+    kern = {"spread_fwd_wavelet": statistics.median(fwd_ms), "wavelet_correlate": statistics.median(cor_ms),
+            "gather_adj": statistics.median(gat_ms)}
+    top = max(kern, key=kern.get)
+    tab = 12 * K.ni * (K.ns + K.nr)
+    algo = {"spread_fwd_wavelet": tab + 8 * K.ni + 4 * K.nsnr * K.nt,
+            "wavelet_correlate": 8 * K.nsnr * K.nt,
+            "gather_adj": tab + 8 * K.ni + 4 * K.nsnr * K.nt}
+    achieved = algo[top] / (kern[top] * 1e-3) / 1e9
+    pairs = K.ni * K.nsnr
+    out = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": "GB/s",
+        "n_gpus": ngpu,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded eikonal velocity with Gaussian anomalies, random-dip layers + spikes)",
+        "config": {"workload": WORKLOAD, "mode": "eikonal", "dynamic": True, "angleaperture_deg": 60,
+                   "grid": [800, 300], "spacing_m": 5.0, "ns": K.ns, "nr": K.nr, "nt": K.nt, "dt": K.dt,
+                   "wavelet_taps": int(len(K.wav)), "l2": "inputs larger than L2 (tables 1.34 GB, data 154 MB)",
+                   "setup_s": round(t_setup, 2)},
+        "traces_per_s": round(ngpu * K.nsnr / (ms_step * 1e-3), 1),
+        "pair_points_per_s": float(f"{ngpu * 2 * pairs / (ms_step * 1e-3):.4e}"),
+        "hbm_fraction": round(value / hbm, 5) if hbm else None,
+        "kernels_ms": {k: round(v, 4) for k, v in kern.items()},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": hbm,
+                     "unit": "GB/s", "frac": round(achieved / hbm, 5) if hbm else None,
+                     "traffic": None, "peak_source": "measured" if hbm else "fallback",
+                     "note": "compulsory bytes / launch time; the kernel is issue/gather bound, not HBM bound"},
+        "gpu_launches": args.steps * (3 + (1 if _gather_split(K.ni) else 0)),
+        "clocks": clk,
+        "e2e": {"value": round(B / e2e_s / 1e9, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": int(4 * K.ni + 4 * K.nsnr * K.nt),
+                "d2h_bytes_per_step": int(4 * K.nsnr * K.nt + 4 * K.ni),
+                "ms_per_step": round(e2e_s * 1e3, 3)},
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cb, nsamp, yc, xc = cpu_baseline(K, m_host.astype(np.float64), d_host, target_s=args.cpu_seconds)
+        out["cpu_baseline"] = cb
+        rows = nsamp * K.nr
+        d_mask = d_host.copy()
+        d_mask[rows * K.nt:] = 0.0
+        x_mask = K.H @ d_mask
+        out["parity"] = {
+            "oracle": "float64 C restatement of the numba loop nest, identical tables",
+            "sample_sources": nsamp,
+            "forward_rel_l2": float(np.linalg.norm(y_dev[:rows * K.nt] - yc[:rows].ravel())
+                                    / np.linalg.norm(yc[:rows])),
+            "adjoint_rel_l2": float(np.linalg.norm(x_mask - xc) / np.linalg.norm(xc)),
+        }
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def _gather_split(ni):
+    """Whether the gather launches its partial-sum pass (fewer than 304
+    blocks of 256 image points)."""
+    return (ni + 255) // 256 < 304
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def run_reference(args):
+    """Reference arm: the C restatement of the numba CPU engine on all host
+    threads, on a bounded sample of the same workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.kirch_oracle_c import COracle, build
+    from oracle.kirchhoff_oracle import pad_wavelet
+
+    build()
+    w = make_workload()
+    # tables exactly as the GPU arm builds them (the package's eikonal solver)
+    K = _HostTables(w)
+    C = COracle(K, pad_wavelet(w["wav"], w["wc"]))
+    m = w["refl"].ravel()
+    d = np.random.default_rng(7).standard_normal(K.nsnr * K.nt)
+    nsamp = max(1, int(args.ref_sources))
+    for _ in range(args.warmup):
+        _cpu_step(C, m, d, 0, 1)
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _cpu_step(C, m, d, 0, nsamp)
+        ts.append(time.perf_counter() - t0)
+    full_s = statistics.median(ts) * K.ns / nsamp
+    B = compulsory_bytes(K.ni, K.ns, K.nr, K.nt)
+    v = B / full_s / 1e9
+    sample = (f"{nsamp} of {K.ns} sources per step (forward+adjoint, float64), scaled by {K.ns / nsamp:.1f} "
+              "to one full step")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GB/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(full_s * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD},
+        "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 4), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+class _HostTables:
+    """Reference-layout tables of the workload, built on the host with the
+    package's table builder (no GPU needed)."""
+
+    def __init__(self, w):
+        from pylops_gb300.waveeqprocessing.kirchhoff import Kirchhoff
+
+        z, x = w["z"], w["x"]
+        ts, tr, ds, dr, gs, gr = Kirchhoff._traveltime_table(z, x, w["srcs"], w["recs"], w["vel"], mode="eikonal")
+        self.trav_srcs, self.trav_recs = ts, tr
+        maxdist = 1e-2 * (ds.max() + dr.max())
+        self.amp_srcs, self.amp_recs = 1 / np.sqrt(ds + maxdist), 1 / np.sqrt(dr + maxdist)
+        self.ns, self.nr, self.nt, self.nz = w["ns"], w["nr"], w["nt"], w["nz"]
+        self.ni = w["nx"] * w["nz"]
+        self.nsnr = self.ns * self.nr
+        self.angle_srcs = np.arctan2(gs[0], gs[1]).reshape(self.ni, self.ns)
+        self.angle_recs = np.arctan2(gr[0], gr[1]).reshape(self.ni, self.nr)
+        self.dt = w["t"][1] - w["t"][0]
+        self.dynamic = True
+        self.vel = w["vel"].ravel()
+        from pylops_gb300.utils.tapers import taper
+
+        self.aperturetap = taper(41, 20, "hanning")[20:]
+        self.aperture = np.array([0.8 * (w["nx"] + 1), w["nx"] + 1.0])
+        self.angleaperture = np.deg2rad([0.8 * 60.0, 60.0])
+        dx = x[1] - x[0]
+        self.six = np.tile((w["srcs"][0] - x[0]) // dx, (self.nr, 1)).T.astype(int).ravel()
+        self.rix = np.tile((w["recs"][0] - x[0]) // dx, (self.ns, 1)).astype(int).ravel()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-sources", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,170 @@
+/*
+ * kirchhoff_gb300.h -- C ABI of the GB300-native Kirchhoff demigration /
+ * migration operator and of its least-squares solvers.
+ *
+ * Plain C: opaque handles, raw pointers and sizes, no framework types.
+ * Every entry point returns an int status (KGB_OK on success); the message
+ * of the last failure on the calling thread is kgb_last_error().
+ *
+ * Pointers named *_dev are CUDA device pointers (any allocator); pointers
+ * named *_host are host memory.  `stream` is a cudaStream_t passed as void*
+ * (NULL = the legacy default stream).  Device entry points are asynchronous
+ * with respect to the host; *_host entry points synchronise before returning.
+ *
+ * Reference interfaces (PyLops 2.5.0, paths inside the pylops project):
+ *   Kirchhoff.__init__              pylops/waveeqprocessing/kirchhoff.py:234-455
+ *   Kirchhoff._matvec / _rmatvec    pylops/waveeqprocessing/kirchhoff.py:1048-1143
+ *   _travsrcrec_kirch_(r)matvec     pylops/waveeqprocessing/kirchhoff.py:728-781
+ *   _ampsrcrec_kirch_(r)matvec      pylops/waveeqprocessing/kirchhoff.py:784-1001
+ *   _KirchhoffCudaHelper            pylops/waveeqprocessing/_kirchhoff_cuda.py:9-489
+ *   _Convolve1Dshort                pylops/signalprocessing/convolve1d.py:57-116
+ *   CGLS / LSQR                     pylops/optimization/cls_basic.py:334-1351
+ */
+#ifndef KIRCHHOFF_GB300_H
+#define KIRCHHOFF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (mapped to Python exceptions by the host wrapper) ---- */
+#define KGB_OK 0
+#define KGB_ERR_VALUE 1           /* ValueError: bad sizes, non-finite tables  */
+#define KGB_ERR_NOT_IMPLEMENTED 2 /* NotImplementedError                       */
+#define KGB_ERR_CUDA 3            /* RuntimeError: a CUDA call failed          */
+#define KGB_ERR_MEMORY 4          /* MemoryError: device allocation failed     */
+#define KGB_ERR_STATE 5           /* RuntimeError: tables missing, bad handle  */
+
+typedef struct kgb_kirchhoff kgb_kirchhoff; /* opaque operator handle */
+
+/* Library version (major*10000 + minor*100 + patch) and last error text. */
+int kgb_version(void);
+const char* kgb_last_error(void);
+
+/* Create an operator for ns sources, nr receivers, nt time samples of
+ * spacing dt and ni image points whose fastest axis is depth (nz samples):
+ * ii = ix*nz + iz in 2-D, (iy*nx + ix)*nz + iz in 3-D.  `wav` is the
+ * wavelet as given to the reference constructor and `wavcenter` its centre
+ * index; the filter is padded exactly as _Convolve1Dshort does
+ * (convolve1d.py:76-88).
+ * Replaces: Kirchhoff.__init__ (kirchhoff.py:234-455) for the sizes, the
+ * wavelet operator (kirchhoff.py:400-409) and the engine registration
+ * (kirchhoff.py:1003-1046). */
+int kgb_kirchhoff_create(kgb_kirchhoff** op, int ns, int nr, int nt, int64_t ni, int nz,
+                         double dt, int dynamic, const double* wav_host, int nwav,
+                         int wavcenter);
+int kgb_kirchhoff_destroy(kgb_kirchhoff* op);
+
+/* Upload traveltime tables in the reference layout: trav_srcs (ni, ns) and
+ * trav_recs (ni, nr), C order, float64 seconds.  They are stored on the
+ * device source-/receiver-major as 32-bit fixed-point sample counts.
+ * Replaces: the trav_srcs / trav_recs attributes (kirchhoff.py:310-343) and
+ * the per-call to_cupy copies (_kirchhoff_cuda.py:318-328). */
+int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* trav_srcs_host,
+                                  const double* trav_recs_host);
+
+/* Upload the dynamic-mode tables (reference layout, float64): amplitudes and
+ * angles (ni, ns) / (ni, nr), velocity (ni), aperture [min, max], angle
+ * aperture [min, max] in radians, the 21-sample aperture taper and the
+ * per-trace source/receiver x indices six, rix (ns*nr).  Angle tapers,
+ * cos/sin of half angles and amplitudes are folded into per-entry weights.
+ * Replaces: amp_*, angle_*, vel, aperture, angleaperture, aperturetap, six,
+ * rix (kirchhoff.py:287-330, 364-393, 411-439, 448-454). */
+int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_srcs_host,
+                              const double* amp_recs_host, const double* angle_srcs_host,
+                              const double* angle_recs_host, const double* vel_host,
+                              const double* aperture2_host, const double* angleaperture2_host,
+                              const double* aperturetap21_host, const int64_t* six_host,
+                              const int64_t* rix_host);
+
+/* Forward d = K m: spreading along traveltime curves then wavelet
+ * convolution.  m_dev (ni) float32, d_dev (ns*nr, nt) float32.
+ * Replaces: Kirchhoff._matvec (kirchhoff.py:1048-1094). */
+int kgb_kirchhoff_forward(kgb_kirchhoff* op, const float* m_dev, float* d_dev, void* stream);
+
+/* Adjoint m = K^H d: wavelet correlation then gathering.
+ * Replaces: Kirchhoff._rmatvec (kirchhoff.py:1096-1143). */
+int kgb_kirchhoff_adjoint(kgb_kirchhoff* op, const float* d_dev, float* m_dev, void* stream);
+
+/* Same as forward/adjoint with host buffers: the copies to and from the
+ * device happen inside the call, which returns after the result is on the
+ * host.  Replaces: _KirchhoffCudaHelper._matvec_cuda / _rmatvec_cuda
+ * (_kirchhoff_cuda.py:443-489) called with numpy arrays. */
+int kgb_kirchhoff_forward_host(kgb_kirchhoff* op, const float* m_host, float* d_host);
+int kgb_kirchhoff_adjoint_host(kgb_kirchhoff* op, const float* d_host, float* m_host);
+
+/* The two kernels without the wavelet: spreading only (into a zeroed
+ * (ns*nr, nt) trace array) and gathering only (from already-correlated data).
+ * Replace: the _kirch_matvec / _kirch_rmatvec kernels of
+ * kirchhoff.py:728-1001 as registered at kirchhoff.py:1039-1046. */
+int kgb_kirchhoff_spread(kgb_kirchhoff* op, const float* m_dev, float* d_dev, void* stream);
+int kgb_kirchhoff_gather(kgb_kirchhoff* op, const float* d_dev, float* m_dev, void* stream);
+
+/* Wavelet convolution (adjoint = 0) or correlation (adjoint = 1) of ntr
+ * traces of nt samples, 'same' mode with the operator's padded wavelet.
+ * Replaces: Kirchhoff.cop._matvec / _rmatvec (convolve1d.py:100-116). */
+int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x_dev, float* y_dev, int adjoint,
+                          void* stream);
+
+/* Introspection used by the host wrapper and the tests. */
+int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* sizes8);
+
+/* Deterministic float64 reductions of float32 vectors (fixed launch shape
+ * and summation tree, so the result is bit-identical run to run).
+ * out_dev receives one double.  Replace: the dot products and norms that
+ * CGLS/LSQR take with ncp.linalg.norm / .dot (cls_basic.py:497-564, 976-1136). */
+int kgb_dot_f64(const float* a_dev, const float* b_dev, int64_t n, double* out_dev, void* stream);
+
+/* ---- solvers: device-resident CGLS / LSQR ------------------------------
+ * The vectors live on the device in float32, every dot product, norm and
+ * scalar recurrence is float64 on the device, and one iteration (both
+ * operator applications included) is captured in a CUDA graph and replayed
+ * without host synchronisation; a device flag retires the remaining
+ * replays once the reference's stopping test fires.
+ * Replace: CGLS.setup/step/run/finalize (cls_basic.py:432-608) and
+ * LSQR.setup/step/run/finalize (cls_basic.py:835-1186). */
+typedef struct kgb_solver kgb_solver;
+
+/* kind: 0 = CGLS, 1 = LSQR.  The solver keeps a reference to op. */
+int kgb_solver_create(kgb_solver** s, kgb_kirchhoff* op, int kind);
+int kgb_solver_destroy(kgb_solver* s);
+
+/* Setup with data y (ns*nr*nt) and optional x0 (ni, may be NULL).  params:
+ * CGLS {damp, tol}; LSQR {damp, atol, btol, conlim}.  Replaces the setup
+ * methods (cls_basic.py:432-506, 835-985). */
+int kgb_solver_setup(kgb_solver* s, const float* y_dev, const float* x0_dev,
+                     const double* params, int nparams, void* stream);
+
+/* Run up to niter further iterations (replays of the captured iteration,
+ * use_graph = 0 launches the same kernels directly).  Replaces run()
+ * (cls_basic.py:570-608, 1138-1186). */
+int kgb_solver_run(kgb_solver* s, int niter, int use_graph, void* stream);
+
+/* Copy out the current model (ni floats, device) and the scalar state:
+ * out16 = {iiter, istop, r1norm, r2norm, anorm, acond, arnorm, xnorm,
+ *          var_scalar, kold, 0...}; cost_host receives iiter+1 values of the
+ * residual-norm history (may be NULL). */
+int kgb_solver_result(kgb_solver* s, float* x_dev, double* out16_host, double* cost_host,
+                      int cost_capacity, void* stream);
+
+/* ---- table builder ------------------------------------------------------
+ * First-arrival traveltimes (and, if dist_out != NULL, distances) from npts
+ * point sources by fast marching on a regular grid of ndim (2 or 3) axes
+ * `dims` (C order, depth fastest) with spacings `dsamp` and velocity
+ * `speed` (prod(dims) values).  pts holds npts x ndim grid indices.  Output
+ * tables are (prod(dims), npts) in C order, i.e. the reference's
+ * trav_srcs / dist_srcs layout.  One OpenMP thread per point source
+ * (nthreads <= 0: all host threads).
+ * Replaces: the skfmm.travel_time / skfmm.distance loop of
+ * Kirchhoff._traveltime_table (kirchhoff.py:609-638). */
+int kgb_eikonal_tables(int ndim, const int* dims, const double* dsamp, const double* speed, int npts,
+                       const int* pts, double* trav_out, double* dist_out, int order, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KIRCHHOFF_GB300_H */

@@ -1,0 +1,103 @@
+// Internal declarations shared by the CUDA translation units of
+// libpylops_gb300.so.  Not part of the public C ABI (include/kirchhoff_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/kirchhoff_gb300.h"
+
+namespace kgb {
+
+// Record the failure message for kgb_last_error() and return `code`.
+int set_error(int code, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+#define KGB_CUDA_TRY(call)                                   \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return ::kgb::cuda_error(_e, #call); \
+    } while (0)
+
+// Device view of one operator's tables, passed by value to the kernels.
+//
+// Layout in HBM (all source-/receiver-major so that a warp's 32 consecutive
+// image points read 128 contiguous bytes of one row):
+//   tsq[is][ii], trq[ir][ii]   int32  traveltime in samples, fixed point with
+//                                     frac_bits fractional bits
+//   wsc/wss[is][ii]            f32    A_s * tap_s * cos(a_s/2), ... * sin(a_s/2)
+//   wrc/wrs[ir][ii]            f32    same for receivers
+//   vscale[ii]                 f32    2 / v(ii)
+//   izmin[is*nr+ir]            int32  first depth index inside the offset aperture
+struct KirchDev {
+    int ns, nr, nt, nz;
+    int64_t ni;
+    int frac_bits;
+    const int32_t* tsq;
+    const int32_t* trq;
+    const float* wsc;
+    const float* wss;
+    const float* wrc;
+    const float* wrs;
+    const float* vscale;
+    const int32_t* izmin;
+};
+
+// Launchers (kirchhoff_kernels.cu).  All asynchronous on `stream`.
+int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,
+                  const float* h, int L, bool fuse_wavelet, cudaStream_t stream);
+int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, float* img,
+                  float* partial, int64_t partial_capacity, cudaStream_t stream);
+int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L,
+                   cudaStream_t stream);
+// How many float partial images launch_gather wants for this geometry.
+int64_t gather_partial_elems(const KirchDev& K);
+
+// Deterministic float64 reductions (solver.cu).
+int launch_dot_f64(const float* a, const float* b, int64_t n, double* out, double* block_scratch,
+                   cudaStream_t stream);
+int dot_scratch_doubles();
+
+}  // namespace kgb
+
+// The operator object behind the opaque C handle.
+struct kgb_kirchhoff {
+    int ns = 0, nr = 0, nt = 0, nz = 0;
+    int64_t ni = 0;
+    double dt = 0.0;
+    int dynamic = 0;
+    int frac_bits = 0;
+    int L = 0;                 // padded wavelet length
+    float* h_dev = nullptr;    // padded wavelet
+    float* hflip_dev = nullptr;// reversed padded wavelet (correlation)
+    int32_t* tsq = nullptr;
+    int32_t* trq = nullptr;
+    float* wsc = nullptr;
+    float* wss = nullptr;
+    float* wrc = nullptr;
+    float* wrs = nullptr;
+    float* vscale = nullptr;
+    int32_t* izmin = nullptr;
+    bool has_gate = false;
+    bool trav_ready = false;
+    bool dyn_ready = false;
+    float* dcorr = nullptr;    // scratch: correlated data for the adjoint
+    float* partial = nullptr;  // scratch: per-split partial images
+    int64_t partial_elems = 0;
+    float* m_stage = nullptr;  // device staging for the host-buffer entry points
+    float* d_stage = nullptr;
+    cudaStream_t stream = nullptr;  // used by the host-buffer entry points
+    int device = 0;
+
+    kgb::KirchDev view() const {
+        kgb::KirchDev K;
+        K.ns = ns; K.nr = nr; K.nt = nt; K.nz = nz; K.ni = ni; K.frac_bits = frac_bits;
+        K.tsq = tsq; K.trq = trq; K.wsc = wsc; K.wss = wss; K.wrc = wrc; K.wrs = wrs;
+        K.vscale = vscale; K.izmin = izmin;
+        return K;
+    }
+    int64_t npair() const { return (int64_t)ns * nr; }
+    int64_t ndata() const { return npair() * nt; }
+};

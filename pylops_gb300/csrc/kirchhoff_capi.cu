@@ -1,0 +1,364 @@
+// C ABI of the Kirchhoff operator (include/kirchhoff_gb300.h): handle
+// life cycle, table upload (quantisation to fixed point, folding of the
+// dynamic weights) and the apply entry points.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "kgb_internal.h"
+
+namespace kgb {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+    return set_error(e == cudaErrorMemoryAllocation ? KGB_ERR_MEMORY : KGB_ERR_CUDA, "%s: %s (%s)",
+                     what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+template <typename T>
+static int dev_alloc(T** p, size_t n, const char* what) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    if (n == 0) return KGB_OK;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_error(e, what);
+    }
+    return KGB_OK;
+}
+
+// numpy/CPython float floor division (npy_divmod), so that taper indices are
+// computed exactly as `a // b` is in the reference's loops.
+static double py_floordiv(double a, double b) {
+    if (b == 0.0) return a / b;
+    double mod = fmod(a, b);
+    double div = (a - mod) / b;
+    if (mod != 0.0) {
+        if ((b < 0) != (mod < 0)) div -= 1.0;
+    }
+    double fl;
+    if (div != 0.0) {
+        fl = floor(div);
+        if (div - fl > 0.5) fl += 1.0;
+    } else {
+        fl = copysign(0.0, a / b);
+    }
+    return fl;
+}
+
+// Fractional bits of the fixed-point traveltime: the largest F such that
+// every table entry and nt fit with headroom for the sum of two entries in
+// an int32 (|q| < 2^30), capped at 22.
+static int choose_frac_bits(double max_samples, int nt) {
+    auto bits_for = [](double v) {
+        int b = 0;
+        while (b < 62 && ldexp(1.0, b) < v) ++b;
+        return b;
+    };
+    int need = std::max(bits_for(max_samples + 2.0), bits_for((double)nt + 1.0));
+    return std::min(22, 30 - need);
+}
+
+}  // namespace kgb
+
+using namespace kgb;
+
+extern "C" {
+
+int kgb_version(void) { return 100; }
+
+const char* kgb_last_error(void) { return g_last_error.c_str(); }
+
+int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni, int nz, double dt,
+                         int dynamic, const double* wav, int nwav, int wavcenter) {
+    if (!out) return set_error(KGB_ERR_VALUE, "create: null output handle");
+    *out = nullptr;
+    if (ns <= 0 || nr <= 0 || nt < 2 || ni <= 0 || nz <= 0 || ni % nz != 0)
+        return set_error(KGB_ERR_VALUE, "create: bad sizes ns=%d nr=%d nt=%d ni=%lld nz=%d", ns, nr, nt,
+                         (long long)ni, nz);
+    if (!(dt > 0.0) || !isfinite(dt)) return set_error(KGB_ERR_VALUE, "create: dt must be positive");
+    if (!wav || nwav <= 0) return set_error(KGB_ERR_VALUE, "create: empty wavelet");
+    if (wavcenter > nwav - 1 || wavcenter < 0)
+        return set_error(KGB_ERR_VALUE, "offset must be smaller than h.shape[axis] - 1");
+    if ((int64_t)ns * nr * (int64_t)nt > ((int64_t)1 << 40))
+        return set_error(KGB_ERR_VALUE, "create: data volume too large");
+    // filter padding of _Convolve1Dshort (convolve1d.py:76-88)
+    int off = 2 * (nwav / 2 - wavcenter);
+    if (nwav % 2 == 0) off -= 1;
+    const int padl = std::max(off, 0), padr = -std::min(off, 0);
+    std::vector<float> h(nwav + padl + padr, 0.f);
+    for (int k = 0; k < nwav; ++k) h[padl + k] = (float)wav[k];
+    std::vector<float> hf(h.rbegin(), h.rend());
+
+    kgb_kirchhoff* op = new kgb_kirchhoff();
+    op->ns = ns; op->nr = nr; op->nt = nt; op->ni = ni; op->nz = nz; op->dt = dt;
+    op->dynamic = dynamic ? 1 : 0;
+    op->L = (int)h.size();
+    int rc = KGB_OK;
+    cudaGetDevice(&op->device);
+    do {
+        if ((rc = dev_alloc(&op->h_dev, h.size(), "alloc wavelet"))) break;
+        if ((rc = dev_alloc(&op->hflip_dev, h.size(), "alloc wavelet"))) break;
+        cudaError_t e = cudaMemcpy(op->h_dev, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { rc = cuda_error(e, "upload wavelet"); break; }
+        e = cudaMemcpy(op->hflip_dev, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { rc = cuda_error(e, "upload wavelet"); break; }
+        if ((rc = dev_alloc(&op->tsq, (size_t)ns * ni, "alloc source traveltimes"))) break;
+        if ((rc = dev_alloc(&op->trq, (size_t)nr * ni, "alloc receiver traveltimes"))) break;
+        if ((rc = dev_alloc(&op->dcorr, (size_t)op->ndata(), "alloc correlation scratch"))) break;
+        op->partial_elems = gather_partial_elems(op->view());
+        if ((rc = dev_alloc(&op->partial, (size_t)op->partial_elems, "alloc partial images"))) break;
+        e = cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { rc = cuda_error(e, "create stream"); break; }
+    } while (0);
+    if (rc != KGB_OK) {
+        kgb_kirchhoff_destroy(op);
+        return rc;
+    }
+    *out = op;
+    return KGB_OK;
+}
+
+int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
+    if (!op) return KGB_OK;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaSetDevice(op->device);
+    void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
+                    op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (op->stream) cudaStreamDestroy(op->stream);
+    cudaSetDevice(dev);
+    delete op;
+    return KGB_OK;
+}
+
+int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* ts, const double* tr) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (!ts || !tr) return set_error(KGB_ERR_VALUE, "set_traveltimes: null table");
+    const int64_t ni = op->ni;
+    const double inv_dt = 1.0 / op->dt;
+    double maxs = 0.0;
+    int64_t bad = -1;
+    const int64_t n_s = ni * op->ns, n_r = ni * op->nr;
+#pragma omp parallel for reduction(max : maxs) reduction(max : bad)
+    for (int64_t k = 0; k < n_s + n_r; ++k) {
+        const double v = fabs((k < n_s ? ts[k] : tr[k - n_s]) * inv_dt);
+        if (!isfinite(v)) bad = std::max(bad, k);
+        else maxs = std::max(maxs, v);
+    }
+    if (bad >= 0)
+        return set_error(KGB_ERR_VALUE, "set_traveltimes: non-finite traveltime at flat index %lld", (long long)bad);
+    const int F = choose_frac_bits(maxs, op->nt);
+    if (F < 8)
+        return set_error(KGB_ERR_VALUE, "set_traveltimes: traveltimes up to %.3g samples exceed the 32-bit fixed-point range", maxs);
+    const double scale = ldexp(1.0, F);
+    // transpose (ni, n) -> (n, ni) while quantising, in cache-sized blocks
+    auto quantise = [&](const double* src, int n, std::vector<int32_t>& dst) {
+        dst.resize((size_t)n * ni);
+        const int64_t B = 64;
+#pragma omp parallel for schedule(static)
+        for (int64_t i0 = 0; i0 < ni; i0 += B)
+            for (int j0 = 0; j0 < n; j0 += (int)B)
+                for (int64_t i = i0; i < std::min(ni, i0 + B); ++i)
+                    for (int j = j0; j < std::min(n, j0 + (int)B); ++j)
+                        dst[(size_t)j * ni + i] = (int32_t)llrint(src[(size_t)i * n + j] * inv_dt * scale);
+    };
+    std::vector<int32_t> qs, qr;
+    quantise(ts, op->ns, qs);
+    quantise(tr, op->nr, qr);
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    KGB_CUDA_TRY(cudaMemcpy(op->tsq, qs.data(), qs.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    KGB_CUDA_TRY(cudaMemcpy(op->trq, qr.data(), qr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    op->frac_bits = F;
+    op->trav_ready = true;
+    return KGB_OK;
+}
+
+int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const double* amp_r,
+                              const double* ang_s, const double* ang_r, const double* vel,
+                              const double* aperture2, const double* angleaperture2,
+                              const double* taper21, const int64_t* six, const int64_t* rix) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (!op->dynamic) return set_error(KGB_ERR_STATE, "set_dynamic: operator was created kinematic");
+    if (!amp_s || !amp_r || !ang_s || !ang_r || !vel || !aperture2 || !angleaperture2 || !taper21 || !six || !rix)
+        return set_error(KGB_ERR_VALUE, "set_dynamic: null table");
+    if (taper21[0] != 1.0)
+        return set_error(KGB_ERR_VALUE, "set_dynamic: aperture taper must start at 1 (taper(41, 20, 'hanning')[20:])");
+    const int64_t ni = op->ni;
+    const double amin = angleaperture2[0], amax = angleaperture2[1];
+    const double dang = amax - amin;
+    // angle taper of kirchhoff.py:845-864, folded per table entry; entries
+    // outside the angle aperture get weight 0, which rejects the pair-point
+    // exactly as the reference's `abs_angle < angleaperturemax` test does.
+    auto fold = [&](const double* amp, const double* ang, int n, std::vector<float>& wc, std::vector<float>& ws) {
+        wc.resize((size_t)n * ni);
+        ws.resize((size_t)n * ni);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < ni; ++i) {
+            for (int j = 0; j < n; ++j) {
+                const double a = ang[(size_t)i * n + j];
+                const double A = amp[(size_t)i * n + j];
+                const double aa = fabs(a);
+                double tap = 0.0;
+                if (aa < amax) {
+                    tap = 1.0;
+                    if (aa >= amin) {
+                        double q = py_floordiv(20.0 * (aa - amin), dang);
+                        long idx = (long)q;
+                        if (idx < 0) idx = 0;
+                        if (idx > 20) idx = 20;
+                        tap = taper21[idx];
+                    }
+                }
+                const double base = A * tap;
+                wc[(size_t)j * ni + i] = (float)(base * cos(a / 2.0));
+                ws[(size_t)j * ni + i] = (float)(base * sin(a / 2.0));
+            }
+        }
+    };
+    std::vector<float> wsc, wss, wrc, wrs;
+    fold(amp_s, ang_s, op->ns, wsc, wss);
+    fold(amp_r, ang_r, op->nr, wrc, wrs);
+    std::vector<float> vs(ni);
+    for (int64_t i = 0; i < ni; ++i) vs[i] = (float)(2.0 / vel[i]);
+    // offset aperture (kirchhoff.py:866-880): |six-rix|/(iz+1) < apmax, which
+    // holds from the first passing depth downwards; inside it the reference's
+    // taper index is 0 and taper[0] == 1, so only this cut-off acts.
+    const double apmax = aperture2[1];
+    const int64_t npair = op->npair();
+    std::vector<int32_t> izmin(npair);
+    bool gate = false;
+    for (int64_t p = 0; p < npair; ++p) {
+        const double off = fabs((double)(six[p] - rix[p]));
+        int iz = 0;
+        while (iz < op->nz && !(off / (double)(iz + 1) < apmax)) ++iz;
+        izmin[p] = iz;
+        gate = gate || iz > 0;
+    }
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    int rc;
+    if ((rc = dev_alloc(&op->wsc, wsc.size(), "alloc weights"))) return rc;
+    if ((rc = dev_alloc(&op->wss, wss.size(), "alloc weights"))) return rc;
+    if ((rc = dev_alloc(&op->wrc, wrc.size(), "alloc weights"))) return rc;
+    if ((rc = dev_alloc(&op->wrs, wrs.size(), "alloc weights"))) return rc;
+    if ((rc = dev_alloc(&op->vscale, vs.size(), "alloc velocity"))) return rc;
+    if ((rc = dev_alloc(&op->izmin, izmin.size(), "alloc aperture"))) return rc;
+    KGB_CUDA_TRY(cudaMemcpy(op->wsc, wsc.data(), wsc.size() * 4, cudaMemcpyHostToDevice));
+    KGB_CUDA_TRY(cudaMemcpy(op->wss, wss.data(), wss.size() * 4, cudaMemcpyHostToDevice));
+    KGB_CUDA_TRY(cudaMemcpy(op->wrc, wrc.data(), wrc.size() * 4, cudaMemcpyHostToDevice));
+    KGB_CUDA_TRY(cudaMemcpy(op->wrs, wrs.data(), wrs.size() * 4, cudaMemcpyHostToDevice));
+    KGB_CUDA_TRY(cudaMemcpy(op->vscale, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice));
+    KGB_CUDA_TRY(cudaMemcpy(op->izmin, izmin.data(), izmin.size() * 4, cudaMemcpyHostToDevice));
+    op->has_gate = gate;
+    op->dyn_ready = true;
+    return KGB_OK;
+}
+
+static int check_ready(const kgb_kirchhoff* op) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (!op->trav_ready) return set_error(KGB_ERR_STATE, "traveltime tables not set");
+    if (op->dynamic && !op->dyn_ready) return set_error(KGB_ERR_STATE, "dynamic tables not set");
+    return KGB_OK;
+}
+
+int kgb_kirchhoff_spread(kgb_kirchhoff* op, const float* m, float* d, void* stream) {
+    int rc = check_ready(op);
+    if (rc) return rc;
+    if (!m || !d) return set_error(KGB_ERR_VALUE, "spread: null pointer");
+    return launch_spread(op->view(), op->dynamic, op->has_gate, m, d, nullptr, 0, false, (cudaStream_t)stream);
+}
+
+int kgb_kirchhoff_forward(kgb_kirchhoff* op, const float* m, float* d, void* stream) {
+    int rc = check_ready(op);
+    if (rc) return rc;
+    if (!m || !d) return set_error(KGB_ERR_VALUE, "forward: null pointer");
+    return launch_spread(op->view(), op->dynamic, op->has_gate, m, d, op->h_dev, op->L, true, (cudaStream_t)stream);
+}
+
+int kgb_kirchhoff_gather(kgb_kirchhoff* op, const float* d, float* m, void* stream) {
+    int rc = check_ready(op);
+    if (rc) return rc;
+    if (!m || !d) return set_error(KGB_ERR_VALUE, "gather: null pointer");
+    return launch_gather(op->view(), op->dynamic, op->has_gate, d, m, op->partial, op->partial_elems,
+                         (cudaStream_t)stream);
+}
+
+int kgb_kirchhoff_adjoint(kgb_kirchhoff* op, const float* d, float* m, void* stream) {
+    int rc = check_ready(op);
+    if (rc) return rc;
+    if (!m || !d) return set_error(KGB_ERR_VALUE, "adjoint: null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = launch_wavelet(d, op->dcorr, op->npair(), op->nt, op->hflip_dev, op->L, s))) return rc;
+    return launch_gather(op->view(), op->dynamic, op->has_gate, op->dcorr, m, op->partial, op->partial_elems, s);
+}
+
+int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x, float* y, int adjoint, void* stream) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (!x || !y) return set_error(KGB_ERR_VALUE, "wavelet: null pointer");
+    return launch_wavelet(x, y, op->npair(), op->nt, adjoint ? op->hflip_dev : op->h_dev, op->L,
+                          (cudaStream_t)stream);
+}
+
+static int ensure_stage(kgb_kirchhoff* op) {
+    int rc;
+    if (!op->m_stage && (rc = dev_alloc(&op->m_stage, (size_t)op->ni, "alloc model staging"))) return rc;
+    if (!op->d_stage && (rc = dev_alloc(&op->d_stage, (size_t)op->ndata(), "alloc data staging"))) return rc;
+    return KGB_OK;
+}
+
+int kgb_kirchhoff_forward_host(kgb_kirchhoff* op, const float* m_host, float* d_host) {
+    int rc = check_ready(op);
+    if (rc) return rc;
+    if (!m_host || !d_host) return set_error(KGB_ERR_VALUE, "forward_host: null pointer");
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    if ((rc = ensure_stage(op))) return rc;
+    KGB_CUDA_TRY(cudaMemcpyAsync(op->m_stage, m_host, (size_t)op->ni * 4, cudaMemcpyHostToDevice, op->stream));
+    if ((rc = kgb_kirchhoff_forward(op, op->m_stage, op->d_stage, op->stream))) return rc;
+    KGB_CUDA_TRY(cudaMemcpyAsync(d_host, op->d_stage, (size_t)op->ndata() * 4, cudaMemcpyDeviceToHost, op->stream));
+    KGB_CUDA_TRY(cudaStreamSynchronize(op->stream));
+    return KGB_OK;
+}
+
+int kgb_kirchhoff_adjoint_host(kgb_kirchhoff* op, const float* d_host, float* m_host) {
+    int rc = check_ready(op);
+    if (rc) return rc;
+    if (!m_host || !d_host) return set_error(KGB_ERR_VALUE, "adjoint_host: null pointer");
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    if ((rc = ensure_stage(op))) return rc;
+    KGB_CUDA_TRY(cudaMemcpyAsync(op->d_stage, d_host, (size_t)op->ndata() * 4, cudaMemcpyHostToDevice, op->stream));
+    if ((rc = kgb_kirchhoff_adjoint(op, op->d_stage, op->m_stage, op->stream))) return rc;
+    KGB_CUDA_TRY(cudaMemcpyAsync(m_host, op->m_stage, (size_t)op->ni * 4, cudaMemcpyDeviceToHost, op->stream));
+    KGB_CUDA_TRY(cudaStreamSynchronize(op->stream));
+    return KGB_OK;
+}
+
+int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
+    if (!op || !s) return set_error(KGB_ERR_VALUE, "info: null pointer");
+    s[0] = op->ns; s[1] = op->nr; s[2] = op->nt; s[3] = op->ni;
+    s[4] = op->frac_bits; s[5] = op->L; s[6] = op->has_gate ? 1 : 0; s[7] = op->dynamic;
+    return KGB_OK;
+}
+
+}  // extern "C"

@@ -112,3 +112,18 @@ def test_traveltime_known_answer():
     ts, tr, ds, dr, _, _ = ko.traveltime_table_analytic(np.arange(0, 200, 1), np.arange(0, 200, 1), src, src, 500.0)
     assert ts[0, 0] == 100 / 500.0 == float(g["trav00"])
     assert ds[0, 0] + dr[0, 0] == 200 == float(g["dist00"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_c_oracle_matches_reference(name):
+    """The OpenMP C restatement against the same golden vectors."""
+    from oracle.kirch_oracle_c import COracle
+
+    g = load(name)
+    K = build(g)
+    C = COracle(K, K.h)
+    tol = 1e-6 if g["adj"].dtype == np.float32 else 1e-11
+    assert rel(C.spread(g["m_in"]), g["spread"]) < max(tol, 1e-12)
+    assert rel(C.gather(g["d_in"]), g["gather"]) < max(tol, 1e-12)
+    assert rel(C.matvec(g["m_in"]), g["fwd"]) < tol
+    assert rel(C.rmatvec(g["d_in"]), g["adj"]) < tol
