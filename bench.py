@@ -209,7 +209,9 @@ def run_gpu(args):
     K, t_setup = build_operator(w)
     L = _native.lib()
     rng = np.random.default_rng(7)
-    m_host = w["refl"].ravel().astype(np.float32)
+    # dense model and data (an LSQR iterate is dense; a sparse reflectivity
+    # would let the forward skip zero image points)
+    m_host = rng.standard_normal(K.ni).astype(np.float32)
     d_host = rng.standard_normal(K.nsnr * K.nt).astype(np.float32)
     m = torch.as_tensor(m_host, device="cuda")
     d = torch.as_tensor(d_host, device="cuda")
@@ -233,6 +235,21 @@ def run_gpu(args):
         if evs:
             evs[3].record(stream)
 
+    # forward-kernel variants, timed on this workload; the fastest is used
+    variant_ms = {}
+    for v in (0, 1, 2):
+        K.set_spread_variant(v)
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            _native.check(L.kgb_kirchhoff_forward(h, m.data_ptr(), y.data_ptr(), sp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        variant_ms[v] = e0.elapsed_time(e1) / 2
+    best = min(variant_ms, key=variant_ms.get)
+    K.set_spread_variant(best)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -308,7 +325,7 @@ def run_gpu(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded eikonal velocity with Gaussian anomalies, random-dip layers + spikes)",
+        "data": "synthetic (seeded eikonal velocity with Gaussian anomalies; dense N(0,1) model and data vectors)",
         "config": {"workload": WORKLOAD, "mode": "eikonal", "dynamic": True, "angleaperture_deg": 60,
                    "grid": [800, 300], "spacing_m": 5.0, "ns": K.ns, "nr": K.nr, "nt": K.nt, "dt": K.dt,
                    "wavelet_taps": int(len(K.wav)), "l2": "inputs larger than L2 (tables 1.34 GB, data 154 MB)",
@@ -317,11 +334,13 @@ def run_gpu(args):
         "pair_points_per_s": float(f"{ngpu * 2 * pairs / (ms_step * 1e-3):.4e}"),
         "hbm_fraction": round(value / hbm, 5) if hbm else None,
         "kernels_ms": {k: round(v, 4) for k, v in kern.items()},
+        "spread_variant_ms": {str(k): round(v, 3) for k, v in variant_ms.items()},
+        "spread_variant": best,
         "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": hbm,
                      "unit": "GB/s", "frac": round(achieved / hbm, 5) if hbm else None,
                      "traffic": None, "peak_source": "measured" if hbm else "fallback",
                      "note": "compulsory bytes / launch time; the kernel is issue/gather bound, not HBM bound"},
-        "gpu_launches": args.steps * (3 + (1 if _gather_split(K.ni) else 0)),
+        "gpu_launches": args.steps * (K.info()["kernels_forward"] + 1 + K.info()["kernels_adjoint"] - 1),
         "clocks": clk,
         "e2e": {"value": round(B / e2e_s / 1e9, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": int(4 * K.ni + 4 * K.nsnr * K.nt),
@@ -348,10 +367,6 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def _gather_split(ni):
-    """Whether the gather launches its partial-sum pass (fewer than 304
-    blocks of 256 image points)."""
-    return (ni + 255) // 256 < 304
 
 
 def _peaks():
@@ -376,8 +391,9 @@ def run_reference(args):
     # tables exactly as the GPU arm builds them (the package's eikonal solver)
     K = _HostTables(w)
     C = COracle(K, pad_wavelet(w["wav"], w["wc"]))
-    m = w["refl"].ravel()
-    d = np.random.default_rng(7).standard_normal(K.nsnr * K.nt)
+    rng = np.random.default_rng(7)
+    m = rng.standard_normal(K.ni)
+    d = rng.standard_normal(K.nsnr * K.nt)
     nsamp = max(1, int(args.ref_sources))
     for _ in range(args.warmup):
         _cpu_step(C, m, d, 0, 1)

@@ -109,8 +109,20 @@ int kgb_kirchhoff_gather(kgb_kirchhoff* op, const float* d_dev, float* m_dev, vo
 int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x_dev, float* y_dev, int adjoint,
                           void* stream);
 
-/* Introspection used by the host wrapper and the tests. */
-int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* sizes8);
+/* Choose the forward (spreading) kernel: 0 = 64-bit fixed-point shared-
+ * memory accumulation, 1 = warp-binned (one trace per warp, the default),
+ * 2 = warp-binned with two traces per warp.  All three are deterministic and
+ * give the same result up to float32 rounding.  No reference counterpart
+ * (the reference has one CUDA kernel per mode, _kirchhoff_cuda.py:55-298);
+ * used by the tile autotuner. */
+int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant);
+
+/* Introspection used by the host wrapper and the tests.  info16 receives
+ * {ns, nr, nt, ni, fixed-point fraction bits, padded wavelet length,
+ *  offset-aperture gate active, dynamic, all times non-negative,
+ *  adjoint source splits, kernels per forward, kernels per adjoint,
+ *  spread variant, 0...}. */
+int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* info16);
 
 /* Deterministic float64 reductions of float32 vectors (fixed launch shape
  * and summation tree, so the result is bit-identical run to run).

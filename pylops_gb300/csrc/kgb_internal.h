@@ -35,6 +35,11 @@ struct KirchDev {
     int ns, nr, nt, nz;
     int64_t ni;
     int frac_bits;
+    int nonneg;        // every ts + tr >= 0: index math without the negative-time case
+    float wmax;        // bound on |dynamic weight| (1 for kinematic), for the fixed-point scale
+    int spread_variant; // 0: 64-bit fixed-point atomics; 1/2: warp-binned, 1/2 traces per warp
+    float* mv;         // scratch: m * 2/v per application (ni)
+    unsigned* absmax;  // scratch: bits of max |mv| per application
     const int32_t* tsq;
     const int32_t* trq;
     const float* wsc;
@@ -50,10 +55,14 @@ int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, fl
                   const float* h, int L, bool fuse_wavelet, cudaStream_t stream);
 int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, float* img,
                   float* partial, int64_t partial_capacity, cudaStream_t stream);
+// Set the kernels' shared-memory attributes once, outside any stream capture.
+int prepare_kernels(const KirchDev& K, int L);
 int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L,
                    cudaStream_t stream);
-// How many float partial images launch_gather wants for this geometry.
+// How many float partial images launch_gather may use, and how many source
+// splits (partial images) it launches for this geometry.
 int64_t gather_partial_elems(const KirchDev& K);
+int gather_nsplit(const KirchDev& K, bool dynamic, bool gate);
 
 // Deterministic float64 reductions (solver.cu).
 int launch_dot_f64(const float* a, const float* b, int64_t n, double* out, double* block_scratch,
@@ -81,6 +90,11 @@ struct kgb_kirchhoff {
     float* vscale = nullptr;
     int32_t* izmin = nullptr;
     bool has_gate = false;
+    bool nonneg = true;
+    float wmax = 1.f;
+    int spread_variant = 1;
+    float* mv = nullptr;
+    unsigned* absmax = nullptr;
     bool trav_ready = false;
     bool dyn_ready = false;
     float* dcorr = nullptr;    // scratch: correlated data for the adjoint
@@ -96,6 +110,8 @@ struct kgb_kirchhoff {
         K.ns = ns; K.nr = nr; K.nt = nt; K.nz = nz; K.ni = ni; K.frac_bits = frac_bits;
         K.tsq = tsq; K.trq = trq; K.wsc = wsc; K.wss = wss; K.wrc = wrc; K.wrs = wrs;
         K.vscale = vscale; K.izmin = izmin;
+        K.nonneg = nonneg ? 1 : 0; K.wmax = wmax; K.mv = mv; K.absmax = absmax;
+        K.spread_variant = spread_variant;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

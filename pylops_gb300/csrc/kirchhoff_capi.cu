@@ -128,6 +128,9 @@ int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni
         if ((rc = dev_alloc(&op->dcorr, (size_t)op->ndata(), "alloc correlation scratch"))) break;
         op->partial_elems = gather_partial_elems(op->view());
         if ((rc = dev_alloc(&op->partial, (size_t)op->partial_elems, "alloc partial images"))) break;
+        if ((rc = dev_alloc(&op->mv, (size_t)ni, "alloc scaled model"))) break;
+        if ((rc = dev_alloc(&op->absmax, 1, "alloc model maximum"))) break;
+        if ((rc = prepare_kernels(op->view(), op->L))) break;
         e = cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) { rc = cuda_error(e, "create stream"); break; }
     } while (0);
@@ -145,7 +148,8 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     cudaGetDevice(&dev);
     cudaSetDevice(op->device);
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
-                    op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage};
+                    op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
+                    op->mv, op->absmax};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);
@@ -159,14 +163,17 @@ int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* ts, const dou
     if (!ts || !tr) return set_error(KGB_ERR_VALUE, "set_traveltimes: null table");
     const int64_t ni = op->ni;
     const double inv_dt = 1.0 / op->dt;
-    double maxs = 0.0;
+    double maxs = 0.0, mins = INFINITY, minr = INFINITY;
     int64_t bad = -1;
     const int64_t n_s = ni * op->ns, n_r = ni * op->nr;
-#pragma omp parallel for reduction(max : maxs) reduction(max : bad)
+#pragma omp parallel for reduction(max : maxs) reduction(max : bad) reduction(min : mins) reduction(min : minr)
     for (int64_t k = 0; k < n_s + n_r; ++k) {
-        const double v = fabs((k < n_s ? ts[k] : tr[k - n_s]) * inv_dt);
+        const double t = (k < n_s ? ts[k] : tr[k - n_s]) * inv_dt;
+        const double v = fabs(t);
         if (!isfinite(v)) bad = std::max(bad, k);
         else maxs = std::max(maxs, v);
+        if (k < n_s) mins = std::min(mins, t);
+        else minr = std::min(minr, t);
     }
     if (bad >= 0)
         return set_error(KGB_ERR_VALUE, "set_traveltimes: non-finite traveltime at flat index %lld", (long long)bad);
@@ -192,6 +199,13 @@ int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* ts, const dou
     KGB_CUDA_TRY(cudaMemcpy(op->tsq, qs.data(), qs.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     KGB_CUDA_TRY(cudaMemcpy(op->trq, qr.data(), qr.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     op->frac_bits = F;
+    // every ts + tr >= 0 (after quantisation): the kernels may skip the
+    // reference's negative-time case (-1 < t/dt < 0 -> it = 0, w < 0)
+    int32_t qmin_s = INT32_MAX, qmin_r = INT32_MAX;
+    for (int32_t q : qs) qmin_s = std::min(qmin_s, q);
+    for (int32_t q : qr) qmin_r = std::min(qmin_r, q);
+    op->nonneg = (int64_t)qmin_s + (int64_t)qmin_r >= 0;
+    (void)mins; (void)minr;
     op->trav_ready = true;
     return KGB_OK;
 }
@@ -243,6 +257,15 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const doub
     fold(amp_r, ang_r, op->nr, wrc, wrs);
     std::vector<float> vs(ni);
     for (int64_t i = 0; i < ni; ++i) vs[i] = (float)(2.0 / vel[i]);
+    // |wc_s wc_r + ws_s ws_r| <= |A_s tap_s| |A_r tap_r| (Cauchy-Schwarz): the
+    // bound the forward's fixed-point scale uses
+    auto maxabs2 = [](const std::vector<float>& c, const std::vector<float>& s_) {
+        double m = 0.0;
+        for (size_t k = 0; k < c.size(); ++k) m = std::max(m, sqrt((double)c[k] * c[k] + (double)s_[k] * s_[k]));
+        return m;
+    };
+    const double wmax = maxabs2(wsc, wss) * maxabs2(wrc, wrs) * 1.0001;
+    if (!isfinite(wmax)) return set_error(KGB_ERR_VALUE, "set_dynamic: non-finite amplitude or angle table");
     // offset aperture (kirchhoff.py:866-880): |six-rix|/(iz+1) < apmax, which
     // holds from the first passing depth downwards; inside it the reference's
     // taper index is 0 and taper[0] == 1, so only this cut-off acts.
@@ -272,6 +295,7 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const doub
     KGB_CUDA_TRY(cudaMemcpy(op->vscale, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice));
     KGB_CUDA_TRY(cudaMemcpy(op->izmin, izmin.data(), izmin.size() * 4, cudaMemcpyHostToDevice));
     op->has_gate = gate;
+    op->wmax = (float)std::max(wmax, 1e-30);
     op->dyn_ready = true;
     return KGB_OK;
 }
@@ -354,10 +378,25 @@ int kgb_kirchhoff_adjoint_host(kgb_kirchhoff* op, const float* d_host, float* m_
     return KGB_OK;
 }
 
+int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (spread_variant < 0 || spread_variant > 2) return set_error(KGB_ERR_VALUE, "set_variant: spread variant must be 0, 1 or 2");
+    op->spread_variant = spread_variant;
+    return KGB_OK;
+}
+
 int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
     if (!op || !s) return set_error(KGB_ERR_VALUE, "info: null pointer");
+    for (int k = 0; k < 16; ++k) s[k] = 0;
     s[0] = op->ns; s[1] = op->nr; s[2] = op->nt; s[3] = op->ni;
     s[4] = op->frac_bits; s[5] = op->L; s[6] = op->has_gate ? 1 : 0; s[7] = op->dynamic;
+    s[8] = op->nonneg ? 1 : 0;
+    s[9] = gather_nsplit(op->view(), op->dynamic, op->has_gate);
+    // kernels per application: forward = prepass + spread; adjoint =
+    // correlation + gather (+ partial-image sum when split)
+    s[10] = 2;
+    s[11] = 2 + (s[9] > 1 ? 1 : 0);
+    s[12] = op->spread_variant;
     return KGB_OK;
 }
 

@@ -13,6 +13,10 @@
 // source-receiver pair is one exact integer add: the integer part is a
 // shift, the fraction a mask, and the index decision is the reference's
 // float64 one except within 2^-frac_bits samples of a bin edge.
+//
+// Both kernels are deterministic: the adjoint sums each image point in a
+// fixed order, the forward accumulates in exact 64-bit fixed point, whose
+// integer additions commute.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,56 +29,87 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int kGatherThreads = 256;
-constexpr int kGatherRC = 8;          // receivers held in registers per thread
-constexpr int kSpreadThreads = 256;   // 8 warps, one trace per warp
-constexpr int kNumSM = 152;
+constexpr int kGatherRC = 8;        // receivers held in registers per thread
+constexpr int kSpreadThreads = 512;
+constexpr int kMaxSplit = 16;       // source splits of the gather (partial images)
 
+int num_sms() {
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 148;
+    if (!sms[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev] = v > 0 ? v : 148;
+    }
+    return sms[dev];
+}
+
+// Fixed-point traveltime decoding.  s = ts + tr in units of 2^-F samples.
+template <bool NONNEG>
 struct FixedPoint {
     int F;
-    unsigned bias;   // 2^F - 1
-    unsigned umax;   // nt*2^F - 1
-    float scale;     // 2^-F
-    __device__ __forceinline__ bool valid(int s) const { return (unsigned)s + bias < umax; }
-    __device__ __forceinline__ int index(int s) const { return max(s, 0) >> F; }
-    __device__ __forceinline__ float frac(int s, int it) const { return (float)(s - (it << F)) * scale; }
+    unsigned bias;   // 2^F - 1 (general case)
+    unsigned umax;   // NONNEG: (nt-1) 2^F; general: nt 2^F - 1
+    unsigned fmask;  // 2^F - 1
+    int fshift;      // 23 - F
+    __device__ __forceinline__ bool valid(int s) const {
+        return NONNEG ? ((unsigned)s < umax) : ((unsigned)s + bias < umax);
+    }
+    __device__ __forceinline__ int index(int s) const {
+        return NONNEG ? (int)((unsigned)s >> F) : (max(s, 0) >> F);
+    }
+    // fraction w = t/dt - it; exact (F <= 22 bits)
+    __device__ __forceinline__ float frac(int s, int it) const {
+        if (NONNEG) {
+            // 1.f + frac * 2^-F built directly in the mantissa, then minus 1
+            return __int_as_float((((unsigned)s & fmask) << fshift) | 0x3f800000u) - 1.0f;
+        }
+        return (float)(s - (it << F)) * __int_as_float((127 - F) << 23);
+    }
 };
 
-__host__ inline FixedPoint make_fp(int F, int nt) {
-    FixedPoint fp;
+template <bool NONNEG>
+FixedPoint<NONNEG> make_fp(int F, int nt) {
+    FixedPoint<NONNEG> fp;
     fp.F = F;
     fp.bias = (1u << F) - 1u;
-    fp.umax = ((unsigned)nt << F) - 1u;
-    fp.scale = 1.0f / (float)(1u << F);
+    fp.umax = NONNEG ? ((unsigned)(nt - 1) << F) : (((unsigned)nt << F) - 1u);
+    fp.fmask = (1u << F) - 1u;
+    fp.fshift = 23 - F;
     return fp;
 }
 
 // ---------------------------------------------------------------------------
 // Adjoint: one thread per image point.  Each thread keeps kGatherRC receiver
-// traveltimes (and weights) in registers and sweeps every source against
-// them, so table reads are ~1/kGatherRC per pair-point and fully coalesced.
-// The sum over traces has a fixed order per image point: the result is
-// bit-identical run to run (no atomics).
+// traveltimes (and weights) in registers and sweeps every source of its
+// split against them, so table reads are ~1/kGatherRC per pair-point and
+// coalesced (a warp reads 128 contiguous bytes of a row).  The sum over
+// traces has a fixed order per image point.
 // ---------------------------------------------------------------------------
-template <bool DYN, bool GATE>
+template <bool DYN, bool GATE, bool NONNEG>
 __global__ void __launch_bounds__(kGatherThreads)
-gather_kernel(const KirchDev K, const FixedPoint fp, const float* __restrict__ d,
+gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float* __restrict__ d,
               float* __restrict__ out, int s_per_split) {
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= K.ni) return;
     const int s_begin = blockIdx.y * s_per_split;
     const int s_end = min(K.ns, s_begin + s_per_split);
-    const int iz = (int)(ii % K.nz);
+    const int iz = GATE ? (int)(ii % K.nz) : 0;
     const int nt = K.nt;
     float total = 0.f;
     for (int r0 = 0; r0 < K.nr; r0 += kGatherRC) {
         int trv[kGatherRC];
         float rcv[kGatherRC], rsv[kGatherRC];
+        int roff[kGatherRC];
 #pragma unroll
         for (int r = 0; r < kGatherRC; ++r) {
             const int ir = r0 + r;
             trv[r] = 0;
             rcv[r] = 0.f;
             rsv[r] = 0.f;
+            roff[r] = r * nt;
             if (ir < K.nr) {
                 trv[r] = __ldg(K.trq + (size_t)ir * K.ni + ii);
                 if (DYN) {
@@ -93,7 +128,7 @@ gather_kernel(const KirchDev K, const FixedPoint fp, const float* __restrict__ d
                 ss = __ldg(K.wss + (size_t)is * K.ni + ii);
             }
             const size_t pair0 = (size_t)is * K.nr + r0;
-            const float* drow = d + pair0 * nt;
+            const float* __restrict__ drow = d + pair0 * nt;
 #pragma unroll
             for (int r = 0; r < kGatherRC; ++r) {
                 if (r < nrc) {
@@ -101,7 +136,7 @@ gather_kernel(const KirchDev K, const FixedPoint fp, const float* __restrict__ d
                     if (fp.valid(s)) {
                         const int it = fp.index(s);
                         const float w = fp.frac(s, it);
-                        const float* p = drow + (size_t)r * nt + it;
+                        const float* p = drow + (roff[r] + it);
                         const float d0 = __ldg(p);
                         const float d1 = __ldg(p + 1);
                         float val = fmaf(w, d1 - d0, d0);
@@ -133,99 +168,266 @@ __global__ void sum_partials_kernel(const float* __restrict__ partial, float* __
 }
 
 // ---------------------------------------------------------------------------
-// Forward: one warp per trace (source-receiver pair) with a private trace in
-// shared memory.  32 consecutive image points are processed per step; lanes
-// whose contributions land in the same time bin are found with
-// __match_any_sync and summed by the lowest lane of the bin in lane order
-// (time-binned warp reduction), then the bin leaders update the shared
-// trace in two conflict-free phases (sample it, then it+1).  No atomics: the
-// result does not depend on scheduling.  The wavelet convolution is applied
-// to the finished trace in shared memory and written once to HBM.
+// Forward.
+// Prepass: mv = m * 2/v (dynamic) or m, and max |mv| for the fixed-point
+// scale of the spreading kernel.
 // ---------------------------------------------------------------------------
-template <bool DYN, bool GATE>
+template <bool DYN>
+__global__ void __launch_bounds__(256)
+spread_prepass_kernel(const KirchDev K, const float* __restrict__ m) {
+    float amax = 0.f;
+    for (int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ii < K.ni;
+         ii += (int64_t)gridDim.x * blockDim.x) {
+        float v = m[ii];
+        if (DYN) v *= __ldg(K.vscale + ii);
+        K.mv[ii] = v;
+        amax = fmaxf(amax, fabsf(v));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(FULL, amax, o));
+    if ((threadIdx.x & 31) == 0 && amax > 0.f) atomicMax(K.absmax, __float_as_uint(amax));
+}
+
+// Exponent e of the fixed-point scale 2^e: |v| 2^e < 2^(61 - ceil(log2(ni+1)))
+// for every contribution bound |v| <= amax, so ni of them sum inside int64.
+__device__ __forceinline__ int spread_scale_exponent(float amax, int64_t ni) {
+    if (!(amax > 0.f)) return 0;
+    int ex;
+    frexpf(amax, &ex);  // amax < 2^ex
+    int nb = 0;
+    while (nb < 40 && ((int64_t)1 << nb) <= ni) ++nb;
+    int e = 61 - nb - ex;
+    return max(-126, min(e, 126));
+}
+
+// Spreading, atomic variant: one CTA per (source, group of R receivers).  The CTA sweeps all
+// image points (one per thread per step), loads the source-side values once
+// per point and, for each of its R traces, accumulates the two contributions
+// v*(1-w), v*w into that trace's shared-memory time bins as 64-bit fixed
+// point: each contribution is scaled by a power of two chosen from a bound on
+// |v|, rounded to an integer (resolution ~2^-42 of the bound) and added
+// exactly, so the trace is independent of the order in which threads arrive.  The finished traces are converted back
+// to float, convolved with the wavelet in shared memory and written once.
+template <bool DYN, bool GATE, bool NONNEG, int R>
 __global__ void __launch_bounds__(kSpreadThreads)
-spread_kernel(const KirchDev K, const FixedPoint fp, const float* __restrict__ m,
-              float* __restrict__ y, const float* __restrict__ h, int L, int Lpad, int nt_pad,
-              int fuse) {
-    extern __shared__ float smem[];
+spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
+              const float* __restrict__ h, int L, int Lpad, int nt_pad, int fuse) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad);
+    float* hs = ftr + nt_pad;
+    const int tid = threadIdx.x;
+    const int nt = K.nt;
+    const int ngroups = (K.nr + R - 1) / R;
+    // source varies fastest across consecutive blocks: the CTAs resident at
+    // one time share a few receiver groups (whose rows stay in L2) and sweep
+    // the sources.
+    const int is = blockIdx.x % K.ns;
+    const int g = blockIdx.x / K.ns;
+    if (g >= ngroups) return;
+    const int r0 = g * R;
+    const int nrr = min(R, K.nr - r0);
+    for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
+    if (fuse)
+        for (int k = tid; k < L; k += blockDim.x) hs[k] = h[k];
+    // fixed-point scale: every contribution |v S| < 2^(61 - log2(ni)), so a
+    // trace sample summing up to ni of them stays inside int64
+    const int e = spread_scale_exponent(__uint_as_float(*K.absmax) * K.wmax, K.ni);
+    const float S = ldexpf(1.f, e);
+    int izmin[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
+    __syncthreads();
+    const int32_t* __restrict__ tsrow = K.tsq + (size_t)is * K.ni;
+    for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
+        const float v = __ldg(K.mv + ii) * S;
+        if (v == 0.f) continue;  // zero model point: no contribution
+        const int ts = __ldg(tsrow + ii);
+        float sc = 0.f, ss = 0.f;
+        if (DYN) {
+            sc = __ldg(K.wsc + (size_t)is * K.ni + ii);
+            ss = __ldg(K.wss + (size_t)is * K.ni + ii);
+        }
+        const int iz = GATE ? (int)(ii % K.nz) : 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (r < nrr) {
+                const size_t ro = (size_t)(r0 + r) * K.ni + ii;
+                const int s = ts + __ldg(K.trq + ro);
+                float val = v;
+                if (DYN) {
+                    float wt = fmaf(sc, __ldg(K.wrc + ro), ss * __ldg(K.wrs + ro));
+                    if (GATE && iz < izmin[r]) wt = 0.f;
+                    val *= wt;
+                }
+                if (fp.valid(s) && val != 0.f) {
+                    const int it = fp.index(s);
+                    const float w = fp.frac(s, it);
+                    const float v1 = val * w;
+                    const float v0 = val - v1;
+                    unsigned long long* a = acc + (size_t)r * nt_pad + it;
+                    atomicAdd(a, (unsigned long long)__float2ll_rn(v0));
+                    atomicAdd(a + 1, (unsigned long long)__float2ll_rn(v1));
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const float invS = ldexpf(1.f, -e);
+    const int c = (L - 1) / 2;
+    for (int r = 0; r < nrr; ++r) {
+        for (int n = tid; n < nt; n += blockDim.x) ftr[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        __syncthreads();
+        float* __restrict__ yrow = y + ((size_t)is * K.nr + r0 + r) * nt;
+        for (int n = tid; n < nt; n += blockDim.x) {
+            float o;
+            if (fuse) {
+                const int kmin = max(0, n + c - (nt - 1));
+                const int kmax = min(L - 1, n + c);
+                o = 0.f;
+                for (int k = kmin; k <= kmax; ++k) o = fmaf(hs[k], ftr[n + c - k], o);
+            } else {
+                o = ftr[n];
+            }
+            yrow[n] = o;
+        }
+        __syncthreads();
+    }
+}
+
+// Spreading, warp-binned variant: each warp owns RT traces (one source, RT
+// receivers) in shared memory and walks the image one depth column at a time,
+// 32 consecutive depths per step, lane = depth.  Down a column the time
+// index of the contributing points normally increases strictly (always so
+// inside an angle aperture below ~60 degrees, where the two-way vertical
+// slowness exceeds one sample per cell); then the lanes' bins are distinct
+// and the contributions are added directly, sample it in one pass and it+1
+// in the next.  Otherwise lanes that share a bin are found with
+// __match_any_sync and summed by the lowest lane of the bin in lane order.
+// No atomics and a fixed summation order: deterministic.
+template <bool DYN, bool GATE, bool NONNEG, int RT>
+__global__ void __launch_bounds__(256)
+spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
+                     const float* __restrict__ h, int L, int Lpad, int nt_pad, int fuse) {
+    extern __shared__ __align__(16) float smem_f[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nw = blockDim.x >> 5;
-    float* hs = smem;
-    float* trace = smem + Lpad + (size_t)warp * nt_pad;
-    if (fuse) {
+    float* hs = smem_f;
+    float* traces = smem_f + Lpad + (size_t)warp * RT * nt_pad;
+    if (fuse)
         for (int k = threadIdx.x; k < L; k += blockDim.x) hs[k] = h[k];
-    }
     __syncthreads();
-    const int64_t npair = (int64_t)K.ns * K.nr;
-    const int64_t pair = (int64_t)blockIdx.x * nw + warp;
-    if (pair >= npair) return;
     const int nt = K.nt;
-    for (int n = lane; n < nt; n += 32) trace[n] = 0.f;
+    const int nz = K.nz;
+    const int per_cta = nw * RT;
+    const int ngroups = (K.nr + per_cta - 1) / per_cta;
+    const int is = blockIdx.x % K.ns;
+    const int g = blockIdx.x / K.ns;
+    if (g >= ngroups) return;
+    const int r0 = g * per_cta + warp * RT;
+    const int nrr = max(0, min(RT, K.nr - r0));
+    if (nrr == 0) return;
+    for (int k = lane; k < RT * nt_pad; k += 32) traces[k] = 0.f;
     __syncwarp();
-    const int is = (int)(pair / K.nr);
-    const int ir = (int)(pair - (int64_t)is * K.nr);
+    int izmin[RT];
+#pragma unroll
+    for (int r = 0; r < RT; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
     const int32_t* __restrict__ tsrow = K.tsq + (size_t)is * K.ni;
-    const int32_t* __restrict__ trrow = K.trq + (size_t)ir * K.ni;
-    const int izmin = GATE ? __ldg(K.izmin + pair) : 0;
+    const float* __restrict__ scrow = DYN ? K.wsc + (size_t)is * K.ni : nullptr;
+    const float* __restrict__ ssrow = DYN ? K.wss + (size_t)is * K.ni : nullptr;
+    const int64_t ncol = K.ni / nz;
     const unsigned lower = (1u << lane) - 1u;
-    for (int64_t base = 0; base < K.ni; base += 32) {
-        const int64_t ii = base + lane;
-        float v0 = 0.f, v1 = 0.f;
-        int it = 0;
-        bool valid = false;
-        if (ii < K.ni) {
-            const int s = __ldg(tsrow + ii) + __ldg(trrow + ii);
-            if (fp.valid(s)) {
-                it = fp.index(s);
-                const float w = fp.frac(s, it);
-                float val = __ldg(m + ii);
+    for (int64_t col = 0; col < ncol; ++col) {
+        for (int iz0 = 0; iz0 < nz; iz0 += 32) {
+            const int iz = iz0 + lane;
+            const bool inb = iz < nz;
+            const int64_t ii = col * nz + (inb ? iz : 0);
+            float v = 0.f, sc = 0.f, ss = 0.f;
+            int ts = 0;
+            if (inb) {
+                v = __ldg(K.mv + ii);
+                ts = __ldg(tsrow + ii);
                 if (DYN) {
-                    float wt = fmaf(__ldg(K.wsc + (size_t)is * K.ni + ii), __ldg(K.wrc + (size_t)ir * K.ni + ii),
-                                    __ldg(K.wss + (size_t)is * K.ni + ii) * __ldg(K.wrs + (size_t)ir * K.ni + ii));
-                    wt *= __ldg(K.vscale + ii);
-                    if (GATE && (int)(ii % K.nz) < izmin) wt = 0.f;
-                    val *= wt;
+                    sc = __ldg(scrow + ii);
+                    ss = __ldg(ssrow + ii);
                 }
-                v1 = val * w;
-                v0 = val - v1;
-                valid = true;
+            }
+#pragma unroll
+            for (int r = 0; r < RT; ++r) {
+                if (r >= nrr) break;
+                const size_t ro = (size_t)(r0 + r) * K.ni + ii;
+                int s = 0;
+                float val = v;
+                if (inb) {
+                    s = ts + __ldg(K.trq + ro);
+                    if (DYN) {
+                        float wt = fmaf(sc, __ldg(K.wrc + ro), ss * __ldg(K.wrs + ro));
+                        if (GATE && iz < izmin[r]) wt = 0.f;
+                        val *= wt;
+                    }
+                }
+                const bool tv = inb && fp.valid(s);
+                const int it = tv ? fp.index(s) : 0;
+                const bool contrib = tv && val != 0.f;
+                if (__ballot_sync(FULL, contrib) == 0u) continue;
+                float v0 = 0.f, v1 = 0.f;
+                if (contrib) {
+                    const float w = fp.frac(s, it);
+                    v1 = val * w;
+                    v0 = val - v1;
+                }
+                float* tr = traces + r * nt_pad;
+                // strictly increasing bins over the time-valid prefix of lanes?
+                const int prev_it = __shfl_up_sync(FULL, it, 1);
+                const bool prev_tv = __shfl_up_sync(FULL, (int)tv, 1) != 0;
+                const bool ok = !tv || lane == 0 || (prev_tv && it > prev_it);
+                if (__all_sync(FULL, ok)) {
+                    if (contrib) tr[it] += v0;
+                    __syncwarp();
+                    if (contrib) tr[it + 1] += v1;
+                    __syncwarp();
+                } else {
+                    const unsigned key = contrib ? (unsigned)it : (0x80000000u | (unsigned)lane);
+                    const unsigned peers = __match_any_sync(FULL, key);
+                    unsigned rest = peers & (peers - 1u);
+                    const int maxc = __reduce_max_sync(FULL, (unsigned)__popc(rest));
+                    float s0 = v0, s1 = v1;
+                    for (int k = 0; k < maxc; ++k) {
+                        const int src = rest ? (__ffs(rest) - 1) : lane;
+                        const float a0 = __shfl_sync(FULL, v0, src);
+                        const float a1 = __shfl_sync(FULL, v1, src);
+                        if (rest) {
+                            s0 += a0;
+                            s1 += a1;
+                            rest &= rest - 1u;
+                        }
+                    }
+                    const bool lead = contrib && ((peers & lower) == 0u);
+                    if (lead) tr[it] += s0;
+                    __syncwarp();
+                    if (lead) tr[it + 1] += s1;
+                    __syncwarp();
+                }
             }
         }
-        if (__ballot_sync(FULL, valid) == 0u) continue;
-        const unsigned key = valid ? (unsigned)it : (0x80000000u | (unsigned)lane);
-        const unsigned peers = __match_any_sync(FULL, key);
-        unsigned rest = peers & (peers - 1u);  // bin members after the lowest lane
-        const int maxc = __reduce_max_sync(FULL, (unsigned)__popc(rest));
-        float s0 = v0, s1 = v1;
-        for (int k = 0; k < maxc; ++k) {
-            const int src = rest ? (__ffs(rest) - 1) : lane;
-            const float a0 = __shfl_sync(FULL, v0, src);
-            const float a1 = __shfl_sync(FULL, v1, src);
-            if (rest) {
-                s0 += a0;
-                s1 += a1;
-                rest &= rest - 1u;
-            }
-        }
-        const bool lead = valid && ((peers & lower) == 0u);
-        if (lead) trace[it] += s0;
-        __syncwarp();
-        if (lead) trace[it + 1] += s1;
-        __syncwarp();
     }
-    float* __restrict__ yrow = y + pair * nt;
-    if (fuse) {
-        const int c = (L - 1) / 2;
+    const int c = (L - 1) / 2;
+    for (int r = 0; r < nrr; ++r) {
+        const float* tr = traces + r * nt_pad;
+        float* __restrict__ yrow = y + ((size_t)is * K.nr + r0 + r) * nt;
         for (int n = lane; n < nt; n += 32) {
-            const int kmin = max(0, n + c - (nt - 1));
-            const int kmax = min(L - 1, n + c);
-            float acc = 0.f;
-            for (int k = kmin; k <= kmax; ++k) acc = fmaf(hs[k], trace[n + c - k], acc);
-            yrow[n] = acc;
+            float o;
+            if (fuse) {
+                const int kmin = max(0, n + c - (nt - 1));
+                const int kmax = min(L - 1, n + c);
+                o = 0.f;
+                for (int k = kmin; k <= kmax; ++k) o = fmaf(hs[k], tr[n + c - k], o);
+            } else {
+                o = tr[n];
+            }
+            yrow[n] = o;
         }
-    } else {
-        for (int n = lane; n < nt; n += 32) yrow[n] = trace[n];
     }
 }
 
@@ -257,79 +459,229 @@ wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, 
     }
 }
 
-int gather_splits(const KirchDev& K) {
+// ---------------------------------------------------------------------------
+// launch configuration
+// ---------------------------------------------------------------------------
+template <bool DYN, bool GATE, bool NONNEG>
+int gather_blocks_per_sm() {
+    static int cached = 0;
+    if (!cached) {
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gather_kernel<DYN, GATE, NONNEG>, kGatherThreads, 0);
+        cached = nb > 0 ? nb : 1;
+    }
+    return cached;
+}
+
+// Number of source splits that keeps the last wave of the gather grid full.
+int choose_split(int64_t blocks, int capacity, int ns) {
+    int best = 1;
+    double best_eff = 0.0;
+    const int maxs = std::min(kMaxSplit, ns);
+    for (int s = 1; s <= maxs; ++s) {
+        const int s_per = (ns + s - 1) / s;
+        const int sp = (ns + s_per - 1) / s_per;
+        const double waves = (double)(blocks * sp) / capacity;
+        const double eff = waves / std::ceil(waves) * (waves >= 1.0 ? 1.0 : waves);
+        if (eff > best_eff + 0.02) {
+            best_eff = eff;
+            best = sp;
+        }
+    }
+    return best;
+}
+
+template <bool DYN, bool GATE, bool NONNEG>
+int gather_launch_t(const KirchDev& K, const float* d, float* img, float* partial, int64_t cap,
+                    cudaStream_t stream) {
+    const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
-    const int64_t want = 2 * kNumSM;
-    if (blocks >= want) return 1;
-    int split = (int)std::min<int64_t>((want + blocks - 1) / blocks, (int64_t)K.ns);
-    return std::max(split, 1);
-}
-
-}  // namespace
-
-int64_t gather_partial_elems(const KirchDev& K) {
-    const int split = gather_splits(K);
-    return split > 1 ? (int64_t)split * K.ni : 0;
-}
-
-int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, float* img,
-                  float* partial, int64_t partial_capacity, cudaStream_t stream) {
-    if (K.ni <= 0 || K.ns <= 0 || K.nr <= 0) return KGB_OK;
-    const FixedPoint fp = make_fp(K.frac_bits, K.nt);
-    int split = gather_splits(K);
-    int s_per = (K.ns + split - 1) / split;
+    const int capacity = num_sms() * gather_blocks_per_sm<DYN, GATE, NONNEG>();
+    int split = choose_split(blocks, capacity, K.ns);
+    if (partial == nullptr || cap < (int64_t)split * K.ni) split = 1;
+    const int s_per = (K.ns + split - 1) / split;
     split = (K.ns + s_per - 1) / s_per;
-    float* out = img;
-    if (split > 1) {
-        if (partial == nullptr || partial_capacity < (int64_t)split * K.ni)
-            return set_error(KGB_ERR_STATE, "gather: partial-image scratch too small");
-        out = partial;
-    }
-    dim3 grid((unsigned)((K.ni + kGatherThreads - 1) / kGatherThreads), (unsigned)split);
-    if (dynamic) {
-        if (gate) gather_kernel<true, true><<<grid, kGatherThreads, 0, stream>>>(K, fp, d, out, s_per);
-        else gather_kernel<true, false><<<grid, kGatherThreads, 0, stream>>>(K, fp, d, out, s_per);
-    } else {
-        gather_kernel<false, false><<<grid, kGatherThreads, 0, stream>>>(K, fp, d, out, s_per);
-    }
+    float* out = split > 1 ? partial : img;
+    dim3 grid((unsigned)blocks, (unsigned)split);
+    gather_kernel<DYN, GATE, NONNEG><<<grid, kGatherThreads, 0, stream>>>(K, fp, d, out, s_per);
     KGB_CUDA_TRY(cudaGetLastError());
     if (split > 1) {
-        const int blocks = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * kNumSM);
-        sum_partials_kernel<<<blocks, 256, 0, stream>>>(partial, img, K.ni, split);
+        const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
+        sum_partials_kernel<<<nb, 256, 0, stream>>>(partial, img, K.ni, split);
         KGB_CUDA_TRY(cudaGetLastError());
     }
     return KGB_OK;
 }
 
-template <bool DYN, bool GATE>
-static int spread_launch_t(const KirchDev& K, const FixedPoint& fp, const float* m, float* y,
-                           const float* h, int L, bool fuse, cudaStream_t stream) {
-    const int Lpad = fuse ? ((L + 3) & ~3) : 0;
-    const int nt_pad = (K.nt + 3) & ~3;
-    int warps = kSpreadThreads / 32;
-    const size_t max_smem = 200 * 1024;
-    while (warps > 1 && (size_t)(Lpad + warps * nt_pad) * sizeof(float) > max_smem) --warps;
-    const size_t smem = (size_t)(Lpad + warps * nt_pad) * sizeof(float);
-    if (smem > 227 * 1024)
-        return set_error(KGB_ERR_NOT_IMPLEMENTED, "spread: nt=%d too long for one trace in shared memory", K.nt);
-    auto kern = spread_kernel<DYN, GATE>;
-    KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t npair = (int64_t)K.ns * K.nr;
-    const int64_t blocks = (npair + warps - 1) / warps;
-    kern<<<(unsigned)blocks, warps * 32, smem, stream>>>(K, fp, m, y, h, L, Lpad, nt_pad, fuse ? 1 : 0);
+struct SpreadShape {
+    int R;
+    size_t smem;
+    int Lpad, nt_pad;
+};
+
+// Receivers per CTA: as many as keep two CTAs per SM, fewer when the grid
+// would not fill the GPU.
+SpreadShape spread_shape(const KirchDev& K, int L) {
+    SpreadShape sh;
+    sh.Lpad = (L + 3) & ~3;
+    sh.nt_pad = (K.nt + 3) & ~3;
+    const size_t fixed = (size_t)(sh.nt_pad + sh.Lpad) * sizeof(float);
+    const size_t budget2 = 110 * 1024, budget1 = 220 * 1024;
+    int R = 8;
+    auto need = [&](int r) { return fixed + (size_t)r * sh.nt_pad * 8; };
+    while (R > 1 && need(R) > budget2) R >>= 1;
+    const int sms = num_sms();
+    while (R > 1 && (int64_t)K.ns * ((K.nr + R - 1) / R) < 2 * sms) R >>= 1;
+    if (need(R) > budget1) R = 0;
+    sh.R = R;
+    sh.smem = R ? need(R) : 0;
+    return sh;
+}
+
+template <bool DYN, bool GATE, bool NONNEG, int R>
+int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
+                    const SpreadShape& sh, cudaStream_t stream, bool prepare_only) {
+    auto kern = spread_kernel<DYN, GATE, NONNEG, R>;
+    if (prepare_only) {
+        KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
+        return KGB_OK;
+    }
+    KGB_CUDA_TRY(cudaMemsetAsync(K.absmax, 0, sizeof(unsigned), stream));
+    const int pb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
+    spread_prepass_kernel<DYN><<<pb, 256, 0, stream>>>(K, m);
+    KGB_CUDA_TRY(cudaGetLastError());
+    const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
+    const int64_t blocks = (int64_t)K.ns * ((K.nr + R - 1) / R);
+    kern<<<(unsigned)blocks, kSpreadThreads, sh.smem, stream>>>(K, fp, y, h, L, sh.Lpad, sh.nt_pad, fuse ? 1 : 0);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
+}
+
+// Warp-binned variant: RT traces per warp, 8 warps per CTA.
+template <bool DYN, bool GATE, bool NONNEG, int RT>
+int spread_binned_launch_r(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
+                           cudaStream_t stream, bool prepare_only) {
+    auto kern = spread_binned_kernel<DYN, GATE, NONNEG, RT>;
+    const int Lpad = (L + 3) & ~3;
+    const int nt_pad = (K.nt + 3) & ~3;
+    const int warps = 8;
+    const size_t smem = (size_t)(Lpad + (size_t)warps * RT * nt_pad) * sizeof(float);
+    if (smem > 227 * 1024)
+        return set_error(KGB_ERR_NOT_IMPLEMENTED, "spread: nt=%d too long for the binned variant", K.nt);
+    if (prepare_only) {
+        KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return KGB_OK;
+    }
+    const int pb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
+    KGB_CUDA_TRY(cudaMemsetAsync(K.absmax, 0, sizeof(unsigned), stream));
+    spread_prepass_kernel<DYN><<<pb, 256, 0, stream>>>(K, m);
+    KGB_CUDA_TRY(cudaGetLastError());
+    const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
+    const int per_cta = warps * RT;
+    const int64_t blocks = (int64_t)K.ns * ((K.nr + per_cta - 1) / per_cta);
+    kern<<<(unsigned)blocks, warps * 32, smem, stream>>>(K, fp, y, h, L, Lpad, nt_pad, fuse ? 1 : 0);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+template <bool DYN, bool GATE, bool NONNEG>
+int spread_launch_t(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
+                    cudaStream_t stream, bool prepare_only) {
+    if (K.spread_variant == 1 || K.spread_variant == 2 || prepare_only) {
+        const int Lpad = (L + 3) & ~3;
+        const int nt_pad = (K.nt + 3) & ~3;
+        const bool fits2 = (size_t)(Lpad + 16 * (size_t)nt_pad) * 4 <= 227 * 1024;
+        int rc = KGB_OK;
+        if (prepare_only) {
+            if ((size_t)(Lpad + 8 * (size_t)nt_pad) * 4 <= 227 * 1024)
+                rc = spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, true);
+            if (!rc && fits2) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, true);
+            if (rc) return rc;
+        } else if (K.spread_variant == 2 && fits2) {
+            return spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, false);
+        } else {
+            return spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, false);
+        }
+    }
+    const SpreadShape sh = spread_shape(K, L);
+    switch (sh.R) {
+        case 8: return spread_launch_r<DYN, GATE, NONNEG, 8>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        case 4: return spread_launch_r<DYN, GATE, NONNEG, 4>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        case 2: return spread_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        case 1: return spread_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        default:
+            return set_error(KGB_ERR_NOT_IMPLEMENTED, "spread: nt=%d too long for one trace in shared memory", K.nt);
+    }
+}
+
+template <bool DYN, bool GATE>
+int spread_dispatch_nn(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
+                       cudaStream_t stream, bool prep) {
+    if (K.nonneg) return spread_launch_t<DYN, GATE, true>(K, m, y, h, L, fuse, stream, prep);
+    return spread_launch_t<DYN, GATE, false>(K, m, y, h, L, fuse, stream, prep);
+}
+
+int spread_dispatch(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y, const float* h,
+                    int L, bool fuse, cudaStream_t stream, bool prep) {
+    if (dynamic) {
+        if (gate) return spread_dispatch_nn<true, true>(K, m, y, h, L, fuse, stream, prep);
+        return spread_dispatch_nn<true, false>(K, m, y, h, L, fuse, stream, prep);
+    }
+    return spread_dispatch_nn<false, false>(K, m, y, h, L, fuse, stream, prep);
+}
+
+}  // namespace
+
+int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
+    const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
+    int bps;
+    if (dynamic) bps = gate ? (K.nonneg ? gather_blocks_per_sm<true, true, true>() : gather_blocks_per_sm<true, true, false>())
+                            : (K.nonneg ? gather_blocks_per_sm<true, false, true>() : gather_blocks_per_sm<true, false, false>());
+    else bps = K.nonneg ? gather_blocks_per_sm<false, false, true>() : gather_blocks_per_sm<false, false, false>();
+    int split = choose_split(blocks, num_sms() * bps, K.ns);
+    const int s_per = (K.ns + split - 1) / split;
+    return (K.ns + s_per - 1) / s_per;
+}
+
+int64_t gather_partial_elems(const KirchDev& K) {
+    return (int64_t)std::min(kMaxSplit, K.ns) * K.ni;
+}
+
+int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, float* img,
+                  float* partial, int64_t cap, cudaStream_t stream) {
+    if (K.ni <= 0 || K.ns <= 0 || K.nr <= 0) return KGB_OK;
+    if (dynamic) {
+        if (gate) {
+            if (K.nonneg) return gather_launch_t<true, true, true>(K, d, img, partial, cap, stream);
+            return gather_launch_t<true, true, false>(K, d, img, partial, cap, stream);
+        }
+        if (K.nonneg) return gather_launch_t<true, false, true>(K, d, img, partial, cap, stream);
+        return gather_launch_t<true, false, false>(K, d, img, partial, cap, stream);
+    }
+    if (K.nonneg) return gather_launch_t<false, false, true>(K, d, img, partial, cap, stream);
+    return gather_launch_t<false, false, false>(K, d, img, partial, cap, stream);
 }
 
 int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,
                   const float* h, int L, bool fuse_wavelet, cudaStream_t stream) {
     if (K.ns <= 0 || K.nr <= 0 || K.nt <= 0) return KGB_OK;
-    const FixedPoint fp = make_fp(K.frac_bits, K.nt);
-    if (dynamic) {
-        if (gate) return spread_launch_t<true, true>(K, fp, m, y, h, L, fuse_wavelet, stream);
-        return spread_launch_t<true, false>(K, fp, m, y, h, L, fuse_wavelet, stream);
+    return spread_dispatch(K, dynamic, gate, m, y, h, L, fuse_wavelet, stream, false);
+}
+
+int prepare_kernels(const KirchDev& K0, int L) {
+    int rc;
+    KirchDev K = K0;
+    for (int nn = 0; nn < 2; ++nn) {
+        K.nonneg = nn;
+        for (int dyn = 0; dyn < 2; ++dyn)
+            for (int gate = 0; gate < 2; ++gate)
+                if ((rc = spread_dispatch(K, dyn, gate, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     }
-    return spread_launch_t<false, false>(K, fp, m, y, h, L, fuse_wavelet, stream);
+    const int Lpad = (L + 3) & ~3;
+    const size_t smem = (size_t)(Lpad + K.nt) * sizeof(float);
+    if (smem <= 227 * 1024)
+        KGB_CUDA_TRY(cudaFuncSetAttribute(wavelet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return KGB_OK;
 }
 
 int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L,
@@ -339,8 +691,13 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
     const size_t smem = (size_t)(Lpad + nt) * sizeof(float);
     if (smem > 227 * 1024)
         return set_error(KGB_ERR_NOT_IMPLEMENTED, "wavelet: nt=%d too long for shared memory", nt);
-    KGB_CUDA_TRY(cudaFuncSetAttribute(wavelet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t blocks = std::min<int64_t>(ntr, 8 * kNumSM);
+    if (smem > 48 * 1024) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(stream, &cs);
+        if (cs == cudaStreamCaptureStatusNone)
+            KGB_CUDA_TRY(cudaFuncSetAttribute(wavelet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    const int64_t blocks = std::min<int64_t>(ntr, 8 * num_sms());
     wavelet_kernel<<<(unsigned)blocks, 256, smem, stream>>>(x, y, ntr, nt, g, L, Lpad);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;

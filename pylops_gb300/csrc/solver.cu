@@ -483,7 +483,14 @@ int enqueue(kgb_solver* s, cudaStream_t stream, int use_handle) {
     return s->kind == 1 ? enqueue_iteration(s, stream, use_handle) : enqueue_cgls_iteration(s, stream, use_handle);
 }
 
-// Graph: [set_target] -> WHILE(active) { iteration }.
+__global__ void cond_from_state_kernel(const SolverState* st, cudaGraphConditionalHandle handle) {
+    cudaGraphSetConditional(handle, st->active ? 1u : 0u);
+}
+
+// Graph: [condition <- state.active] -> WHILE(condition) { iteration }.
+// The WHILE node's condition is reset to its default (0) at every launch, so
+// the first node of the graph sets it from the device state that
+// set_target_kernel prepared.
 int build_graph(kgb_solver* s, cudaStream_t stream) {
     if (s->exec) return KGB_OK;
     cudaGraph_t g = nullptr;
@@ -492,13 +499,24 @@ int build_graph(kgb_solver* s, cudaStream_t stream) {
     cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
     if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_error(e, "cudaGraphConditionalHandleCreate"); }
     s->handle = h;
+    e = cudaStreamBeginCaptureToGraph(stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_error(e, "cudaStreamBeginCaptureToGraph(init)"); }
+    cond_from_state_kernel<<<1, 1, 0, stream>>>(s->st, h);
+    cudaError_t le = cudaGetLastError();
+    cudaGraph_t tmp = nullptr;
+    e = cudaStreamEndCapture(stream, &tmp);
+    if (le != cudaSuccess || e != cudaSuccess) { cudaGraphDestroy(g); return cuda_error(le != cudaSuccess ? le : e, "capture init node"); }
+    cudaGraphNode_t init = nullptr;
+    size_t nn = 1;
+    e = cudaGraphGetNodes(g, &init, &nn);
+    if (e != cudaSuccess || nn != 1) { cudaGraphDestroy(g); return set_error(KGB_ERR_CUDA, "graph init node lookup failed"); }
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
     cudaGraphNode_t wnode;
-    e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &cp);
+    e = cudaGraphAddNode(&wnode, g, &init, nullptr, 1, &cp);
     if (e != cudaSuccess) { cudaGraphDestroy(g); return cuda_error(e, "cudaGraphAddNode(while)"); }
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     e = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
@@ -749,8 +767,6 @@ int kgb_solver_run(kgb_solver* s, int niter, int use_graph, void* stream_) {
         if ((rc = build_graph(s, stream))) return rc;
         set_target_kernel<<<1, 1, 0, stream>>>(s->st, niter, s->handle, 0);
         KGB_CUDA_TRY(cudaGetLastError());
-        // the WHILE node's default condition is 0; the first body launch is
-        // decided by this upstream set (a one-node graph sets it too)
         KGB_CUDA_TRY(cudaGraphLaunch(s->exec, stream));
         return KGB_OK;
     }

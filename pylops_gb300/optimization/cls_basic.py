@@ -126,11 +126,11 @@ class _DeviceSolver:
         return x, self.out.copy(), cost
 
 
-def _like_input(x_dev, ref, dtype):
-    """Return a device result in the kind (numpy/torch) of the user's data."""
+def _like_input(x_dev, ref):
+    """Return a device result in the kind (numpy/torch) and dtype of the user's data."""
     if is_torch(ref):
         return x_dev if x_dev.dtype == ref.dtype else x_dev.to(ref.dtype)
-    return x_dev.cpu().numpy().astype(dtype, copy=False)
+    return x_dev.cpu().numpy().astype(ref.dtype, copy=False)
 
 
 # ----------------------------------------------------------------------------
@@ -180,7 +180,7 @@ class CGLS(Solver):
             self.cost = [float(cost[0])]
             self.cost1 = [float(cost[1])]
             self.iiter = 0
-            x = _like_input(x_dev, y, np.dtype(y.dtype))
+            x = _like_input(x_dev, y)
         else:
             if x0 is None:
                 x = _zeros_like_model(self.Op, y)
@@ -214,7 +214,7 @@ class CGLS(Solver):
         if self._native:
             self._dev.run(1, graph=False)
             x_dev = self._sync_native()
-            x = _like_input(x_dev, self.y, np.dtype(self._ydtype))
+            x = _like_input(x_dev, self.y)
         else:
             a = self.kold / (_dot(self.q, self.q) + self.damp * _dot(self.c, self.c))
             x = x + a * self.c
@@ -240,7 +240,7 @@ class CGLS(Solver):
         if self._native and not show and not self.callbacks and type(self).callback is CGLS.callback:
             self._dev.run(niter - self.iiter, graph=True)
             x_dev = self._sync_native()
-            return _like_input(x_dev, self.y, np.dtype(self._ydtype))
+            return _like_input(x_dev, self.y)
         while self.iiter < niter and self.kold > self.tol:
             showstep = show and (self.iiter < itershow[0] or niter - self.iiter < itershow[1]
                                  or self.iiter % itershow[2] == 0)
@@ -340,7 +340,7 @@ class LSQR(Solver):
             self._dev.setup(y, x0, [damp, atol, btol, conlim, niter])
             x_dev, out, cost = self._dev.result(want_x=True, cost_cap=1)
             self._read_state(out, cost)
-            x = _like_input(x_dev, y, np.dtype(y.dtype))
+            x = _like_input(x_dev, y)
             self.alfa = self.arnorm / self.beta if self.beta else 0.0
         else:
             self.var = None
@@ -412,7 +412,7 @@ class LSQR(Solver):
         if self._native:
             self._dev.run(1, graph=False)
             x_dev = self._sync_native()
-            x = _like_input(x_dev, self.y, np.dtype(self._ydtype))
+            x = _like_input(x_dev, self.y)
             if show:
                 self._print_step(x)
             return x
@@ -497,7 +497,7 @@ class LSQR(Solver):
         if self._native and not show and not self.callbacks and type(self).callback is LSQR.callback:
             self._dev.run(niter - self.iiter, graph=True)
             x_dev = self._sync_native()
-            return _like_input(x_dev, self.y, np.dtype(self._ydtype))
+            return _like_input(x_dev, self.y)
         while self.iiter < niter and self.istop == 0:
             x = self.step(x, show and (self.niter <= 40 or self.iiter < itershow[0]
                                        or niter - self.iiter < itershow[1] or self.iiter % itershow[2] == 0))

@@ -288,12 +288,23 @@ class Kirchhoff(LinearOperator):
         self._sync_tables()
         return self._h
 
+    def info(self) -> dict:
+        """Device-side layout and launch facts of this operator."""
+        self._sync_tables()
+        v = (ctypes.c_int64 * 16)()
+        _native.check(_native.lib().kgb_kirchhoff_info(self._h, v))
+        keys = ("ns", "nr", "nt", "ni", "frac_bits", "wavelet_len", "offset_gate", "dynamic", "nonneg",
+                "adjoint_splits", "kernels_forward", "kernels_adjoint", "spread_variant")
+        return {k: int(v[i]) for i, k in enumerate(keys)}
+
+    def set_spread_variant(self, variant: int) -> None:
+        """Select the forward kernel: 0 fixed-point atomics, 1 warp-binned
+        (one trace per warp), 2 warp-binned (two traces per warp)."""
+        _native.check(_native.lib().kgb_kirchhoff_set_variant(self._h, int(variant)))
+
     @property
     def frac_bits(self) -> int:
-        self._sync_tables()
-        info = (ctypes.c_int64 * 8)()
-        _native.check(_native.lib().kgb_kirchhoff_info(self._h, info))
-        return int(info[4])
+        return self.info()["frac_bits"]
 
     # ---------------------------------------------------------------- apply
     def _run(self, x, which):

@@ -34,6 +34,19 @@ def test_forward_adjoint_match_reference(name):
     assert rel(x, g["adj"]) < TOL, rel(x, g["adj"])
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_forward_variants_match_reference(name, variant):
+    """Every forward kernel variant against the reference, bitwise repeatable."""
+    g = load(name)
+    K = _op(g)
+    K.set_spread_variant(variant)
+    y = K @ g["m_in"].astype(np.float32)
+    assert rel(y, g["fwd"]) < TOL, rel(y, g["fwd"])
+    assert rel(K.spread(g["m_in"]), g["spread"]) < TOL
+    assert np.array_equal(y, K @ g["m_in"].astype(np.float32))
+
+
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_spread_gather_match_reference(name):
     g = load(name)
@@ -82,10 +95,17 @@ def test_config1_scale_against_oracle(dynamic, angleaperture, aperture):
     kw = dict(mode="analytic", dynamic=dynamic, angleaperture=angleaperture, aperture=aperture)
     K = Kirchhoff(*args, engine="cuda", dtype="float32", **kw)
     O = ko.KirchhoffOracle(*args, **kw)
-    y = K @ c["m"].astype(np.float32)
     x = K.H @ c["d"].astype(np.float32)
-    assert rel(y, O.matvec(c["m"])) < TOL
     assert rel(x, O.rmatvec(c["d"])) < TOL
+    yo = O.matvec(c["m"])
+    mr = np.random.default_rng(5).standard_normal(K.ni)  # dense model as well
+    yr = O.matvec(mr)
+    for variant in (0, 1, 2):
+        K.set_spread_variant(variant)
+        y = K @ c["m"].astype(np.float32)
+        assert rel(y, yo) < TOL, (variant, rel(y, yo))
+        y = K @ mr.astype(np.float32)
+        assert rel(y, yr) < TOL, (variant, rel(y, yr))
 
 
 def test_bitwise_determinism():
@@ -96,10 +116,12 @@ def test_bitwise_determinism():
                   dynamic=True, angleaperture=40.0, dtype="float32")
     m = c["m"].astype(np.float32)
     d = c["d"].astype(np.float32)
-    ys = [K @ m for _ in range(3)]
+    for variant in (0, 1, 2):
+        K.set_spread_variant(variant)
+        ys = [K @ m for _ in range(3)]
+        for y in ys[1:]:
+            assert np.array_equal(y, ys[0])
     xs = [K.H @ d for _ in range(3)]
-    for y in ys[1:]:
-        assert np.array_equal(y, ys[0])
     for x in xs[1:]:
         assert np.array_equal(x, xs[0])
 
