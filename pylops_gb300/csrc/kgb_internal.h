@@ -48,6 +48,10 @@ struct KirchDev {
     const float* wrs;
     const float* vscale;
     const int32_t* izmin;
+    // dynamic mode: per-entry records {tq, wc, ws, 0} (one 16-byte load gives
+    // a table entry's traveltime and both weights)
+    const int4* stab;  // [ns][ni]
+    const int4* rtab;  // [nr][ni]
 };
 
 // Launchers (kirchhoff_kernels.cu).  All asynchronous on `stream`.
@@ -57,8 +61,14 @@ int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, fl
                   float* partial, int64_t partial_capacity, cudaStream_t stream);
 // Set the kernels' shared-memory attributes once, outside any stream capture.
 int prepare_kernels(const KirchDev& K, int L);
+// Wavelet filter along time.  interleave = 0 writes y[tr][n]; interleave = 1
+// writes the pair (o[n], o[n+1]) at y[tr][2n] (o[nt] = 0), the layout the
+// gather reads with one 8-byte load.  g == nullptr copies (no filter).
 int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L,
-                   cudaStream_t stream);
+                   int interleave, cudaStream_t stream);
+// Build the dynamic-mode records from the traveltime and weight arrays.
+int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
+                       const float* wrs, int4* stab, int4* rtab, cudaStream_t stream);
 // How many float partial images launch_gather may use, and how many source
 // splits (partial images) it launches for this geometry.
 int64_t gather_partial_elems(const KirchDev& K);
@@ -97,7 +107,9 @@ struct kgb_kirchhoff {
     unsigned* absmax = nullptr;
     bool trav_ready = false;
     bool dyn_ready = false;
-    float* dcorr = nullptr;    // scratch: correlated data for the adjoint
+    int4* stab = nullptr;
+    int4* rtab = nullptr;
+    float* dcorr = nullptr;    // scratch: correlated data for the adjoint, interleaved pairs (2 x ndata)
     float* partial = nullptr;  // scratch: per-split partial images
     int64_t partial_elems = 0;
     float* m_stage = nullptr;  // device staging for the host-buffer entry points
@@ -112,6 +124,7 @@ struct kgb_kirchhoff {
         K.vscale = vscale; K.izmin = izmin;
         K.nonneg = nonneg ? 1 : 0; K.wmax = wmax; K.mv = mv; K.absmax = absmax;
         K.spread_variant = spread_variant;
+        K.stab = stab; K.rtab = rtab;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

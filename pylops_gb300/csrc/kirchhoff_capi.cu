@@ -79,6 +79,19 @@ static int choose_frac_bits(double max_samples, int nt) {
     return std::min(22, 30 - need);
 }
 
+// Dynamic-mode records {tq, wc, ws} from the traveltime and weight arrays;
+// run whenever either side changes.
+static int repack(kgb_kirchhoff* op) {
+    if (!op->dynamic || !op->trav_ready || !op->dyn_ready) return KGB_OK;
+    int rc;
+    if (!op->stab && (rc = dev_alloc(&op->stab, (size_t)op->ns * op->ni, "alloc source records"))) return rc;
+    if (!op->rtab && (rc = dev_alloc(&op->rtab, (size_t)op->nr * op->ni, "alloc receiver records"))) return rc;
+    if ((rc = launch_pack_tables(op->view(), op->wsc, op->wss, op->wrc, op->wrs, op->stab, op->rtab, nullptr)))
+        return rc;
+    KGB_CUDA_TRY(cudaDeviceSynchronize());
+    return KGB_OK;
+}
+
 }  // namespace kgb
 
 using namespace kgb;
@@ -125,7 +138,7 @@ int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni
         if (e != cudaSuccess) { rc = cuda_error(e, "upload wavelet"); break; }
         if ((rc = dev_alloc(&op->tsq, (size_t)ns * ni, "alloc source traveltimes"))) break;
         if ((rc = dev_alloc(&op->trq, (size_t)nr * ni, "alloc receiver traveltimes"))) break;
-        if ((rc = dev_alloc(&op->dcorr, (size_t)op->ndata(), "alloc correlation scratch"))) break;
+        if ((rc = dev_alloc(&op->dcorr, (size_t)2 * op->ndata(), "alloc correlation scratch"))) break;
         op->partial_elems = gather_partial_elems(op->view());
         if ((rc = dev_alloc(&op->partial, (size_t)op->partial_elems, "alloc partial images"))) break;
         if ((rc = dev_alloc(&op->mv, (size_t)ni, "alloc scaled model"))) break;
@@ -149,7 +162,7 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     cudaSetDevice(op->device);
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
                     op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
-                    op->mv, op->absmax};
+                    op->mv, op->absmax, op->stab, op->rtab};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);
@@ -207,7 +220,7 @@ int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* ts, const dou
     op->nonneg = (int64_t)qmin_s + (int64_t)qmin_r >= 0;
     (void)mins; (void)minr;
     op->trav_ready = true;
-    return KGB_OK;
+    return repack(op);
 }
 
 int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const double* amp_r,
@@ -297,7 +310,7 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const doub
     op->has_gate = gate;
     op->wmax = (float)std::max(wmax, 1e-30);
     op->dyn_ready = true;
-    return KGB_OK;
+    return repack(op);
 }
 
 static int check_ready(const kgb_kirchhoff* op) {
@@ -325,8 +338,9 @@ int kgb_kirchhoff_gather(kgb_kirchhoff* op, const float* d, float* m, void* stre
     int rc = check_ready(op);
     if (rc) return rc;
     if (!m || !d) return set_error(KGB_ERR_VALUE, "gather: null pointer");
-    return launch_gather(op->view(), op->dynamic, op->has_gate, d, m, op->partial, op->partial_elems,
-                         (cudaStream_t)stream);
+    cudaStream_t s = (cudaStream_t)stream;
+    if ((rc = launch_wavelet(d, op->dcorr, op->npair(), op->nt, nullptr, 1, 1, s))) return rc;
+    return launch_gather(op->view(), op->dynamic, op->has_gate, op->dcorr, m, op->partial, op->partial_elems, s);
 }
 
 int kgb_kirchhoff_adjoint(kgb_kirchhoff* op, const float* d, float* m, void* stream) {
@@ -334,14 +348,14 @@ int kgb_kirchhoff_adjoint(kgb_kirchhoff* op, const float* d, float* m, void* str
     if (rc) return rc;
     if (!m || !d) return set_error(KGB_ERR_VALUE, "adjoint: null pointer");
     cudaStream_t s = (cudaStream_t)stream;
-    if ((rc = launch_wavelet(d, op->dcorr, op->npair(), op->nt, op->hflip_dev, op->L, s))) return rc;
+    if ((rc = launch_wavelet(d, op->dcorr, op->npair(), op->nt, op->hflip_dev, op->L, 1, s))) return rc;
     return launch_gather(op->view(), op->dynamic, op->has_gate, op->dcorr, m, op->partial, op->partial_elems, s);
 }
 
 int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x, float* y, int adjoint, void* stream) {
     if (!op) return set_error(KGB_ERR_STATE, "null operator");
     if (!x || !y) return set_error(KGB_ERR_VALUE, "wavelet: null pointer");
-    return launch_wavelet(x, y, op->npair(), op->nt, adjoint ? op->hflip_dev : op->h_dev, op->L,
+    return launch_wavelet(x, y, op->npair(), op->nt, adjoint ? op->hflip_dev : op->h_dev, op->L, 0,
                           (cudaStream_t)stream);
 }
 

@@ -7,16 +7,20 @@
 //   forward:  y[pair, it] += x*(1-w)*W;  y[pair, it+1] += x*w*W
 //   adjoint:  img[ii] += (d[pair, it]*(1-w) + d[pair, it+1]*w)*W
 // with W = 1 (kinematic) or the dynamic weight
-//   W = 2 cos((a_s - a_r)/2) A_s A_r / v * taper_s * taper_r * offset_gate.
+//   W = 2 cos((a_s - a_r)/2) A_s A_r / v * taper_s * taper_r * offset_gate
+//     = (2/v) * (wc_s wc_r + ws_s ws_r) * offset_gate,
+//   wc = A taper cos(a/2), ws = A taper sin(a/2) (folded per table entry).
+// A pair-point whose weight is exactly zero (outside the angle aperture)
+// contributes exactly zero and is skipped before its data is touched.
 //
 // Traveltimes are stored as 32-bit fixed-point sample counts, so t/dt of a
 // source-receiver pair is one exact integer add: the integer part is a
 // shift, the fraction a mask, and the index decision is the reference's
 // float64 one except within 2^-frac_bits samples of a bin edge.
 //
-// Both kernels are deterministic: the adjoint sums each image point in a
-// fixed order, the forward accumulates in exact 64-bit fixed point, whose
-// integer additions commute.
+// Both directions are deterministic: the adjoint sums each image point in a
+// fixed order; the forward either accumulates exact 64-bit fixed point
+// (integer additions commute) or bins contributions per warp in lane order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -81,16 +85,39 @@ FixedPoint<NONNEG> make_fp(int F, int nt) {
     return fp;
 }
 
+// One table entry: traveltime (fixed point) and, in dynamic mode, weights.
+struct Entry {
+    int t;
+    float c, s;
+};
+
+template <bool DYN>
+__device__ __forceinline__ Entry load_entry(const int32_t* __restrict__ tq, const int4* __restrict__ tab,
+                                            size_t idx) {
+    Entry e;
+    if (DYN) {
+        const int4 v = __ldg(tab + idx);
+        e.t = v.x;
+        e.c = __int_as_float(v.y);
+        e.s = __int_as_float(v.z);
+    } else {
+        e.t = __ldg(tq + idx);
+        e.c = 1.f;
+        e.s = 0.f;
+    }
+    return e;
+}
+
 // ---------------------------------------------------------------------------
 // Adjoint: one thread per image point.  Each thread keeps kGatherRC receiver
-// traveltimes (and weights) in registers and sweeps every source of its
-// split against them, so table reads are ~1/kGatherRC per pair-point and
-// coalesced (a warp reads 128 contiguous bytes of a row).  The sum over
-// traces has a fixed order per image point.
+// entries in registers and sweeps every source of its split against them, so
+// table reads are ~1/kGatherRC per pair-point and coalesced.  The correlated
+// data is stored as interleaved pairs (d[it], d[it+1]) so one 8-byte load
+// feeds the interpolation.  The sum over traces has a fixed order.
 // ---------------------------------------------------------------------------
 template <bool DYN, bool GATE, bool NONNEG>
 __global__ void __launch_bounds__(kGatherThreads)
-gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float* __restrict__ d,
+gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __restrict__ d2,
               float* __restrict__ out, int s_per_split) {
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= K.ni) return;
@@ -100,52 +127,39 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float* __rest
     const int nt = K.nt;
     float total = 0.f;
     for (int r0 = 0; r0 < K.nr; r0 += kGatherRC) {
-        int trv[kGatherRC];
-        float rcv[kGatherRC], rsv[kGatherRC];
+        Entry re[kGatherRC];
         int roff[kGatherRC];
+        const int nrc = min(kGatherRC, K.nr - r0);
 #pragma unroll
         for (int r = 0; r < kGatherRC; ++r) {
-            const int ir = r0 + r;
-            trv[r] = 0;
-            rcv[r] = 0.f;
-            rsv[r] = 0.f;
             roff[r] = r * nt;
-            if (ir < K.nr) {
-                trv[r] = __ldg(K.trq + (size_t)ir * K.ni + ii);
-                if (DYN) {
-                    rcv[r] = __ldg(K.wrc + (size_t)ir * K.ni + ii);
-                    rsv[r] = __ldg(K.wrs + (size_t)ir * K.ni + ii);
-                }
-            }
+            re[r].t = 0;
+            re[r].c = 0.f;
+            re[r].s = 0.f;
+            if (r < nrc) re[r] = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
         }
-        const int nrc = min(kGatherRC, K.nr - r0);
         float chunk = 0.f;
+#pragma unroll 2
         for (int is = s_begin; is < s_end; ++is) {
-            const int ts = __ldg(K.tsq + (size_t)is * K.ni + ii);
-            float sc = 0.f, ss = 0.f;
-            if (DYN) {
-                sc = __ldg(K.wsc + (size_t)is * K.ni + ii);
-                ss = __ldg(K.wss + (size_t)is * K.ni + ii);
-            }
+            const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
+            if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
             const size_t pair0 = (size_t)is * K.nr + r0;
-            const float* __restrict__ drow = d + pair0 * nt;
+            const float2* __restrict__ drow = d2 + pair0 * nt;
 #pragma unroll
             for (int r = 0; r < kGatherRC; ++r) {
                 if (r < nrc) {
-                    const int s = ts + trv[r];
-                    if (fp.valid(s)) {
+                    const int s = se.t + re[r].t;
+                    float wt = 1.f;
+                    if (DYN) {
+                        wt = fmaf(se.c, re[r].c, se.s * re[r].s);
+                        if (GATE && iz < __ldg(K.izmin + pair0 + r)) wt = 0.f;
+                    }
+                    if (fp.valid(s) && (!DYN || wt != 0.f)) {
                         const int it = fp.index(s);
                         const float w = fp.frac(s, it);
-                        const float* p = drow + (roff[r] + it);
-                        const float d0 = __ldg(p);
-                        const float d1 = __ldg(p + 1);
-                        float val = fmaf(w, d1 - d0, d0);
-                        if (DYN) {
-                            float wt = fmaf(sc, rcv[r], ss * rsv[r]);
-                            if (GATE && iz < __ldg(K.izmin + pair0 + r)) wt = 0.f;
-                            val *= wt;
-                        }
-                        chunk += val;
+                        const float2 dd = __ldg(drow + (roff[r] + it));
+                        const float val = fmaf(w, dd.y - dd.x, dd.x);
+                        chunk = DYN ? fmaf(val, wt, chunk) : chunk + val;
                     }
                 }
             }
@@ -196,18 +210,19 @@ __device__ __forceinline__ int spread_scale_exponent(float amax, int64_t ni) {
     frexpf(amax, &ex);  // amax < 2^ex
     int nb = 0;
     while (nb < 40 && ((int64_t)1 << nb) <= ni) ++nb;
-    int e = 61 - nb - ex;
+    const int e = 61 - nb - ex;
     return max(-126, min(e, 126));
 }
 
-// Spreading, atomic variant: one CTA per (source, group of R receivers).  The CTA sweeps all
-// image points (one per thread per step), loads the source-side values once
-// per point and, for each of its R traces, accumulates the two contributions
-// v*(1-w), v*w into that trace's shared-memory time bins as 64-bit fixed
-// point: each contribution is scaled by a power of two chosen from a bound on
-// |v|, rounded to an integer (resolution ~2^-42 of the bound) and added
-// exactly, so the trace is independent of the order in which threads arrive.  The finished traces are converted back
-// to float, convolved with the wavelet in shared memory and written once.
+// Spreading, fixed-point variant: one CTA per (source, group of R receivers).
+// The CTA sweeps all image points (one per thread per step), loads the
+// source-side entry once per point and, for each of its R traces,
+// accumulates the two contributions v*(1-w), v*w into that trace's shared-
+// memory time bins as 64-bit fixed point: each contribution is scaled by a
+// power of two chosen from a bound on |v|, rounded to an integer (resolution
+// ~2^-42 of the bound) and added exactly, so the trace is independent of the
+// order in which threads arrive.  The finished traces are converted back to
+// float, convolved with the wavelet in shared memory and written once.
 template <bool DYN, bool GATE, bool NONNEG, int R>
 __global__ void __launch_bounds__(kSpreadThreads)
 spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
@@ -230,33 +245,29 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
     if (fuse)
         for (int k = tid; k < L; k += blockDim.x) hs[k] = h[k];
-    // fixed-point scale: every contribution |v S| < 2^(61 - log2(ni)), so a
-    // trace sample summing up to ni of them stays inside int64
     const int e = spread_scale_exponent(__uint_as_float(*K.absmax) * K.wmax, K.ni);
     const float S = ldexpf(1.f, e);
     int izmin[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
     __syncthreads();
-    const int32_t* __restrict__ tsrow = K.tsq + (size_t)is * K.ni;
     for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
         const float v = __ldg(K.mv + ii) * S;
         if (v == 0.f) continue;  // zero model point: no contribution
-        const int ts = __ldg(tsrow + ii);
-        float sc = 0.f, ss = 0.f;
-        if (DYN) {
-            sc = __ldg(K.wsc + (size_t)is * K.ni + ii);
-            ss = __ldg(K.wss + (size_t)is * K.ni + ii);
-        }
+        const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
+        if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
         const int iz = GATE ? (int)(ii % K.nz) : 0;
+        Entry re[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (r < nrr) re[r] = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (r < nrr) {
-                const size_t ro = (size_t)(r0 + r) * K.ni + ii;
-                const int s = ts + __ldg(K.trq + ro);
+                const int s = se.t + re[r].t;
                 float val = v;
                 if (DYN) {
-                    float wt = fmaf(sc, __ldg(K.wrc + ro), ss * __ldg(K.wrs + ro));
+                    float wt = fmaf(se.c, re[r].c, se.s * re[r].s);
                     if (GATE && iz < izmin[r]) wt = 0.f;
                     val *= wt;
                 }
@@ -333,9 +344,6 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
     int izmin[RT];
 #pragma unroll
     for (int r = 0; r < RT; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
-    const int32_t* __restrict__ tsrow = K.tsq + (size_t)is * K.ni;
-    const float* __restrict__ scrow = DYN ? K.wsc + (size_t)is * K.ni : nullptr;
-    const float* __restrict__ ssrow = DYN ? K.wss + (size_t)is * K.ni : nullptr;
     const int64_t ncol = K.ni / nz;
     const unsigned lower = (1u << lane) - 1u;
     for (int64_t col = 0; col < ncol; ++col) {
@@ -343,34 +351,35 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
             const int iz = iz0 + lane;
             const bool inb = iz < nz;
             const int64_t ii = col * nz + (inb ? iz : 0);
-            float v = 0.f, sc = 0.f, ss = 0.f;
-            int ts = 0;
+            float v = 0.f;
+            Entry se;
+            se.t = 0;
+            se.c = se.s = 0.f;
             if (inb) {
                 v = __ldg(K.mv + ii);
-                ts = __ldg(tsrow + ii);
-                if (DYN) {
-                    sc = __ldg(scrow + ii);
-                    ss = __ldg(ssrow + ii);
-                }
+                se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
+                if (DYN && se.c == 0.f && se.s == 0.f) v = 0.f;
             }
+            if (__ballot_sync(FULL, v != 0.f) == 0u) continue;
 #pragma unroll
             for (int r = 0; r < RT; ++r) {
                 if (r >= nrr) break;
-                const size_t ro = (size_t)(r0 + r) * K.ni + ii;
                 int s = 0;
                 float val = v;
-                if (inb) {
-                    s = ts + __ldg(K.trq + ro);
+                if (inb && v != 0.f) {
+                    const Entry re = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
+                    s = se.t + re.t;
                     if (DYN) {
-                        float wt = fmaf(sc, __ldg(K.wrc + ro), ss * __ldg(K.wrs + ro));
+                        float wt = fmaf(se.c, re.c, se.s * re.s);
                         if (GATE && iz < izmin[r]) wt = 0.f;
                         val *= wt;
                     }
                 }
-                const bool tv = inb && fp.valid(s);
+                const bool tv = inb && v != 0.f && fp.valid(s);
                 const int it = tv ? fp.index(s) : 0;
                 const bool contrib = tv && val != 0.f;
-                if (__ballot_sync(FULL, contrib) == 0u) continue;
+                const unsigned cm = __ballot_sync(FULL, contrib);
+                if (cm == 0u) continue;
                 float v0 = 0.f, v1 = 0.f;
                 if (contrib) {
                     const float w = fp.frac(s, it);
@@ -378,11 +387,14 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
                     v0 = val - v1;
                 }
                 float* tr = traces + r * nt_pad;
-                // strictly increasing bins over the time-valid prefix of lanes?
+                // the contributing lanes form one run of consecutive lanes with
+                // strictly increasing bins?
+                const int first = __ffs(cm) - 1;
+                const unsigned sh = cm >> first;
+                const bool run = (sh & (sh + 1u)) == 0u;
                 const int prev_it = __shfl_up_sync(FULL, it, 1);
-                const bool prev_tv = __shfl_up_sync(FULL, (int)tv, 1) != 0;
-                const bool ok = !tv || lane == 0 || (prev_tv && it > prev_it);
-                if (__all_sync(FULL, ok)) {
+                const bool ok = !contrib || lane == first || it > prev_it;
+                if (run && __all_sync(FULL, ok)) {
                     if (contrib) tr[it] += v0;
                     __syncwarp();
                     if (contrib) tr[it + 1] += v1;
@@ -432,31 +444,55 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
 }
 
 // ---------------------------------------------------------------------------
-// 'same'-mode FIR along time: y[n] = sum_k g[k] x[n + c - k], c = (L-1)/2.
+// 'same'-mode FIR along time: o[n] = sum_k g[k] x[n + c - k], c = (L-1)/2.
 // One block per trace (grid-stride), trace and taps staged in shared memory.
+// interleave = 1 writes (o[n], o[n+1]) pairs for the gather; g == nullptr
+// copies the trace (o = x).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, int nt,
-               const float* __restrict__ g, int L, int Lpad) {
+               const float* __restrict__ g, int L, int Lpad, int interleave) {
     extern __shared__ float smem[];
     float* gs = smem;
     float* xs = smem + Lpad;
-    for (int k = threadIdx.x; k < L; k += blockDim.x) gs[k] = g[k];
+    float* os = xs + ((nt + 3) & ~3);
+    if (g)
+        for (int k = threadIdx.x; k < L; k += blockDim.x) gs[k] = g[k];
     const int c = (L - 1) / 2;
     for (int64_t tr = blockIdx.x; tr < ntr; tr += gridDim.x) {
         __syncthreads();
         const float* xrow = x + tr * nt;
         for (int n = threadIdx.x; n < nt; n += blockDim.x) xs[n] = xrow[n];
         __syncthreads();
-        float* yrow = y + tr * nt;
         for (int n = threadIdx.x; n < nt; n += blockDim.x) {
-            const int kmin = max(0, n + c - (nt - 1));
-            const int kmax = min(L - 1, n + c);
-            float acc = 0.f;
-            for (int k = kmin; k <= kmax; ++k) acc = fmaf(gs[k], xs[n + c - k], acc);
-            yrow[n] = acc;
+            float acc;
+            if (g) {
+                const int kmin = max(0, n + c - (nt - 1));
+                const int kmax = min(L - 1, n + c);
+                acc = 0.f;
+                for (int k = kmin; k <= kmax; ++k) acc = fmaf(gs[k], xs[n + c - k], acc);
+            } else {
+                acc = xs[n];
+            }
+            os[n] = acc;
+        }
+        __syncthreads();
+        if (interleave) {
+            float2* yrow = reinterpret_cast<float2*>(y) + tr * nt;
+            for (int n = threadIdx.x; n < nt; n += blockDim.x)
+                yrow[n] = make_float2(os[n], n + 1 < nt ? os[n + 1] : 0.f);
+        } else {
+            float* yrow = y + tr * nt;
+            for (int n = threadIdx.x; n < nt; n += blockDim.x) yrow[n] = os[n];
         }
     }
+}
+
+// Dynamic-mode records {tq, wc, ws, 0}.
+__global__ void pack_tables_kernel(const int32_t* __restrict__ tq, const float* __restrict__ wc,
+                                   const float* __restrict__ ws, int4* __restrict__ tab, int64_t n) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        tab[k] = make_int4(tq[k], __float_as_int(wc[k]), __float_as_int(ws[k]), 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -492,7 +528,7 @@ int choose_split(int64_t blocks, int capacity, int ns) {
 }
 
 template <bool DYN, bool GATE, bool NONNEG>
-int gather_launch_t(const KirchDev& K, const float* d, float* img, float* partial, int64_t cap,
+int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* partial, int64_t cap,
                     cudaStream_t stream) {
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
@@ -503,7 +539,7 @@ int gather_launch_t(const KirchDev& K, const float* d, float* img, float* partia
     split = (K.ns + s_per - 1) / s_per;
     float* out = split > 1 ? partial : img;
     dim3 grid((unsigned)blocks, (unsigned)split);
-    gather_kernel<DYN, GATE, NONNEG><<<grid, kGatherThreads, 0, stream>>>(K, fp, d, out, s_per);
+    gather_kernel<DYN, GATE, NONNEG><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, s_per);
     KGB_CUDA_TRY(cudaGetLastError());
     if (split > 1) {
         const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
@@ -538,6 +574,15 @@ SpreadShape spread_shape(const KirchDev& K, int L) {
     return sh;
 }
 
+template <bool DYN>
+int launch_prepass(const KirchDev& K, const float* m, cudaStream_t stream) {
+    KGB_CUDA_TRY(cudaMemsetAsync(K.absmax, 0, sizeof(unsigned), stream));
+    const int pb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
+    spread_prepass_kernel<DYN><<<pb, 256, 0, stream>>>(K, m);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
 template <bool DYN, bool GATE, bool NONNEG, int R>
 int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                     const SpreadShape& sh, cudaStream_t stream, bool prepare_only) {
@@ -546,10 +591,8 @@ int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h,
         KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
         return KGB_OK;
     }
-    KGB_CUDA_TRY(cudaMemsetAsync(K.absmax, 0, sizeof(unsigned), stream));
-    const int pb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
-    spread_prepass_kernel<DYN><<<pb, 256, 0, stream>>>(K, m);
-    KGB_CUDA_TRY(cudaGetLastError());
+    int rc = launch_prepass<DYN>(K, m, stream);
+    if (rc) return rc;
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (int64_t)K.ns * ((K.nr + R - 1) / R);
     kern<<<(unsigned)blocks, kSpreadThreads, sh.smem, stream>>>(K, fp, y, h, L, sh.Lpad, sh.nt_pad, fuse ? 1 : 0);
@@ -572,10 +615,8 @@ int spread_binned_launch_r(const KirchDev& K, const float* m, float* y, const fl
         KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         return KGB_OK;
     }
-    const int pb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
-    KGB_CUDA_TRY(cudaMemsetAsync(K.absmax, 0, sizeof(unsigned), stream));
-    spread_prepass_kernel<DYN><<<pb, 256, 0, stream>>>(K, m);
-    KGB_CUDA_TRY(cudaGetLastError());
+    int rc = launch_prepass<DYN>(K, m, stream);
+    if (rc) return rc;
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int per_cta = warps * RT;
     const int64_t blocks = (int64_t)K.ns * ((K.nr + per_cta - 1) / per_cta);
@@ -587,21 +628,19 @@ int spread_binned_launch_r(const KirchDev& K, const float* m, float* y, const fl
 template <bool DYN, bool GATE, bool NONNEG>
 int spread_launch_t(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                     cudaStream_t stream, bool prepare_only) {
-    if (K.spread_variant == 1 || K.spread_variant == 2 || prepare_only) {
-        const int Lpad = (L + 3) & ~3;
-        const int nt_pad = (K.nt + 3) & ~3;
-        const bool fits2 = (size_t)(Lpad + 16 * (size_t)nt_pad) * 4 <= 227 * 1024;
-        int rc = KGB_OK;
-        if (prepare_only) {
-            if ((size_t)(Lpad + 8 * (size_t)nt_pad) * 4 <= 227 * 1024)
-                rc = spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, true);
-            if (!rc && fits2) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, true);
-            if (rc) return rc;
-        } else if (K.spread_variant == 2 && fits2) {
-            return spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, false);
-        } else {
-            return spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, false);
-        }
+    const int Lpad = (L + 3) & ~3;
+    const int nt_pad = (K.nt + 3) & ~3;
+    const bool fits1 = (size_t)(Lpad + 8 * (size_t)nt_pad) * 4 <= 227 * 1024;
+    const bool fits2 = (size_t)(Lpad + 16 * (size_t)nt_pad) * 4 <= 227 * 1024;
+    int rc = KGB_OK;
+    if (prepare_only) {
+        if (fits1) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, true);
+        if (!rc && fits2) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, true);
+        if (rc) return rc;
+    } else if (K.spread_variant == 2 && fits2) {
+        return spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, false);
+    } else if (K.spread_variant == 1 && fits1) {
+        return spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, false);
     }
     const SpreadShape sh = spread_shape(K, L);
     switch (sh.R) {
@@ -630,6 +669,11 @@ int spread_dispatch(const KirchDev& K, bool dynamic, bool gate, const float* m, 
     return spread_dispatch_nn<false, false>(K, m, y, h, L, fuse, stream, prep);
 }
 
+size_t wavelet_smem(int L, int nt) {
+    const int Lpad = (L + 3) & ~3;
+    return (size_t)(Lpad + 2 * ((nt + 3) & ~3)) * sizeof(float);
+}
+
 }  // namespace
 
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
@@ -650,16 +694,17 @@ int64_t gather_partial_elems(const KirchDev& K) {
 int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, float* img,
                   float* partial, int64_t cap, cudaStream_t stream) {
     if (K.ni <= 0 || K.ns <= 0 || K.nr <= 0) return KGB_OK;
+    const float2* d2 = reinterpret_cast<const float2*>(d);
     if (dynamic) {
         if (gate) {
-            if (K.nonneg) return gather_launch_t<true, true, true>(K, d, img, partial, cap, stream);
-            return gather_launch_t<true, true, false>(K, d, img, partial, cap, stream);
+            if (K.nonneg) return gather_launch_t<true, true, true>(K, d2, img, partial, cap, stream);
+            return gather_launch_t<true, true, false>(K, d2, img, partial, cap, stream);
         }
-        if (K.nonneg) return gather_launch_t<true, false, true>(K, d, img, partial, cap, stream);
-        return gather_launch_t<true, false, false>(K, d, img, partial, cap, stream);
+        if (K.nonneg) return gather_launch_t<true, false, true>(K, d2, img, partial, cap, stream);
+        return gather_launch_t<true, false, false>(K, d2, img, partial, cap, stream);
     }
-    if (K.nonneg) return gather_launch_t<false, false, true>(K, d, img, partial, cap, stream);
-    return gather_launch_t<false, false, false>(K, d, img, partial, cap, stream);
+    if (K.nonneg) return gather_launch_t<false, false, true>(K, d2, img, partial, cap, stream);
+    return gather_launch_t<false, false, false>(K, d2, img, partial, cap, stream);
 }
 
 int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,
@@ -677,28 +722,30 @@ int prepare_kernels(const KirchDev& K0, int L) {
             for (int gate = 0; gate < 2; ++gate)
                 if ((rc = spread_dispatch(K, dyn, gate, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     }
-    const int Lpad = (L + 3) & ~3;
-    const size_t smem = (size_t)(Lpad + K.nt) * sizeof(float);
+    const size_t smem = wavelet_smem(L, K.nt);
     if (smem <= 227 * 1024)
         KGB_CUDA_TRY(cudaFuncSetAttribute(wavelet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return KGB_OK;
 }
 
-int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L,
+int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L, int interleave,
                    cudaStream_t stream) {
     if (ntr <= 0 || nt <= 0) return KGB_OK;
     const int Lpad = (L + 3) & ~3;
-    const size_t smem = (size_t)(Lpad + nt) * sizeof(float);
+    const size_t smem = wavelet_smem(L, nt);
     if (smem > 227 * 1024)
         return set_error(KGB_ERR_NOT_IMPLEMENTED, "wavelet: nt=%d too long for shared memory", nt);
-    if (smem > 48 * 1024) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        cudaStreamIsCapturing(stream, &cs);
-        if (cs == cudaStreamCaptureStatusNone)
-            KGB_CUDA_TRY(cudaFuncSetAttribute(wavelet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    }
     const int64_t blocks = std::min<int64_t>(ntr, 8 * num_sms());
-    wavelet_kernel<<<(unsigned)blocks, 256, smem, stream>>>(x, y, ntr, nt, g, L, Lpad);
+    wavelet_kernel<<<(unsigned)blocks, 256, smem, stream>>>(x, y, ntr, nt, g, L, Lpad, interleave);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
+                       const float* wrs, int4* stab, int4* rtab, cudaStream_t stream) {
+    const int nb = 4 * num_sms();
+    pack_tables_kernel<<<nb, 256, 0, stream>>>(K.tsq, wsc, wss, stab, (int64_t)K.ns * K.ni);
+    pack_tables_kernel<<<nb, 256, 0, stream>>>(K.trq, wrc, wrs, rtab, (int64_t)K.nr * K.ni);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

@@ -126,6 +126,12 @@ class _DeviceSolver:
         return x, self.out.copy(), cost
 
 
+def _has_user_callback(solver) -> bool:
+    """True when a per-iteration ``callback`` was attached to the instance or
+    overridden in a subclass (the solve then steps from the host)."""
+    return "callback" in solver.__dict__ or type(solver).callback is not Solver.callback
+
+
 def _like_input(x_dev, ref):
     """Return a device result in the kind (numpy/torch) and dtype of the user's data."""
     if is_torch(ref):
@@ -237,7 +243,7 @@ class CGLS(Solver):
         niter = self.niter if niter is None else niter
         if niter is None:
             raise ValueError("niter must not be None")
-        if self._native and not show and not self.callbacks and type(self).callback is CGLS.callback:
+        if self._native and not show and not self.callbacks and not _has_user_callback(self):
             self._dev.run(niter - self.iiter, graph=True)
             x_dev = self._sync_native()
             return _like_input(x_dev, self.y)
@@ -494,7 +500,7 @@ class LSQR(Solver):
     def run(self, x, niter: Optional[int] = None, show: bool = False, itershow=(10, 10, 10)):
         """Iterate while ``iiter < niter and istop == 0`` (``cls_basic.py:1138-1186``)."""
         niter = self.niter if niter is None else niter
-        if self._native and not show and not self.callbacks and type(self).callback is LSQR.callback:
+        if self._native and not show and not self.callbacks and not _has_user_callback(self):
             self._dev.run(niter - self.iiter, graph=True)
             x_dev = self._sync_native()
             return _like_input(x_dev, self.y)
