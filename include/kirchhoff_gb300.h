@@ -85,6 +85,19 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_srcs_host,
  * Replaces: Kirchhoff._matvec (kirchhoff.py:1048-1094). */
 int kgb_kirchhoff_forward(kgb_kirchhoff* op, const float* m_dev, float* d_dev, void* stream);
 
+/* Forward d = K m exactly as kgb_kirchhoff_forward, but the call allocates
+ * nothing: its scratch (the model scaled by 2/v and that scale's maximum)
+ * lives in a static device array inside the library instead of buffers the
+ * operator owns.  For callers that must not call cudaMalloc while they run
+ * (a fixed device-memory budget, memory owned by a pool or caching
+ * allocator, latency-critical loops).  At most 4,194,304 image points
+ * (16 MiB of scratch, held on every GPU where the library's device code is
+ * loaded until exit); larger operators get KGB_ERR_VALUE.  All calls on a
+ * GPU share the array, so calls that overlap on the GPU race.  The first
+ * call on a device looks the array up (make it before any stream capture).
+ * No counterpart in the reference. */
+int kgb_kirchhoff_forward_static(kgb_kirchhoff* op, const float* m_dev, float* d_dev, void* stream);
+
 /* Adjoint m = K^H d: wavelet correlation then gathering.
  * Replaces: Kirchhoff._rmatvec (kirchhoff.py:1096-1143). */
 int kgb_kirchhoff_adjoint(kgb_kirchhoff* op, const float* d_dev, float* m_dev, void* stream);

@@ -48,6 +48,7 @@ _SIGNATURES = {
     "kgb_kirchhoff_set_dynamic": ([c_vp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_i64p, c_i64p], c_int),
     "kgb_kirchhoff_forward": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),
+    "kgb_kirchhoff_forward_static": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_forward_host": ([c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_adjoint_host": ([c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_spread": ([c_vp, c_vp, c_vp, c_vp], c_int),
