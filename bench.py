@@ -188,6 +188,16 @@ def _dist():
     return 0, 1, None
 
 
+def subset_sources(w, ns):
+    """Keep ns evenly spaced sources of the workload (small cases for ncu captures)."""
+    if ns and ns < w["ns"]:
+        idx = np.linspace(0, w["ns"] - 1, ns).round().astype(int)
+        w = dict(w)
+        w["srcs"] = w["srcs"][:, idx]
+        w["ns"] = ns
+    return w
+
+
 def build_operator(w):
     from pylops_gb300.waveeqprocessing import Kirchhoff
 
@@ -205,7 +215,7 @@ def run_gpu(args):
     rank, ws, dist = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    w = make_workload()
+    w = subset_sources(make_workload(), args.sources)
     K, t_setup = build_operator(w)
     L = _native.lib()
     rng = np.random.default_rng(7)
@@ -237,7 +247,7 @@ def run_gpu(args):
 
     # forward-kernel variants, timed on this workload; the fastest is used
     variant_ms = {}
-    for v in (0, 1, 2):
+    for v in ((0, 1, 2) if args.variant < 0 else (args.variant,)):
         K.set_spread_variant(v)
         step()
         torch.cuda.synchronize()
@@ -281,22 +291,24 @@ def run_gpu(args):
     y_dev = y.cpu().numpy().astype(np.float64)
 
     # e2e: public API, host numpy buffers (pinned), copies inside the timed region
+    if args.no_e2e:
+        args.steps_e2e = 0
     m_pin = torch.empty(K.ni, dtype=torch.float32, pin_memory=True).numpy()
     d_pin = torch.empty(K.nsnr * K.nt, dtype=torch.float32, pin_memory=True).numpy()
     m_pin[:] = m_host
     d_pin[:] = d_host
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, args.warmup) if args.steps_e2e else 0):
         K @ m_pin
         K.H @ d_pin
     torch.cuda.synchronize()
     te = []
-    for _ in range(args.steps):
+    xx = None
+    for _ in range(args.steps_e2e):
         t0 = time.perf_counter()
-        yy = K @ m_pin
+        K @ m_pin
         xx = K.H @ d_pin
         te.append(time.perf_counter() - t0)
-    e2e_s = statistics.median(te)
-    del yy
+    e2e_s = statistics.median(te) if te else float("nan")
 
     B = compulsory_bytes(K.ni, K.ns, K.nr, K.nt)
     ngpu = ws
@@ -342,12 +354,12 @@ def run_gpu(args):
                      "note": "compulsory bytes / launch time; the kernel is issue/gather bound, not HBM bound"},
         "gpu_launches": args.steps * (K.info()["kernels_forward"] + 1 + K.info()["kernels_adjoint"] - 1),
         "clocks": clk,
-        "e2e": {"value": round(B / e2e_s / 1e9, 3), "unit": "GB/s",
+        "e2e": {"value": round(B / e2e_s / 1e9, 3) if te else None, "unit": "GB/s",
                 "h2d_bytes_per_step": int(4 * K.ni + 4 * K.nsnr * K.nt),
                 "d2h_bytes_per_step": int(4 * K.nsnr * K.nt + 4 * K.ni),
-                "ms_per_step": round(e2e_s * 1e3, 3)},
+                "ms_per_step": round(e2e_s * 1e3, 3) if te else None},
     }
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline and not args.sources:
         cb, nsamp, yc, xc = cpu_baseline(K, m_host.astype(np.float64), d_host, target_s=args.cpu_seconds)
         out["cpu_baseline"] = cb
         rows = nsamp * K.nr
@@ -457,7 +469,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-sources", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
+    ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
+    ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
     args = ap.parse_args()
+    args.steps_e2e = args.steps
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":
         run_reference(args)

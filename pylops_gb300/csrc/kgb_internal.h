@@ -52,6 +52,10 @@ struct KirchDev {
     // a table entry's traveltime and both weights)
     const int4* stab;  // [ns][ni]
     const int4* rtab;  // [nr][ni]
+    // dynamic mode: per (row, depth column) the depth range [lo, hi) outside
+    // which the row's weight is exactly zero, packed lo | hi << 16
+    const uint32_t* srng;  // [ns][ncol]
+    const uint32_t* rrng;  // [nr][ncol]
 };
 
 // Launchers (kirchhoff_kernels.cu).  All asynchronous on `stream`.
@@ -66,9 +70,11 @@ int prepare_kernels(const KirchDev& K, int L);
 // gather reads with one 8-byte load.  g == nullptr copies (no filter).
 int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L,
                    int interleave, cudaStream_t stream);
-// Build the dynamic-mode records from the traveltime and weight arrays.
+// Build the dynamic-mode records and the active depth ranges from the
+// traveltime and weight arrays.
 int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
-                       const float* wrs, int4* stab, int4* rtab, cudaStream_t stream);
+                       const float* wrs, int4* stab, int4* rtab, uint32_t* srng, uint32_t* rrng,
+                       cudaStream_t stream);
 // How many float partial images launch_gather may use, and how many source
 // splits (partial images) it launches for this geometry.
 int64_t gather_partial_elems(const KirchDev& K);
@@ -109,6 +115,8 @@ struct kgb_kirchhoff {
     bool dyn_ready = false;
     int4* stab = nullptr;
     int4* rtab = nullptr;
+    uint32_t* srng = nullptr;
+    uint32_t* rrng = nullptr;
     float* dcorr = nullptr;    // scratch: correlated data for the adjoint, interleaved pairs (2 x ndata)
     float* partial = nullptr;  // scratch: per-split partial images
     int64_t partial_elems = 0;
@@ -124,7 +132,7 @@ struct kgb_kirchhoff {
         K.vscale = vscale; K.izmin = izmin;
         K.nonneg = nonneg ? 1 : 0; K.wmax = wmax; K.mv = mv; K.absmax = absmax;
         K.spread_variant = spread_variant;
-        K.stab = stab; K.rtab = rtab;
+        K.stab = stab; K.rtab = rtab; K.srng = srng; K.rrng = rrng;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

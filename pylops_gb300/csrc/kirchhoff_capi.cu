@@ -86,7 +86,11 @@ static int repack(kgb_kirchhoff* op) {
     int rc;
     if (!op->stab && (rc = dev_alloc(&op->stab, (size_t)op->ns * op->ni, "alloc source records"))) return rc;
     if (!op->rtab && (rc = dev_alloc(&op->rtab, (size_t)op->nr * op->ni, "alloc receiver records"))) return rc;
-    if ((rc = launch_pack_tables(op->view(), op->wsc, op->wss, op->wrc, op->wrs, op->stab, op->rtab, nullptr)))
+    const int64_t ncol = op->ni / op->nz;
+    if (!op->srng && (rc = dev_alloc(&op->srng, (size_t)op->ns * ncol, "alloc source ranges"))) return rc;
+    if (!op->rrng && (rc = dev_alloc(&op->rrng, (size_t)op->nr * ncol, "alloc receiver ranges"))) return rc;
+    if ((rc = launch_pack_tables(op->view(), op->wsc, op->wss, op->wrc, op->wrs, op->stab, op->rtab, op->srng,
+                                 op->rrng, nullptr)))
         return rc;
     KGB_CUDA_TRY(cudaDeviceSynchronize());
     return KGB_OK;
@@ -106,7 +110,7 @@ int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni
                          int dynamic, const double* wav, int nwav, int wavcenter) {
     if (!out) return set_error(KGB_ERR_VALUE, "create: null output handle");
     *out = nullptr;
-    if (ns <= 0 || nr <= 0 || nt < 2 || ni <= 0 || nz <= 0 || ni % nz != 0)
+    if (ns <= 0 || nr <= 0 || nt < 2 || ni <= 0 || nz <= 0 || ni % nz != 0 || nz > 32767)
         return set_error(KGB_ERR_VALUE, "create: bad sizes ns=%d nr=%d nt=%d ni=%lld nz=%d", ns, nr, nt,
                          (long long)ni, nz);
     if (!(dt > 0.0) || !isfinite(dt)) return set_error(KGB_ERR_VALUE, "create: dt must be positive");
@@ -162,7 +166,7 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     cudaSetDevice(op->device);
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
                     op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
-                    op->mv, op->absmax, op->stab, op->rtab};
+                    op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);

@@ -91,21 +91,37 @@ struct Entry {
     float c, s;
 };
 
-template <bool DYN>
+// STREAM: the record is read once per application (evict-first in L1 and
+// L2, so the caches keep what is reused: data traces, model, re-read rows).
+template <bool DYN, bool STREAM = false>
 __device__ __forceinline__ Entry load_entry(const int32_t* __restrict__ tq, const int4* __restrict__ tab,
                                             size_t idx) {
     Entry e;
     if (DYN) {
-        const int4 v = __ldg(tab + idx);
+        const int4 v = STREAM ? __ldcs(tab + idx) : __ldg(tab + idx);
         e.t = v.x;
         e.c = __int_as_float(v.y);
         e.s = __int_as_float(v.z);
     } else {
-        e.t = __ldg(tq + idx);
+        e.t = STREAM ? __ldcs(tq + idx) : __ldg(tq + idx);
         e.c = 1.f;
         e.s = 0.f;
     }
     return e;
+}
+
+__device__ __forceinline__ Entry zero_entry() {
+    Entry e;
+    e.t = 0;
+    e.c = 0.f;
+    e.s = 0.f;
+    return e;
+}
+
+// Is depth iz inside a row's active range (packed lo | hi << 16) for this column?
+__device__ __forceinline__ bool in_range(const uint32_t* __restrict__ rng, size_t idx, int iz) {
+    const uint32_t v = __ldg(rng + idx);
+    return iz >= (int)(v & 0xffffu) && iz < (int)(v >> 16);
 }
 
 // ---------------------------------------------------------------------------
@@ -116,31 +132,45 @@ __device__ __forceinline__ Entry load_entry(const int32_t* __restrict__ tq, cons
 // feeds the interpolation.  The sum over traces has a fixed order.
 // ---------------------------------------------------------------------------
 template <bool DYN, bool GATE, bool NONNEG>
-__global__ void __launch_bounds__(kGatherThreads)
+__global__ void __launch_bounds__(kGatherThreads, 4)
 gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __restrict__ d2,
               float* __restrict__ out, int s_per_split) {
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= K.ni) return;
     const int s_begin = blockIdx.y * s_per_split;
     const int s_end = min(K.ns, s_begin + s_per_split);
-    const int iz = GATE ? (int)(ii % K.nz) : 0;
+    int64_t col = 0;
+    int iz = 0;
+    if (DYN || GATE) {
+        col = ii / K.nz;
+        iz = (int)(ii - col * K.nz);
+    }
+    const int64_t ncol = K.ni / K.nz;
     const int nt = K.nt;
+    // dynamic: which sources of this split are active at this image point
+    // (sources beyond the first 64 of the split are always tested)
+    unsigned long long smask = ~0ull;
+    if (DYN) {
+        smask = 0ull;
+        for (int is = s_begin; is < min(s_end, s_begin + 64); ++is)
+            if (in_range(K.srng, (size_t)is * ncol + col, iz)) smask |= 1ull << (is - s_begin);
+    }
     float total = 0.f;
     for (int r0 = 0; r0 < K.nr; r0 += kGatherRC) {
         Entry re[kGatherRC];
-        int roff[kGatherRC];
         const int nrc = min(kGatherRC, K.nr - r0);
 #pragma unroll
         for (int r = 0; r < kGatherRC; ++r) {
-            roff[r] = r * nt;
-            re[r].t = 0;
-            re[r].c = 0.f;
-            re[r].s = 0.f;
-            if (r < nrc) re[r] = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
+            re[r] = zero_entry();
+            if (r < nrc) re[r] = load_entry<DYN, true>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
         }
         float chunk = 0.f;
 #pragma unroll 2
         for (int is = s_begin; is < s_end; ++is) {
+            if (DYN) {
+                const int k = is - s_begin;
+                if (k < 64 ? !((smask >> k) & 1ull) : !in_range(K.srng, (size_t)is * ncol + col, iz)) continue;
+            }
             const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
             if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
             const size_t pair0 = (size_t)is * K.nr + r0;
@@ -157,7 +187,7 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
                     if (fp.valid(s) && (!DYN || wt != 0.f)) {
                         const int it = fp.index(s);
                         const float w = fp.frac(s, it);
-                        const float2 dd = __ldg(drow + (roff[r] + it));
+                        const float2 dd = __ldg(drow + ((size_t)r * nt + it));
                         const float val = fmaf(w, dd.y - dd.x, dd.x);
                         chunk = DYN ? fmaf(val, wt, chunk) : chunk + val;
                     }
@@ -224,7 +254,7 @@ __device__ __forceinline__ int spread_scale_exponent(float amax, int64_t ni) {
 // order in which threads arrive.  The finished traces are converted back to
 // float, convolved with the wavelet in shared memory and written once.
 template <bool DYN, bool GATE, bool NONNEG, int R>
-__global__ void __launch_bounds__(kSpreadThreads)
+__global__ void __launch_bounds__(kSpreadThreads, 2)
 spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
               const float* __restrict__ h, int L, int Lpad, int nt_pad, int fuse) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -251,16 +281,30 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
 #pragma unroll
     for (int r = 0; r < R; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
     __syncthreads();
+    const int64_t ncol = K.ni / K.nz;
+    // depth column and depth of this thread's point, advanced incrementally
+    int64_t col = tid / K.nz;
+    int iz = tid - (int)(col * K.nz);
+    const int64_t stride_col = (int64_t)blockDim.x / K.nz;
+    const int stride_iz = blockDim.x - (int)(stride_col * K.nz);
     for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
+        const int64_t colp = col;
+        const int izp = iz;
+        col += stride_col;
+        iz += stride_iz;
+        if (iz >= K.nz) {
+            iz -= K.nz;
+            ++col;
+        }
         const float v = __ldg(K.mv + ii) * S;
         if (v == 0.f) continue;  // zero model point: no contribution
+        if (DYN && !in_range(K.srng, (size_t)is * ncol + colp, izp)) continue;  // source weight zero here
         const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
         if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
-        const int iz = GATE ? (int)(ii % K.nz) : 0;
+        // all R receiver records in flight before any is used
         Entry re[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-            if (r < nrr) re[r] = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
+        for (int r = 0; r < R; ++r) re[r] = r < nrr ? load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii) : zero_entry();
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (r < nrr) {
@@ -268,7 +312,7 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
                 float val = v;
                 if (DYN) {
                     float wt = fmaf(se.c, re[r].c, se.s * re[r].s);
-                    if (GATE && iz < izmin[r]) wt = 0.f;
+                    if (GATE && izp < izmin[r]) wt = 0.f;
                     val *= wt;
                 }
                 if (fp.valid(s) && val != 0.f) {
@@ -300,7 +344,7 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
             } else {
                 o = ftr[n];
             }
-            yrow[n] = o;
+            __stcs(yrow + n, o);
         }
         __syncthreads();
     }
@@ -357,16 +401,20 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
             se.c = se.s = 0.f;
             if (inb) {
                 v = __ldg(K.mv + ii);
-                se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
-                if (DYN && se.c == 0.f && se.s == 0.f) v = 0.f;
+                if (DYN && !in_range(K.srng, (size_t)is * ncol + col, iz)) v = 0.f;
+                if (v != 0.f) {
+                    se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
+                    if (DYN && se.c == 0.f && se.s == 0.f) v = 0.f;
+                }
             }
             if (__ballot_sync(FULL, v != 0.f) == 0u) continue;
 #pragma unroll
             for (int r = 0; r < RT; ++r) {
                 if (r >= nrr) break;
                 int s = 0;
-                float val = v;
-                if (inb && v != 0.f) {
+                float val = 0.f;  // stays 0 for a receiver outside its active range
+                if (inb && v != 0.f && (!DYN || in_range(K.rrng, (size_t)(r0 + r) * ncol + col, iz))) {
+                    val = v;
                     const Entry re = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
                     s = se.t + re.t;
                     if (DYN) {
@@ -375,7 +423,7 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
                         val *= wt;
                     }
                 }
-                const bool tv = inb && v != 0.f && fp.valid(s);
+                const bool tv = inb && val != 0.f && fp.valid(s);
                 const int it = tv ? fp.index(s) : 0;
                 const bool contrib = tv && val != 0.f;
                 const unsigned cm = __ballot_sync(FULL, contrib);
@@ -493,6 +541,26 @@ __global__ void pack_tables_kernel(const int32_t* __restrict__ tq, const float* 
                                    const float* __restrict__ ws, int4* __restrict__ tab, int64_t n) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
         tab[k] = make_int4(tq[k], __float_as_int(wc[k]), __float_as_int(ws[k]), 0);
+}
+
+// Per (row, depth column): smallest and one-past-largest depth with a
+// nonzero weight (lo = hi = 0 when the whole column is zero).
+__global__ void range_kernel(const float* __restrict__ wc, const float* __restrict__ ws, uint32_t* __restrict__ rng,
+                             int64_t nrows, int64_t ncol, int nz) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nrows * ncol;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = k / ncol, col = k - row * ncol;
+        const size_t base = (size_t)row * ncol * nz + (size_t)col * nz;
+        int lo = -1, hi = 0;
+        for (int iz = 0; iz < nz; ++iz) {
+            if (wc[base + iz] != 0.f || ws[base + iz] != 0.f) {
+                if (lo < 0) lo = iz;
+                hi = iz + 1;
+            }
+        }
+        if (lo < 0) lo = hi = 0;
+        rng[k] = (uint32_t)lo | ((uint32_t)hi << 16);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -742,10 +810,14 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
 }
 
 int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
-                       const float* wrs, int4* stab, int4* rtab, cudaStream_t stream) {
+                       const float* wrs, int4* stab, int4* rtab, uint32_t* srng, uint32_t* rrng,
+                       cudaStream_t stream) {
     const int nb = 4 * num_sms();
     pack_tables_kernel<<<nb, 256, 0, stream>>>(K.tsq, wsc, wss, stab, (int64_t)K.ns * K.ni);
     pack_tables_kernel<<<nb, 256, 0, stream>>>(K.trq, wrc, wrs, rtab, (int64_t)K.nr * K.ni);
+    const int64_t ncol = K.ni / K.nz;
+    range_kernel<<<nb, 256, 0, stream>>>(wsc, wss, srng, K.ns, ncol, K.nz);
+    range_kernel<<<nb, 256, 0, stream>>>(wrc, wrs, rrng, K.nr, ncol, K.nz);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
