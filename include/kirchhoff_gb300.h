@@ -133,7 +133,7 @@ int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant);
 /* Introspection used by the host wrapper and the tests.  info16 receives
  * {ns, nr, nt, ni, fixed-point fraction bits, padded wavelet length,
  *  offset-aperture gate active, dynamic, all times non-negative,
- *  adjoint source splits, kernels per forward, kernels per adjoint,
+ *  adjoint receiver splits, kernels per forward, kernels per adjoint,
  *  spread variant, 0...}. */
 int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* info16);
 

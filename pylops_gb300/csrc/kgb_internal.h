@@ -75,7 +75,7 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
 int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
                        const float* wrs, int4* stab, int4* rtab, uint32_t* srng, uint32_t* rrng,
                        cudaStream_t stream);
-// How many float partial images launch_gather may use, and how many source
+// How many float partial images launch_gather may use, and how many receiver
 // splits (partial images) it launches for this geometry.
 int64_t gather_partial_elems(const KirchDev& K);
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate);
@@ -118,7 +118,7 @@ struct kgb_kirchhoff {
     uint32_t* srng = nullptr;
     uint32_t* rrng = nullptr;
     float* dcorr = nullptr;    // scratch: correlated data for the adjoint, interleaved pairs (2 x ndata)
-    float* partial = nullptr;  // scratch: per-split partial images
+    float* partial = nullptr;  // scratch: per-receiver-split partial images
     int64_t partial_elems = 0;
     float* m_stage = nullptr;  // device staging for the host-buffer entry points
     float* d_stage = nullptr;

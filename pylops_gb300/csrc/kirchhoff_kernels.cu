@@ -126,19 +126,23 @@ __device__ __forceinline__ bool in_range(const uint32_t* __restrict__ rng, size_
 
 // ---------------------------------------------------------------------------
 // Adjoint: one thread per image point.  Each thread keeps kGatherRC receiver
-// entries in registers and sweeps every source of its split against them, so
-// table reads are ~1/kGatherRC per pair-point and coalesced.  The correlated
+// entries in registers and sweeps every source against them, so table reads
+// are ~1/kGatherRC per pair-point and coalesced.  The correlated
 // data is stored as interleaved pairs (d[it], d[it+1]) so one 8-byte load
 // feeds the interpolation.  The sum over traces has a fixed order.
 // ---------------------------------------------------------------------------
 template <bool DYN, bool GATE, bool NONNEG>
 __global__ void __launch_bounds__(kGatherThreads, 4)
 gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __restrict__ d2,
-              float* __restrict__ out, int s_per_split) {
+              float* __restrict__ out, int r_per_split) {
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (ii >= K.ni) return;
-    const int s_begin = blockIdx.y * s_per_split;
-    const int s_end = min(K.ns, s_begin + s_per_split);
+    // blockIdx.y selects a range of receivers: every split sweeps all sources,
+    // which are re-streamed per receiver chunk anyway, so splitting adds no
+    // table traffic
+    const int s_begin = 0, s_end = K.ns;
+    const int r_begin = blockIdx.y * r_per_split;
+    const int r_end = min(K.nr, r_begin + r_per_split);
     int64_t col = 0;
     int iz = 0;
     if (DYN || GATE) {
@@ -156,9 +160,9 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
             if (in_range(K.srng, (size_t)is * ncol + col, iz)) smask |= 1ull << (is - s_begin);
     }
     float total = 0.f;
-    for (int r0 = 0; r0 < K.nr; r0 += kGatherRC) {
+    for (int r0 = r_begin; r0 < r_end; r0 += kGatherRC) {
         Entry re[kGatherRC];
-        const int nrc = min(kGatherRC, K.nr - r0);
+        const int nrc = min(kGatherRC, r_end - r0);
 #pragma unroll
         for (int r = 0; r < kGatherRC; ++r) {
             re[r] = zero_entry();
@@ -577,14 +581,16 @@ int gather_blocks_per_sm() {
     return cached;
 }
 
-// Number of source splits that keeps the last wave of the gather grid full.
-int choose_split(int64_t blocks, int capacity, int ns) {
+// Number of receiver splits (ranges of whole register chunks) that keeps the
+// last wave of the gather grid full.
+int choose_split(int64_t blocks, int capacity, int nr) {
     int best = 1;
     double best_eff = 0.0;
-    const int maxs = std::min(kMaxSplit, ns);
+    const int nchunks = (nr + kGatherRC - 1) / kGatherRC;
+    const int maxs = std::min(kMaxSplit, nchunks);
     for (int s = 1; s <= maxs; ++s) {
-        const int s_per = (ns + s - 1) / s;
-        const int sp = (ns + s_per - 1) / s_per;
+        const int c_per = (nchunks + s - 1) / s;
+        const int sp = (nchunks + c_per - 1) / c_per;
         const double waves = (double)(blocks * sp) / capacity;
         const double eff = waves / std::ceil(waves) * (waves >= 1.0 ? 1.0 : waves);
         if (eff > best_eff + 0.02) {
@@ -601,13 +607,14 @@ int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* part
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
     const int capacity = num_sms() * gather_blocks_per_sm<DYN, GATE, NONNEG>();
-    int split = choose_split(blocks, capacity, K.ns);
+    int split = choose_split(blocks, capacity, K.nr);
     if (partial == nullptr || cap < (int64_t)split * K.ni) split = 1;
-    const int s_per = (K.ns + split - 1) / split;
-    split = (K.ns + s_per - 1) / s_per;
+    const int nchunks = (K.nr + kGatherRC - 1) / kGatherRC;
+    const int c_per = (nchunks + split - 1) / split;
+    split = (nchunks + c_per - 1) / c_per;
     float* out = split > 1 ? partial : img;
     dim3 grid((unsigned)blocks, (unsigned)split);
-    gather_kernel<DYN, GATE, NONNEG><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, s_per);
+    gather_kernel<DYN, GATE, NONNEG><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
     KGB_CUDA_TRY(cudaGetLastError());
     if (split > 1) {
         const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
@@ -750,13 +757,14 @@ int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
     if (dynamic) bps = gate ? (K.nonneg ? gather_blocks_per_sm<true, true, true>() : gather_blocks_per_sm<true, true, false>())
                             : (K.nonneg ? gather_blocks_per_sm<true, false, true>() : gather_blocks_per_sm<true, false, false>());
     else bps = K.nonneg ? gather_blocks_per_sm<false, false, true>() : gather_blocks_per_sm<false, false, false>();
-    int split = choose_split(blocks, num_sms() * bps, K.ns);
-    const int s_per = (K.ns + split - 1) / split;
-    return (K.ns + s_per - 1) / s_per;
+    int split = choose_split(blocks, num_sms() * bps, K.nr);
+    const int nchunks = (K.nr + kGatherRC - 1) / kGatherRC;
+    const int c_per = (nchunks + split - 1) / split;
+    return (nchunks + c_per - 1) / c_per;
 }
 
 int64_t gather_partial_elems(const KirchDev& K) {
-    return (int64_t)std::min(kMaxSplit, K.ns) * K.ni;
+    return (int64_t)std::min(kMaxSplit, (K.nr + kGatherRC - 1) / kGatherRC) * K.ni;
 }
 
 int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, float* img,
