@@ -460,6 +460,49 @@ class _HostTables:
         self.rix = np.tile((w["recs"][0] - x[0]) // dx, (self.ns, 1)).astype(int).ravel()
 
 
+def run_batch(args):
+    """Batched LSM workload (256 independent 2-D kinematic problems of random
+    size, 20 CGLS iterations each, one CUDA-graph launch).  A step is one
+    batched CGLS solve; value = compulsory GB/s of its 2*20+2 operator
+    applications."""
+    import torch
+
+    from pylops_gb300.waveeqprocessing.batch import build_batch, random_problems
+
+    t0 = time.perf_counter()
+    probs = random_problems(args.batch_problems, seed=3)
+    B = build_batch(probs)
+    tune = B.autotune(candidates=(2, 4, 8), reps=2)
+    t_setup = time.perf_counter() - t0
+    y = torch.cat([torch.as_tensor(K @ p["refl"].ravel().astype(np.float32), device="cuda")
+                   for K, p in zip(B.ops, probs)])
+    for _ in range(args.warmup):
+        B.cgls(y, niter=args.cgls_iters, tol=0.0)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x, iiter, kold, cost = B.cgls(y, niter=args.cgls_iters, tol=0.0)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    step = statistics.median(ts)
+    napply = 2 * args.cgls_iters + 2
+    Bytes = sum(compulsory_bytes(K.ni, K.ns, K.nr, K.nt, s_tab=4) for K in B.ops) / 2 * napply
+    rels = [float(c[-1] / c[0]) for c in cost]
+    print(json.dumps({
+        "metric": "batched LSM (CGLS) GB/s and problems/s", "value": round(Bytes / step / 1e9, 3), "unit": "GB/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched_lsm_256x2d_kinematic_nt501", "problems": len(B.ops),
+                   "cgls_iterations": args.cgls_iters, "model_total": B.shape[1], "data_total": B.shape[0],
+                   "tile_ms": {str(k): round(v, 3) for k, v in tune.items()}, "tile": B.tile,
+                   "setup_s": round(t_setup, 2)},
+        "problems_per_s": round(len(B.ops) / step, 2),
+        "residual_reduction_median": round(float(np.median(rels)), 5),
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -472,11 +515,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch"],
+                    help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems")
+    ap.add_argument("--batch-problems", type=int, default=256)
+    ap.add_argument("--cgls-iters", type=int, default=20)
     args = ap.parse_args()
     args.steps_e2e = args.steps
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_gpu(args)
 

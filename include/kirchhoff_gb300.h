@@ -175,6 +175,30 @@ int kgb_solver_run(kgb_solver* s, int niter, int use_graph, void* stream);
 int kgb_solver_result(kgb_solver* s, float* x_dev, double* out16_host, double* cost_host,
                       int cost_capacity, void* stream);
 
+/* ---- batched least-squares migration ------------------------------------
+ * A batch is the block-diagonal operator diag(K_1..K_P) of P kinematic
+ * operators (created and filled as above; the batch keeps pointers to their
+ * device tables, which must outlive it) over the concatenated models
+ * (sum ni_p) and data (sum ns_p*nr_p*nt_p), problem by problem in order.
+ * Each application is a single launch per kernel over a work list covering
+ * every problem.  kgb_batch_cgls runs CGLS (x0 = 0) on every problem at once
+ * with per-problem float64 scalars, replaying one captured iteration in a
+ * CUDA-graph WHILE node until every problem meets its stopping rule or has
+ * done niter iterations.  cost_host (may be NULL) receives P rows of
+ * niter+1 residual norms (row-major), iiter_host / kold_host (may be NULL)
+ * P values each.
+ * Replaces: a Python loop of LSM problems, each driving CGLS
+ * (cls_basic.py:334-708) over its own Kirchhoff operator. */
+typedef struct kgb_batch kgb_batch;
+int kgb_batch_create(kgb_batch** batch, kgb_kirchhoff* const* ops, int nops);
+int kgb_batch_destroy(kgb_batch* batch);
+int kgb_batch_sizes(const kgb_batch* batch, int64_t* sizes4); /* {P, model, data, tile} */
+int kgb_batch_set_tile(kgb_batch* batch, int receivers_per_item); /* 1, 2, 4 or 8 (autotuner) */
+int kgb_batch_forward(kgb_batch* batch, const float* m_dev, float* d_dev, void* stream);
+int kgb_batch_adjoint(kgb_batch* batch, const float* d_dev, float* m_dev, void* stream);
+int kgb_batch_cgls(kgb_batch* batch, const float* y_dev, float* x_dev, int niter, double damp, double tol,
+                   int use_graph, double* cost_host, int* iiter_host, double* kold_host, void* stream);
+
 /* ---- table builder ------------------------------------------------------
  * First-arrival traveltimes (and, if dist_out != NULL, distances) from npts
  * point sources by fast marching on a regular grid of ndim (2 or 3) axes

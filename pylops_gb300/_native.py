@@ -62,6 +62,13 @@ _SIGNATURES = {
     "kgb_solver_setup": ([c_vp, c_vp, c_vp, c_dp, c_int, c_vp], c_int),
     "kgb_solver_run": ([c_vp, c_int, c_int, c_vp], c_int),
     "kgb_solver_result": ([c_vp, c_vp, c_dp, c_dp, c_int, c_vp], c_int),
+    "kgb_batch_create": ([ctypes.POINTER(c_vp), ctypes.POINTER(c_vp), c_int], c_int),
+    "kgb_batch_destroy": ([c_vp], c_int),
+    "kgb_batch_sizes": ([c_vp, c_i64p], c_int),
+    "kgb_batch_set_tile": ([c_vp, c_int], c_int),
+    "kgb_batch_forward": ([c_vp, c_vp, c_vp, c_vp], c_int),
+    "kgb_batch_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),
+    "kgb_batch_cgls": ([c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_int, c_dp, c_ip, c_dp, c_vp], c_int),
     "kgb_eikonal_tables": ([c_int, c_ip, c_dp, c_dp, c_int, c_ip, c_dp, c_dp, c_int, c_int], c_int),
 }
 
