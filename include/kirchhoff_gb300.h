@@ -199,6 +199,18 @@ int kgb_batch_adjoint(kgb_batch* batch, const float* d_dev, float* m_dev, void* 
 int kgb_batch_cgls(kgb_batch* batch, const float* y_dev, float* x_dev, int niter, double damp, double tol,
                    int use_graph, double* cost_host, int* iiter_host, double* kold_host, void* stream);
 
+/* ---- tensor-core GEMM (U-Net preconditioner) ------------------------------
+ * C[m][n] = sum_k A[m][k] B[n][k] (+ bias[n]) (ReLU if flags & 1), A (M x K,
+ * leading dimension lda) and B (N x K, ldb) bf16 row-major with K contiguous,
+ * C float32 (or bf16 if flags & 2) with leading dimension ldc.  K, lda and
+ * ldb must be multiples of 8 and A, B 16-byte aligned.  tcgen05 MMAs with
+ * tensor-memory accumulators and TMA-loaded operands; err_dev (may be NULL)
+ * is set to 1 if a pipeline wait timed out.  No reference counterpart: the
+ * learned preconditioner is new (its training and inference convolutions
+ * are lowered to this GEMM). */
+int kgb_gemm_bf16_tn(const void* A_dev, const void* B_dev, void* C_dev, int M, int N, int K, int lda, int ldb,
+                     int ldc, const float* bias_dev, int flags, int* err_dev, void* stream);
+
 /* ---- table builder ------------------------------------------------------
  * First-arrival traveltimes (and, if dist_out != NULL, distances) from npts
  * point sources by fast marching on a regular grid of ndim (2 or 3) axes

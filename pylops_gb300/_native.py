@@ -69,6 +69,7 @@ _SIGNATURES = {
     "kgb_batch_forward": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_batch_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_batch_cgls": ([c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_int, c_dp, c_ip, c_dp, c_vp], c_int),
+    "kgb_gemm_bf16_tn": ([c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_vp, c_int, c_vp, c_vp], c_int),
     "kgb_eikonal_tables": ([c_int, c_ip, c_dp, c_dp, c_int, c_ip, c_dp, c_dp, c_int, c_int], c_int),
 }
 
