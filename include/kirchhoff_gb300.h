@@ -143,6 +143,14 @@ int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* info16);
  * CGLS/LSQR take with ncp.linalg.norm / .dot (cls_basic.py:497-564, 976-1136). */
 int kgb_dot_f64(const float* a_dev, const float* b_dev, int64_t n, double* out_dev, void* stream);
 
+/* out = base_coef * base + sum_{j<k} coefs[j] * vecs[j] over n floats (base
+ * may be NULL; k <= 16; vecs and coefs are host arrays of device pointers
+ * and coefficients).  One pass, fixed summation order.  Used by the
+ * flexible (network-preconditioned) steps of the learned LSM solve; no
+ * reference counterpart. */
+int kgb_lincomb_f32(float* out_dev, const float* base_dev, double base_coef, const float* const* vecs,
+                    const double* coefs, int k, int64_t n, void* stream);
+
 /* ---- solvers: device-resident CGLS / LSQR ------------------------------
  * The vectors live on the device in float32, every dot product, norm and
  * scalar recurrence is float64 on the device, and one iteration (both
@@ -156,6 +164,14 @@ typedef struct kgb_solver kgb_solver;
 /* kind: 0 = CGLS, 1 = LSQR.  The solver keeps a reference to op. */
 int kgb_solver_create(kgb_solver** s, kgb_kirchhoff* op, int kind);
 int kgb_solver_destroy(kgb_solver* s);
+
+/* Right preconditioner: with p_dev (ni floats, device, kept by reference;
+ * NULL removes it) the solver inverts K diag(p) instead of K, and x, x0 and
+ * the model-space state are in the preconditioned variable z (x = p * z),
+ * as the reference solvers do on `Kop * Diagonal(p)`
+ * (basicoperators/diagonal.py:92-105, linearoperator.py:612-702).  Call
+ * before kgb_solver_setup. */
+int kgb_solver_set_diagonal(kgb_solver* s, const float* p_dev);
 
 /* Setup with data y (ns*nr*nt) and optional x0 (ni, may be NULL).  params:
  * CGLS {damp, tol}; LSQR {damp, atol, btol, conlim}.  Replaces the setup
@@ -210,6 +226,59 @@ int kgb_batch_cgls(kgb_batch* batch, const float* y_dev, float* x_dev, int niter
  * are lowered to this GEMM). */
 int kgb_gemm_bf16_tn(const void* A_dev, const void* B_dev, void* C_dev, int M, int N, int K, int lda, int ldb,
                      int ldc, const float* bias_dev, int flags, int* err_dev, void* stream);
+
+/* Split-K form for reductions over many pixels (weight gradients): C
+ * (float32) = A . B^T with the K range cut into `splits` slices (<= 0:
+ * chosen to fill the GPU) computed into `work` (splits x M x N floats, at
+ * most work_elems; fewer splits if it is smaller) and summed in slice order,
+ * so the result is deterministic.  No reference counterpart. */
+int kgb_gemm_bf16_tn_splitk(const void* A_dev, const void* B_dev, float* C_dev, int M, int N, int K, int lda,
+                            int ldb, int ldc, int splits, float* work_dev, int64_t work_elems, int* err_dev,
+                            void* stream);
+
+/* ---- U-Net helper kernels (NHWC bf16 activations) ------------------------
+ * No reference counterpart (the learned preconditioner is new).  A ks x ks
+ * convolution (ks 1 or 3, padding ks/2, stride 1 or 2) with weights
+ * W[co][(ky*ks+kx)*Cin + ci] runs as GEMMs on unfolded operands:
+ *  unfold       out[pd][(ky*ks+kx)*C + c] = src[pixel, c], rows over the
+ *               destination grid B x Hd x Wd, columns zero-padded to Kpad;
+ *               transposed = 0: source pixel (hd*s+ky-pad, wd*s+kx-pad)
+ *               (forward operand); transposed = 1: the source pixel whose
+ *               window tap (ky,kx) lands on (hd, wd) (data-gradient operand);
+ *  unfold_t     colT[(tap*C + c)][p] over the output pixels p of the
+ *               convolution of x (weight-gradient operand);
+ *  transpose    out[c][r] = in[r][c] (kind 0 bf16, 1 float32);
+ *  weights      bf16 W (Cout x Kpad) and, if Wt != NULL, Wt (Cin x Kg) with
+ *               Wt[ci][tap*Cout + co] = W[co][tap*Cin + ci], from float32 W;
+ *  relu_grad    g = dy * (y > 0) (relu) or dy, as bf16;
+ *  rowsum       out[r] = sum_c in[r][c] (bf16 in, bias gradients);
+ *  upsample     nearest x2 of x into channels [coff, coff+C) of y (Ctot
+ *               channels), or (grad) its adjoint from float32 dy;
+ *  channels     put (bf16 x into channels of y) or take (float32 channels of
+ *               x into y, accumulate optional);
+ *  to_bf16      y = x * scale[image] (scale may be NULL);
+ *  image_rms    scale[b] = 1/rms of image b (B images of n floats; 0 if zero);
+ *  mse          loss = mean (y - t)^2 (double, device), grad = 2 (y - t)/n
+ *               (may be NULL), partials: 304 doubles of scratch;
+ *  adam         Adam step `step` (1-based) on float32 weights. */
+int kgb_unet_unfold(const void* src, void* out, int B, int Hs, int Ws, int C, int Hd, int Wd, int ks, int stride,
+                    int transposed, int Kpad, void* stream);
+int kgb_unet_unfold_t(const void* x, void* colT, int B, int H, int W, int C, int ks, int stride, void* stream);
+int kgb_unet_transpose(const void* in, void* out, int64_t rows, int cols, int64_t ldi, int64_t ldo, int kind,
+                       void* stream);
+int kgb_unet_weights(const float* W, void* Wb, void* Wt, int Cout, int Cin, int ks, int Kpad, int Kg, void* stream);
+int kgb_unet_relu_grad(const float* dy, const void* y, void* g, int64_t n, int relu, void* stream);
+int kgb_unet_rowsum(const void* in, float* out, int rows, int64_t cols, void* stream);
+int kgb_unet_upsample(const void* x, void* y, int B, int H, int W, int C, int Ctot, int coff, int grad,
+                      void* stream);
+int kgb_unet_channels(const void* x, void* y, int64_t P, int C, int Ctot, int coff, int take, int accumulate,
+                      void* stream);
+int kgb_unet_to_bf16(const float* x, void* y, int64_t n, int B, const float* scale, void* stream);
+int kgb_unet_image_rms(const float* x, int64_t n, int B, float* scale, void* stream);
+int kgb_unet_mse(const float* y, const float* t, float* grad, int64_t n, double* partials, double* loss,
+                 void* stream);
+int kgb_unet_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,
+                  int step, void* stream);
 
 /* ---- table builder ------------------------------------------------------
  * First-arrival traveltimes (and, if dist_out != NULL, distances) from npts

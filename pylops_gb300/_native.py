@@ -33,6 +33,7 @@ _lock = threading.Lock()
 
 c_int = ctypes.c_int
 c_i64 = ctypes.c_int64
+c_float = ctypes.c_float
 c_dbl = ctypes.c_double
 c_vp = ctypes.c_void_p
 c_dp = ctypes.POINTER(ctypes.c_double)
@@ -59,6 +60,8 @@ _SIGNATURES = {
     "kgb_dot_f64": ([c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
     "kgb_solver_create": ([ctypes.POINTER(c_vp), c_vp, c_int], c_int),
     "kgb_solver_destroy": ([c_vp], c_int),
+    "kgb_lincomb_f32": ([c_vp, c_vp, c_dbl, c_vp, c_vp, c_int, c_i64, c_vp], c_int),
+    "kgb_solver_set_diagonal": ([c_vp, c_vp], c_int),
     "kgb_solver_setup": ([c_vp, c_vp, c_vp, c_dp, c_int, c_vp], c_int),
     "kgb_solver_run": ([c_vp, c_int, c_int, c_vp], c_int),
     "kgb_solver_result": ([c_vp, c_vp, c_dp, c_dp, c_int, c_vp], c_int),
@@ -70,6 +73,20 @@ _SIGNATURES = {
     "kgb_batch_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_batch_cgls": ([c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_int, c_dp, c_ip, c_dp, c_vp], c_int),
     "kgb_gemm_bf16_tn": ([c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_vp, c_int, c_vp, c_vp], c_int),
+    "kgb_gemm_bf16_tn_splitk": ([c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_vp, c_i64,
+                                 c_vp, c_vp], c_int),
+    "kgb_unet_unfold": ([c_vp, c_vp] + [c_int] * 10 + [c_vp], c_int),
+    "kgb_unet_unfold_t": ([c_vp, c_vp] + [c_int] * 6 + [c_vp], c_int),
+    "kgb_unet_transpose": ([c_vp, c_vp, c_i64, c_int, c_i64, c_i64, c_int, c_vp], c_int),
+    "kgb_unet_weights": ([c_vp, c_vp, c_vp] + [c_int] * 5 + [c_vp], c_int),
+    "kgb_unet_relu_grad": ([c_vp, c_vp, c_vp, c_i64, c_int, c_vp], c_int),
+    "kgb_unet_rowsum": ([c_vp, c_vp, c_int, c_i64, c_vp], c_int),
+    "kgb_unet_upsample": ([c_vp, c_vp] + [c_int] * 7 + [c_vp], c_int),
+    "kgb_unet_channels": ([c_vp, c_vp, c_i64, c_int, c_int, c_int, c_int, c_int, c_vp], c_int),
+    "kgb_unet_to_bf16": ([c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    "kgb_unet_image_rms": ([c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    "kgb_unet_mse": ([c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
+    "kgb_unet_adam": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_float, c_float, c_float, c_float, c_int, c_vp], c_int),
     "kgb_eikonal_tables": ([c_int, c_ip, c_dp, c_dp, c_int, c_ip, c_dp, c_dp, c_int, c_int], c_int),
 }
 

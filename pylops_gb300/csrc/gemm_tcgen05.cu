@@ -83,6 +83,11 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
     return d;
 }
 
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
 // Instruction descriptor, kind::f16: D f32 (bits [4,6) = 1), A and B bf16
 // (bits [7,10) and [10,13) = 1), both K-major, N >> 3 in [17,23), M >> 4 in
 // [24,29).
@@ -93,7 +98,8 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
 template <int BN>
 __global__ void __launch_bounds__(128, 1)
 gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, void* __restrict__ C,
-               int M, int N, int K, int ldc, const float* __restrict__ bias, int flags, int* __restrict__ err) {
+               int M, int N, int K, int ldc, const float* __restrict__ bias, int flags, int* __restrict__ err,
+               int kt_per, int64_t split_stride) {
     constexpr int A_BYTES = BM * BK * 2;
     constexpr int B_BYTES = BN * BK * 2;
     extern __shared__ uint8_t smem_dyn[];
@@ -113,7 +119,11 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-    const int ktiles = (K + BK - 1) / BK;
+    // split-K: this CTA reduces k-tiles [kt0, kt0 + ktiles) into its own
+    // slice of C (the host makes every slice non-empty)
+    const int kt0 = blockIdx.z * kt_per;
+    const int ktiles = min((K + BK - 1) / BK - kt0, kt_per);
+    if (blockIdx.z) C = reinterpret_cast<float*>(C) + blockIdx.z * split_stride;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -143,8 +153,8 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 break;
             }
             mbar_expect_tx(bar_full + 8 * s, A_BYTES + B_BYTES);
-            tma_load_2d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, kt * BK, m0);
-            tma_load_2d(sB + s * B_BYTES, &tmB, bar_full + 8 * s, kt * BK, n0);
+            tma_load_2d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, (kt0 + kt) * BK, m0);
+            tma_load_2d(sB + s * B_BYTES, &tmB, bar_full + 8 * s, (kt0 + kt) * BK, n0);
         }
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
@@ -194,7 +204,32 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
               "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (good && row < M) {
+        if (good && row < M && (flags & 4) && n0 + c0 + 32 <= N) {
+            // whole 32-column chunk, 16-byte aligned row segment
+            float v[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                v[j] = __uint_as_float(r[j]);
+                if (bias) v[j] += __ldg(bias + n0 + c0 + j);
+                if (flags & 1) v[j] = fmaxf(v[j], 0.f);
+            }
+            if (flags & 2) {
+                uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(C) + (size_t)row * ldc + n0 + c0);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint4 u;
+                    u.x = pack_bf16(v[8 * q + 0], v[8 * q + 1]);
+                    u.y = pack_bf16(v[8 * q + 2], v[8 * q + 3]);
+                    u.z = pack_bf16(v[8 * q + 4], v[8 * q + 5]);
+                    u.w = pack_bf16(v[8 * q + 6], v[8 * q + 7]);
+                    dst[q] = u;
+                }
+            } else {
+                float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(C) + (size_t)row * ldc + n0 + c0);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            }
+        } else if (good && row < M) {
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 const int col = n0 + c0 + j;
@@ -254,17 +289,56 @@ size_t gemm_smem() {
 
 template <int BN>
 int gemm_launch(const CUtensorMap& ma, const CUtensorMap& mb, void* C, int M, int N, int K, int ldc, const float* bias,
-                int flags, int* err, cudaStream_t s) {
+                int flags, int* err, int splits, int kt_per, int64_t split_stride, cudaStream_t s) {
     static bool attr = false;
     const size_t smem = gemm_smem<BN>();
     if (!attr) {
         KGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tn_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)((N + BN - 1) / BN));
-    gemm_tn_kernel<BN><<<grid, 128, smem, s>>>(ma, mb, C, M, N, K, ldc, bias, flags, err);
+    dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)((N + BN - 1) / BN), (unsigned)splits);
+    gemm_tn_kernel<BN><<<grid, 128, smem, s>>>(ma, mb, C, M, N, K, ldc, bias, flags, err, kt_per, split_stride);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
+}
+
+// C[m][n] = sum over z of work[z][m][n], in order z = 0, 1, ...
+__global__ void splitk_sum_kernel(const float* __restrict__ work, float* __restrict__ C, int M, int N, int ldc,
+                                  int splits) {
+    const int64_t total = (int64_t)M * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        for (int z = 0; z < splits; ++z) acc += work[z * total + i];
+        C[(i / N) * ldc + (i % N)] = acc;
+    }
+}
+
+int check_args(const void* A, const void* B, const void* C, int M, int N, int K, int lda, int ldb, int ldc) {
+    if (!A || !B || !C) return set_error(KGB_ERR_VALUE, "gemm: null pointer");
+    if (M <= 0 || N <= 0 || K <= 0) return set_error(KGB_ERR_VALUE, "gemm: sizes must be positive");
+    if (K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K)
+        return set_error(KGB_ERR_VALUE, "gemm: K and the leading dimensions must be multiples of 8 (16-byte rows)");
+    if (((uintptr_t)A | (uintptr_t)B) & 15) return set_error(KGB_ERR_VALUE, "gemm: A and B must be 16-byte aligned");
+    if (ldc < N) return set_error(KGB_ERR_VALUE, "gemm: ldc < N");
+    return KGB_OK;
+}
+
+// 16-byte vector stores in the epilogue when every row segment is aligned
+int vector_flag(const void* C, int ldc, int flags) {
+    const int elems = (flags & 2) ? 8 : 4;
+    return (((uintptr_t)C & 15) == 0 && ldc % elems == 0) ? 4 : 0;
+}
+
+int run_gemm(const void* A, const void* B, void* C, int M, int N, int K, int lda, int ldb, int ldc, const float* bias,
+             int flags, int* err, int splits, int kt_per, int64_t split_stride, cudaStream_t s) {
+    const int BN = N <= 64 ? 64 : 128;
+    CUtensorMap ma, mb;
+    int rc;
+    if ((rc = make_map(&ma, A, M, K, lda, BM))) return rc;
+    if ((rc = make_map(&mb, B, N, K, ldb, BN))) return rc;
+    flags = (flags & 3) | vector_flag(C, ldc, flags);
+    if (BN == 64) return gemm_launch<64>(ma, mb, C, M, N, K, ldc, bias, flags, err, splits, kt_per, split_stride, s);
+    return gemm_launch<128>(ma, mb, C, M, N, K, ldc, bias, flags, err, splits, kt_per, split_stride, s);
 }
 
 }  // namespace
@@ -274,18 +348,33 @@ using namespace kgb;
 
 extern "C" int kgb_gemm_bf16_tn(const void* A, const void* B, void* C, int M, int N, int K, int lda, int ldb, int ldc,
                                 const float* bias, int flags, int* err_dev, void* stream) {
-    if (!A || !B || !C) return set_error(KGB_ERR_VALUE, "gemm: null pointer");
-    if (M <= 0 || N <= 0 || K <= 0) return set_error(KGB_ERR_VALUE, "gemm: sizes must be positive");
-    if (K % 8 || lda % 8 || ldb % 8 || lda < K || ldb < K)
-        return set_error(KGB_ERR_VALUE, "gemm: K and the leading dimensions must be multiples of 8 (16-byte rows)");
-    if (((uintptr_t)A | (uintptr_t)B) & 15) return set_error(KGB_ERR_VALUE, "gemm: A and B must be 16-byte aligned");
-    if (ldc < N) return set_error(KGB_ERR_VALUE, "gemm: ldc < N");
+    int rc = check_args(A, B, C, M, N, K, lda, ldb, ldc);
+    if (rc) return rc;
+    const int ktiles = (K + BK - 1) / BK;
+    return run_gemm(A, B, C, M, N, K, lda, ldb, ldc, bias, flags, err_dev, 1, ktiles, 0, (cudaStream_t)stream);
+}
+
+extern "C" int kgb_gemm_bf16_tn_splitk(const void* A, const void* B, float* C, int M, int N, int K, int lda, int ldb,
+                                       int ldc, int splits, float* work, int64_t work_elems, int* err_dev,
+                                       void* stream) {
+    int rc = check_args(A, B, C, M, N, K, lda, ldb, ldc);
+    if (rc) return rc;
+    const int ktiles = (K + BK - 1) / BK;
     const int BN = N <= 64 ? 64 : 128;
-    CUtensorMap ma, mb;
-    int rc;
-    if ((rc = make_map(&ma, A, M, K, lda, BM))) return rc;
-    if ((rc = make_map(&mb, B, N, K, ldb, BN))) return rc;
+    const int64_t tiles = (int64_t)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    if (splits <= 0) splits = (int)std::max<int64_t>(1, (2 * 152 + tiles - 1) / tiles);
+    const int64_t mn = (int64_t)M * N;
+    if (work && ((uintptr_t)work & 15) == 0) splits = (int)std::min<int64_t>(splits, work_elems / mn);
+    else splits = 1;
+    splits = std::max(1, std::min(splits, ktiles));
+    // every split gets at least one k-tile
+    const int kt_per = (ktiles + splits - 1) / splits;
+    splits = (ktiles + kt_per - 1) / kt_per;
     cudaStream_t s = (cudaStream_t)stream;
-    if (BN == 64) return gemm_launch<64>(ma, mb, C, M, N, K, ldc, bias, flags, err_dev, s);
-    return gemm_launch<128>(ma, mb, C, M, N, K, ldc, bias, flags, err_dev, s);
+    if (splits == 1) return run_gemm(A, B, C, M, N, K, lda, ldb, ldc, nullptr, 0, err_dev, 1, ktiles, 0, s);
+    if ((rc = run_gemm(A, B, work, M, N, K, lda, ldb, N, nullptr, 0, err_dev, splits, kt_per, mn, s))) return rc;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4 * 152));
+    splitk_sum_kernel<<<grid, 256, 0, s>>>(work, C, M, N, ldc, splits);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
 }

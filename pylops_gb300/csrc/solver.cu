@@ -379,6 +379,9 @@ struct kgb_solver {
     cudaGraphExec_t exec = nullptr;
     cudaGraphConditionalHandle handle = 0;
     bool setup_done = false;
+    // optional right preconditioner: the solver then works on K diag(pdiag)
+    const float* pdiag = nullptr;
+    float* mvp = nullptr;  // model-space scratch for pdiag * v
 };
 
 namespace kgb {
@@ -407,19 +410,40 @@ int ensure_cost(kgb_solver* s, int need) {
     return KGB_OK;
 }
 
+__global__ void diag_mul_kernel(float* __restrict__ out, const float* __restrict__ p, const float* __restrict__ v,
+                                int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = p[i] * v[i];
+}
+
+// The operator the solver inverts: K, or K diag(p) with a right preconditioner.
+int op_forward(kgb_solver* s, const float* v, float* out, cudaStream_t stream) {
+    if (!s->pdiag) return kgb_kirchhoff_forward(s->op, v, out, stream);
+    diag_mul_kernel<<<grid_for(s->n), kRedThreads, 0, stream>>>(s->mvp, s->pdiag, v, s->n);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return kgb_kirchhoff_forward(s->op, s->mvp, out, stream);
+}
+
+int op_adjoint(kgb_solver* s, const float* u, float* out, cudaStream_t stream) {
+    int rc = kgb_kirchhoff_adjoint(s->op, u, out, stream);
+    if (rc || !s->pdiag) return rc;
+    diag_mul_kernel<<<grid_for(s->n), kRedThreads, 0, stream>>>(out, s->pdiag, out, s->n);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
 // One LSQR iteration's launches on `stream` (captured or direct).
 int enqueue_iteration(kgb_solver* s, cudaStream_t stream, int use_handle) {
-    kgb_kirchhoff* op = s->op;
     const int gn = grid_for(s->n), gm = grid_for(s->m);
     double* P0 = s->partials;
     double* P1 = s->partials + kRedBlocks;
     int rc;
     {  // LSQR: x, v=mv1, w=mv2, vb=mv3; u=dv1, ub=dv2
-        if ((rc = kgb_kirchhoff_forward(op, s->mv1, s->dv2, stream))) return rc;
+        if ((rc = op_forward(s, s->mv1, s->dv2, stream))) return rc;
         lsqr_u_kernel<<<gm, kRedThreads, 0, stream>>>(s->dv1, s->dv2, s->m, s->st, P0);
         lsqr_beta_kernel<<<1, kRedThreads, 0, stream>>>(s->st, P0, gm);
         scale_kernel<<<gm, kRedThreads, 0, stream>>>(s->dv1, s->m, s->st, 0);
-        if ((rc = kgb_kirchhoff_adjoint(op, s->dv1, s->mv3, stream))) return rc;
+        if ((rc = op_adjoint(s, s->dv1, s->mv3, stream))) return rc;
         lsqr_v_kernel<<<gn, kRedThreads, 0, stream>>>(s->mv1, s->mv3, s->n, s->st, P0);
         lsqr_rot_kernel<<<1, kRedThreads, 0, stream>>>(s->st, P0, gn);
         lsqr_xw_kernel<<<gn, kRedThreads, 0, stream>>>(s->x, s->mv2, s->mv1, s->n, s->st, P1);
@@ -456,7 +480,6 @@ cgls_b2_kernel(SolverState* st, const double* __restrict__ pr, int npr, const do
 }
 
 int enqueue_cgls_iteration(kgb_solver* s, cudaStream_t stream, int use_handle) {
-    kgb_kirchhoff* op = s->op;
     const int gn = grid_for(s->n), gm = grid_for(s->m);
     double* P0 = s->partials;
     double* P1 = s->partials + kRedBlocks;
@@ -469,11 +492,11 @@ int enqueue_cgls_iteration(kgb_solver* s, cudaStream_t stream, int use_handle) {
     cgls_a2_kernel<<<1, kRedThreads, 0, stream>>>(s->st, P0, gm, P1, gn);
     cgls_x_kernel<<<gn, kRedThreads, 0, stream>>>(s->x, s->mv1, s->n, s->st, P2);
     cgls_s_kernel<<<gm, kRedThreads, 0, stream>>>(s->dv1, s->dv2, s->m, s->st, P3);
-    if ((rc = kgb_kirchhoff_adjoint(op, s->dv1, s->mv2, stream))) return rc;
+    if ((rc = op_adjoint(s, s->dv1, s->mv2, stream))) return rc;
     cgls_r_kernel<<<gn, kRedThreads, 0, stream>>>(s->mv2, s->x, s->n, s->st, P0);
     cgls_b2_kernel<<<1, kRedThreads, 0, stream>>>(s->st, P0, gn, P3, gm, P2, gn, s->cost, s->cost1);
     cgls_c_kernel<<<gn, kRedThreads, 0, stream>>>(s->mv1, s->mv2, s->n, s->st);
-    if ((rc = kgb_kirchhoff_forward(op, s->mv1, s->dv2, stream))) return rc;
+    if ((rc = op_forward(s, s->mv1, s->dv2, stream))) return rc;
     cgls_tail_kernel<<<1, 1, 0, stream>>>(s->st, s->handle, use_handle);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
@@ -640,7 +663,44 @@ sq_partial_plain_kernel(const float* __restrict__ a, int64_t n, double* __restri
 
 using namespace kgb::sk;
 
+namespace kgb {
+namespace sk {
+
+constexpr int kMaxComb = 16;
+struct CombArgs {
+    const float* v[kMaxComb];
+    float c[kMaxComb];
+};
+
+// out = c0 * base + sum_j c[j] v[j] (base may be NULL), summed in index order
+__global__ void lincomb_kernel(float* __restrict__ out, const float* __restrict__ base, float c0, CombArgs a, int k,
+                               int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float acc = base ? c0 * base[i] : 0.f;
+        for (int j = 0; j < k; ++j) acc = fmaf(a.c[j], a.v[j][i], acc);
+        out[i] = acc;
+    }
+}
+
+}  // namespace sk
+}  // namespace kgb
+
 extern "C" {
+
+int kgb_lincomb_f32(float* out, const float* base, double base_coef, const float* const* vecs, const double* coefs,
+                    int k, int64_t n, void* stream) {
+    if (!out || k < 0 || k > sk::kMaxComb || n <= 0 || (k > 0 && (!vecs || !coefs)))
+        return set_error(KGB_ERR_VALUE, "lincomb: bad arguments (k <= 16)");
+    sk::CombArgs a;
+    for (int j = 0; j < sk::kMaxComb; ++j) {
+        a.v[j] = j < k ? vecs[j] : nullptr;
+        a.c[j] = j < k ? (float)coefs[j] : 0.f;
+        if (j < k && !vecs[j]) return set_error(KGB_ERR_VALUE, "lincomb: null vector");
+    }
+    sk::lincomb_kernel<<<grid_for(n), kRedThreads, 0, (cudaStream_t)stream>>>(out, base, (float)base_coef, a, k, n);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
 
 int kgb_dot_f64(const float* a, const float* b, int64_t n, double* out, void* stream) {
     if (!a || !b || !out) return set_error(KGB_ERR_VALUE, "dot: null pointer");
@@ -685,9 +745,22 @@ int kgb_solver_destroy(kgb_solver* s) {
     if (!s) return KGB_OK;
     if (s->exec) cudaGraphExecDestroy(s->exec);
     if (s->graph) cudaGraphDestroy(s->graph);
-    void* ptrs[] = {s->x, s->mv1, s->mv2, s->mv3, s->dv1, s->dv2, s->st, s->partials, s->cost, s->cost1};
+    void* ptrs[] = {s->x, s->mv1, s->mv2, s->mv3, s->dv1, s->dv2, s->st, s->partials, s->cost, s->cost1, s->mvp};
     for (void* p : ptrs) if (p) cudaFree(p);
     delete s;
+    return KGB_OK;
+}
+
+int kgb_solver_set_diagonal(kgb_solver* s, const float* p) {
+    if (!s) return set_error(KGB_ERR_VALUE, "solver_set_diagonal: null solver");
+    if (p && !s->mvp) KGB_CUDA_TRY(cudaMalloc(&s->mvp, (size_t)s->n * sizeof(float)));
+    if (p != s->pdiag) {
+        // the captured iteration bakes the operator in
+        if (s->exec) { cudaGraphExecDestroy(s->exec); s->exec = nullptr; }
+        if (s->graph) { cudaGraphDestroy(s->graph); s->graph = nullptr; }
+    }
+    s->pdiag = p;
+    s->setup_done = false;
     return KGB_OK;
 }
 
@@ -700,7 +773,6 @@ int kgb_solver_setup(kgb_solver* s, const float* y, const float* x0, const doubl
     if (s->kind == 1) { p[1] = 1e-8; p[2] = 1e-8; p[3] = 1e8; } else { p[1] = 1e-4; }
     for (int i = 0; i < nparams && i < 4; ++i) p[i] = params[i];
     if (nparams >= 5) niter_setup = (int)params[4];
-    kgb_kirchhoff* op = s->op;
     const int gn = grid_for(s->n), gm = grid_for(s->m);
     double* P0 = s->partials;
     double* P1 = s->partials + kRedBlocks;
@@ -711,7 +783,7 @@ int kgb_solver_setup(kgb_solver* s, const float* y, const float* x0, const doubl
         // x = x0 or 0; u = y - K x0 or y (cls_basic.py:944-956)
         if (x0) {
             KGB_CUDA_TRY(cudaMemcpyAsync(s->x, x0, s->n * 4, cudaMemcpyDeviceToDevice, stream));
-            if ((rc = kgb_kirchhoff_forward(op, x0, s->dv2, stream))) return rc;
+            if ((rc = op_forward(s, x0, s->dv2, stream))) return rc;
             sub_kernel<<<gm, kRedThreads, 0, stream>>>(s->dv1, y, s->dv2, s->m);
         } else {
             KGB_CUDA_TRY(cudaMemsetAsync(s->x, 0, s->n * 4, stream));
@@ -722,7 +794,7 @@ int kgb_solver_setup(kgb_solver* s, const float* y, const float* x0, const doubl
         scale_by_kernel<<<gm, kRedThreads, 0, stream>>>(s->dv1, s->m, s->st, 0);
         // v = K^H u when beta > 0, else v = x (cls_basic.py:957-969); computing
         // the adjoint unconditionally is harmless because it is discarded.
-        if ((rc = kgb_kirchhoff_adjoint(op, s->dv1, s->mv1, stream))) return rc;
+        if ((rc = op_adjoint(s, s->dv1, s->mv1, stream))) return rc;
         sq_partial_plain_kernel<<<gn, kRedThreads, 0, stream>>>(s->mv1, s->n, P1);
         lsqr_setup_alfa_kernel<<<1, kRedThreads, 0, stream>>>(s->st, P1, gn, s->cost);
         scale_by_kernel<<<gn, kRedThreads, 0, stream>>>(s->mv1, s->n, s->st, 1);
@@ -732,16 +804,16 @@ int kgb_solver_setup(kgb_solver* s, const float* y, const float* x0, const doubl
         // CGLS setup (cls_basic.py:474-503)
         if (x0) {
             KGB_CUDA_TRY(cudaMemcpyAsync(s->x, x0, s->n * 4, cudaMemcpyDeviceToDevice, stream));
-            if ((rc = kgb_kirchhoff_forward(op, x0, s->dv2, stream))) return rc;
+            if ((rc = op_forward(s, x0, s->dv2, stream))) return rc;
             sub_kernel<<<gm, kRedThreads, 0, stream>>>(s->dv1, y, s->dv2, s->m);
-            if ((rc = kgb_kirchhoff_adjoint(op, s->dv1, s->mv1, stream))) return rc;
+            if ((rc = op_adjoint(s, s->dv1, s->mv1, stream))) return rc;
             axpy_kernel<<<gn, kRedThreads, 0, stream>>>(s->mv1, s->x, (float)(-p[0]), s->n);  // unsquared damp
         } else {
             KGB_CUDA_TRY(cudaMemsetAsync(s->x, 0, s->n * 4, stream));
             KGB_CUDA_TRY(cudaMemcpyAsync(s->dv1, y, s->m * 4, cudaMemcpyDeviceToDevice, stream));
-            if ((rc = kgb_kirchhoff_adjoint(op, s->dv1, s->mv1, stream))) return rc;
+            if ((rc = op_adjoint(s, s->dv1, s->mv1, stream))) return rc;
         }
-        if ((rc = kgb_kirchhoff_forward(op, s->mv1, s->dv2, stream))) return rc;  // q = K c
+        if ((rc = op_forward(s, s->mv1, s->dv2, stream))) return rc;  // q = K c
         sq_partial_plain_kernel<<<gn, kRedThreads, 0, stream>>>(s->mv1, s->n, P0);
         sq_partial_plain_kernel<<<gm, kRedThreads, 0, stream>>>(s->dv1, s->m, P1);
         sq_partial_plain_kernel<<<gn, kRedThreads, 0, stream>>>(s->x, s->n, P2);

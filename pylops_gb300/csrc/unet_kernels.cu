@@ -1,0 +1,441 @@
+// Memory-bound kernels of the U-Net image preconditioner; its convolutions
+// run on the tcgen05 GEMM (gemm_tcgen05.cu).  Activations are NHWC (channel
+// fastest).  A ks x ks convolution (ks = 1 or 3, zero padding ks/2, stride s)
+//   y[b,ho,wo,co] = sum_{ky,kx,ci} W[co][(ky*ks+kx)*Cin+ci] x[b, ho*s+ky-pad, wo*s+kx-pad, ci]
+// is lowered to three GEMMs:
+//   forward          y    = col  . W^T      col  = unfold(x)        (P_out x Kpad)
+//   weight gradient  dW   = g^T  . colT^T   colT = unfold(x)^T      (ks^2 Cin x P_out)
+//   data gradient    dx   = gcol . Wt^T     gcol = unfold^T(g)      (P_in x Kg)
+// where g = dy (.) relu'(y) and Wt[ci][(tap)*Cout+co] = W[co][tap*Cin+ci];
+// unfold^T gathers, for every input pixel, the output-gradient pixels whose
+// window covers it, so the data gradient is a plain GEMM (no scatter) and
+// training is deterministic.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "kgb_internal.h"
+
+namespace kgb {
+namespace un {
+
+typedef __nv_bfloat16 bf16;
+
+int grid_for(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 16 * 152)); }
+
+// Source pixel of destination pixel (hd, wd) for tap (ky, kx).  Forward
+// unfold: hs = hd*s + ky - pad.  Transposed unfold: hd = hs*s + ky - pad.
+template <bool TRANS>
+__device__ __forceinline__ bool src_pixel(int hd, int wd, int ky, int kx, int s, int pad, int Hs, int Ws, int& hs,
+                                          int& ws) {
+    if (!TRANS) {
+        hs = hd * s + ky - pad;
+        ws = wd * s + kx - pad;
+    } else {
+        const int nh = hd + pad - ky, nw = wd + pad - kx;
+        if (nh < 0 || nw < 0) return false;
+        if (s == 2 && ((nh | nw) & 1)) return false;
+        hs = s == 2 ? nh >> 1 : nh;
+        ws = s == 2 ? nw >> 1 : nw;
+    }
+    return hs >= 0 && hs < Hs && ws >= 0 && ws < Ws;
+}
+
+// out[pd][(ky*ks+kx)*C + c] for pd over B x Hd x Wd, columns padded to Kpad.
+// VEC: C % 8 == 0 and 8 channels (16 bytes) per thread.
+template <bool TRANS, bool VEC>
+__global__ void unfold_kernel(const bf16* __restrict__ src, bf16* __restrict__ out, int B, int Hs, int Ws, int C,
+                              int Hd, int Wd, int ks, int s, int Kpad) {
+    const int pad = ks >> 1;
+    const int G = VEC ? 8 : 1;
+    const int kunits = Kpad / G;
+    const int64_t total = (int64_t)B * Hd * Wd * kunits;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(i % kunits) * G;
+        const int64_t p = i / kunits;
+        const int wd = (int)(p % Wd);
+        const int64_t t = p / Wd;
+        const int hd = (int)(t % Hd);
+        const int b = (int)(t / Hd);
+        const bf16* sp = nullptr;
+        if (k < ks * ks * C) {
+            const int tap = k / C, c = k - tap * C;
+            const int ky = tap / ks, kx = tap - ky * ks;
+            int hs, ws;
+            if (src_pixel<TRANS>(hd, wd, ky, kx, s, pad, Hs, Ws, hs, ws))
+                sp = src + (((int64_t)b * Hs + hs) * Ws + ws) * C + c;
+        }
+        if (VEC) {
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (sp) v = __ldg(reinterpret_cast<const uint4*>(sp));
+            reinterpret_cast<uint4*>(out)[i] = v;
+        } else {
+            out[i] = sp ? sp[0] : __float2bfloat16(0.f);
+        }
+    }
+}
+
+// colT[(tap*C + c)][p] = x[pixel(p, tap), c]: 32 pixels x 32 channels per
+// block through shared memory, coalesced on both sides.
+__global__ void unfold_t_kernel(const bf16* __restrict__ x, bf16* __restrict__ colT, int B, int H, int W, int C,
+                                int Ho, int Wo, int ks, int s, int64_t P) {
+    __shared__ bf16 tile[32][34];
+    const int pad = ks >> 1;
+    const int64_t p0 = (int64_t)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    const int tap = blockIdx.z;
+    const int ky = tap / ks, kx = tap - ky * ks;
+    const int tx = threadIdx.x;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t p = p0 + j;
+        const int c = c0 + tx;
+        bf16 v = __float2bfloat16(0.f);
+        if (p < P && c < C) {
+            const int wo = (int)(p % Wo);
+            const int64_t t = p / Wo;
+            const int ho = (int)(t % Ho);
+            const int b = (int)(t / Ho);
+            const int h = ho * s + ky - pad, w = wo * s + kx - pad;
+            if (h >= 0 && h < H && w >= 0 && w < W) v = x[(((int64_t)b * H + h) * W + w) * C + c];
+        }
+        tile[j][tx] = v;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int c = c0 + j;
+        const int64_t p = p0 + tx;
+        if (c < C && p < P) colT[((int64_t)tap * C + c) * P + p] = tile[tx][j];
+    }
+}
+
+// out[c][r] = in[r][c]; rows x cols, in leading dimension ldi, out ldo.
+template <typename TI, typename TO>
+__global__ void transpose_kernel(const TI* __restrict__ in, TO* __restrict__ out, int64_t rows, int cols, int64_t ldi,
+                                 int64_t ldo) {
+    __shared__ float tile[32][33];
+    const int64_t r0 = (int64_t)blockIdx.x * 32;
+    const int c0 = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int64_t r = r0 + j;
+        const int c = c0 + threadIdx.x;
+        tile[j][threadIdx.x] = (r < rows && c < cols) ? (float)in[r * ldi + c] : 0.f;
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+        const int c = c0 + j;
+        const int64_t r = r0 + threadIdx.x;
+        if (c < cols && r < rows) out[(int64_t)c * ldo + r] = (TO)tile[threadIdx.x][j];
+    }
+}
+
+// bf16 weights for the forward (W, Cout x Kpad) and data-gradient (Wt,
+// Cin x Kg) GEMMs from the float32 master weights.
+__global__ void weights_kernel(const float* __restrict__ Wm, bf16* __restrict__ Wb, bf16* __restrict__ Wt, int Cout,
+                               int Cin, int taps, int Kpad, int Kg) {
+    const int64_t nW = (int64_t)Cout * Kpad, nT = Wt ? (int64_t)Cin * Kg : 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nW + nT; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nW) {
+            Wb[i] = __float2bfloat16(Wm[i]);
+        } else {
+            const int64_t j = i - nW;
+            const int ci = (int)(j / Kg), q = (int)(j % Kg);
+            float v = 0.f;
+            if (q < taps * Cout) {
+                const int tap = q / Cout, co = q - tap * Cout;
+                v = Wm[(int64_t)co * Kpad + tap * Cin + ci];
+            }
+            Wt[j] = __float2bfloat16(v);
+        }
+    }
+}
+
+// g = dy (.) (y > 0)  (relu) or dy, rounded to bf16
+__global__ void relu_grad_kernel(const float* __restrict__ dy, const bf16* __restrict__ y, bf16* __restrict__ g,
+                                 int64_t n, int relu) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float v = dy[i];
+        if (relu && !(__bfloat162float(y[i]) > 0.f)) v = 0.f;
+        g[i] = __float2bfloat16(v);
+    }
+}
+
+// out[r] = sum_c in[r][c] (bias gradient from g^T), fixed reduction order
+__global__ void rowsum_kernel(const bf16* __restrict__ in, float* __restrict__ out, int64_t cols) {
+    const int r = blockIdx.x;
+    float acc = 0.f;
+    for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) acc += __bfloat162float(in[r * cols + c]);
+    __shared__ float sh[512];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[r] = sh[0];
+}
+
+// nearest x2 upsampling of x (B x H x W x C) into channels [coff, coff+C)
+// of y (B x 2H x 2W x Ctot)
+__global__ void upsample_kernel(const bf16* __restrict__ x, bf16* __restrict__ y, int B, int H, int W, int C, int Ctot,
+                                int coff) {
+    const int64_t total = (int64_t)B * 2 * H * 2 * W * C;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        int64_t t = i / C;
+        const int w = (int)(t % (2 * W));
+        t /= 2 * W;
+        const int h = (int)(t % (2 * H));
+        const int b = (int)(t / (2 * H));
+        y[(((int64_t)b * 2 * H + h) * 2 * W + w) * Ctot + coff + c] = x[(((int64_t)b * H + h / 2) * W + w / 2) * C + c];
+    }
+}
+
+// its gradient: dx[b,h,w,c] = sum of the 2x2 block of dy[..., coff + c]
+__global__ void upsample_grad_kernel(const float* __restrict__ dy, float* __restrict__ dx, int B, int H, int W, int C,
+                                     int Ctot, int coff) {
+    const int64_t total = (int64_t)B * H * W * C;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        int64_t t = i / C;
+        const int w = (int)(t % W);
+        t /= W;
+        const int h = (int)(t % H);
+        const int b = (int)(t / H);
+        const int64_t r0 = (((int64_t)b * 2 * H + 2 * h) * 2 * W + 2 * w) * Ctot + coff + c;
+        const int64_t rs = (int64_t)2 * W * Ctot;
+        dx[i] = (dy[r0] + dy[r0 + Ctot]) + (dy[r0 + rs] + dy[r0 + rs + Ctot]);
+    }
+}
+
+// y[p][coff + c] = x[p][c]  (skip connection into the concatenation)
+__global__ void put_channels_kernel(const bf16* __restrict__ x, bf16* __restrict__ y, int64_t P, int C, int Ctot,
+                                    int coff) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P * C; i += (int64_t)gridDim.x * blockDim.x)
+        y[(i / C) * Ctot + coff + (i % C)] = x[i];
+}
+
+// y[p][c] (+)= x[p][coff + c]  (gradient of the skip connection)
+__global__ void take_channels_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t P, int C, int Ctot,
+                                     int coff, int accumulate) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P * C; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = x[(i / C) * Ctot + coff + (i % C)];
+        y[i] = accumulate ? y[i] + v : v;
+    }
+}
+
+// x (float, B images of n values) * per-image scale -> bf16 (NHWC with C = 1)
+__global__ void to_bf16_kernel(const float* __restrict__ x, bf16* __restrict__ y, int64_t n, int B,
+                               const float* __restrict__ scale) {
+    const int64_t total = n * B;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16(x[i] * (scale ? scale[i / n] : 1.f));
+}
+
+// Mean-squared error: grad = 2 (y - t) / n, per-block partial sums of
+// (y - t)^2 in double, then one thread sums them in order.
+constexpr int kMseBlocks = 304;
+__global__ void mse_kernel(const float* __restrict__ y, const float* __restrict__ t, float* __restrict__ grad,
+                           int64_t n, double* __restrict__ partials) {
+    double acc = 0.0;
+    const float sc = 2.f / (float)n;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float d = y[i] - t[i];
+        acc += (double)d * d;
+        if (grad) grad[i] = sc * d;
+    }
+    __shared__ double sh[256];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+__global__ void mse_final_kernel(const double* __restrict__ partials, int np, int64_t n, double* __restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < np; ++i) s += partials[i];
+        out[0] = s / (double)n;
+    }
+}
+
+// scale[b] = 1 / sqrt(mean over image b of x^2) (0 for an all-zero image);
+// one block per image, fixed reduction order
+__global__ void image_rms_kernel(const float* __restrict__ x, int64_t n, float* __restrict__ scale) {
+    const float* xb = x + (int64_t)blockIdx.x * n;
+    double acc = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += (double)xb[i] * xb[i];
+    __shared__ double sh[512];
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) scale[blockIdx.x] = sh[0] > 0.0 ? (float)(1.0 / sqrt(sh[0] / (double)n)) : 0.f;
+}
+
+// Adam on float32 master weights (bias-corrected moments)
+__global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float c1,
+                            float c2) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+}  // namespace un
+}  // namespace kgb
+
+using namespace kgb;
+using namespace kgb::un;
+
+extern "C" {
+
+int kgb_unet_unfold(const void* src, void* out, int B, int Hs, int Ws, int C, int Hd, int Wd, int ks, int stride,
+                    int transposed, int Kpad, void* stream) {
+    if (!src || !out || B <= 0 || Hs <= 0 || Ws <= 0 || C <= 0 || Hd <= 0 || Wd <= 0 || (ks != 1 && ks != 3) ||
+        (stride != 1 && stride != 2) || Kpad < ks * ks * C || Kpad % 8)
+        return set_error(KGB_ERR_VALUE, "unet_unfold: bad arguments");
+    const bool vec = C % 8 == 0 && ((uintptr_t)src & 15) == 0 && ((uintptr_t)out & 15) == 0;
+    const int64_t n = (int64_t)B * Hd * Wd * (vec ? Kpad / 8 : Kpad);
+    cudaStream_t s = (cudaStream_t)stream;
+    const bf16* x = (const bf16*)src;
+    bf16* y = (bf16*)out;
+    if (transposed) {
+        if (vec) unfold_kernel<true, true><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
+        else unfold_kernel<true, false><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
+    } else {
+        if (vec) unfold_kernel<false, true><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
+        else unfold_kernel<false, false><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
+    }
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_unfold_t(const void* x, void* colT, int B, int H, int W, int C, int ks, int stride, void* stream) {
+    if (!x || !colT || B <= 0 || H <= 0 || W <= 0 || C <= 0 || (ks != 1 && ks != 3) || (stride != 1 && stride != 2))
+        return set_error(KGB_ERR_VALUE, "unet_unfold_t: bad arguments");
+    const int pad = ks >> 1;
+    const int Ho = (H + 2 * pad - ks) / stride + 1, Wo = (W + 2 * pad - ks) / stride + 1;
+    const int64_t P = (int64_t)B * Ho * Wo;
+    if ((P + 31) / 32 > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "unet_unfold_t: too many pixels");
+    dim3 grid((unsigned)((P + 31) / 32), (unsigned)((C + 31) / 32), (unsigned)(ks * ks)), block(32, 8);
+    unfold_t_kernel<<<grid, block, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, B, H, W, C, Ho, Wo, ks,
+                                                              stride, P);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+// kind: 0 bf16 -> bf16, 1 float -> float
+int kgb_unet_transpose(const void* in, void* out, int64_t rows, int cols, int64_t ldi, int64_t ldo, int kind,
+                       void* stream) {
+    if (!in || !out || rows <= 0 || cols <= 0 || ldi < cols || ldo < rows || (kind != 0 && kind != 1))
+        return set_error(KGB_ERR_VALUE, "unet_transpose: bad arguments");
+    if ((rows + 31) / 32 > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "unet_transpose: too many rows");
+    dim3 grid((unsigned)((rows + 31) / 32), (unsigned)((cols + 31) / 32)), block(32, 8);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (kind == 0)
+        transpose_kernel<bf16, bf16><<<grid, block, 0, s>>>((const bf16*)in, (bf16*)out, rows, cols, ldi, ldo);
+    else
+        transpose_kernel<float, float><<<grid, block, 0, s>>>((const float*)in, (float*)out, rows, cols, ldi, ldo);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_weights(const float* Wm, void* Wb, void* Wt, int Cout, int Cin, int ks, int Kpad, int Kg, void* stream) {
+    if (!Wm || !Wb || Cout <= 0 || Cin <= 0 || (ks != 1 && ks != 3) || Kpad < ks * ks * Cin ||
+        (Wt && Kg < ks * ks * Cout))
+        return set_error(KGB_ERR_VALUE, "unet_weights: bad arguments");
+    const int64_t n = (int64_t)Cout * Kpad + (Wt ? (int64_t)Cin * Kg : 0);
+    weights_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(Wm, (bf16*)Wb, (bf16*)Wt, Cout, Cin, ks * ks, Kpad,
+                                                                  Kg);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_relu_grad(const float* dy, const void* y, void* g, int64_t n, int relu, void* stream) {
+    if (!dy || !g || (relu && !y) || n <= 0) return set_error(KGB_ERR_VALUE, "unet_relu_grad: bad arguments");
+    relu_grad_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(dy, (const bf16*)y, (bf16*)g, n, relu);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_rowsum(const void* in, float* out, int rows, int64_t cols, void* stream) {
+    if (!in || !out || rows <= 0 || cols <= 0) return set_error(KGB_ERR_VALUE, "unet_rowsum: bad arguments");
+    rowsum_kernel<<<rows, 512, 0, (cudaStream_t)stream>>>((const bf16*)in, out, cols);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_upsample(const void* x, void* y, int B, int H, int W, int C, int Ctot, int coff, int grad, void* stream) {
+    if (!x || !y || B <= 0 || H <= 0 || W <= 0 || C <= 0 || coff < 0 || coff + C > Ctot)
+        return set_error(KGB_ERR_VALUE, "unet_upsample: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (grad) {
+        const int64_t n = (int64_t)B * H * W * C;
+        upsample_grad_kernel<<<grid_for(n), 256, 0, s>>>((const float*)x, (float*)y, B, H, W, C, Ctot, coff);
+    } else {
+        const int64_t n = (int64_t)B * 4 * H * W * C;
+        upsample_kernel<<<grid_for(n), 256, 0, s>>>((const bf16*)x, (bf16*)y, B, H, W, C, Ctot, coff);
+    }
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_channels(const void* x, void* y, int64_t P, int C, int Ctot, int coff, int take, int accumulate,
+                      void* stream) {
+    if (!x || !y || P <= 0 || C <= 0 || coff < 0 || coff + C > Ctot)
+        return set_error(KGB_ERR_VALUE, "unet_channels: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (take)
+        take_channels_kernel<<<grid_for(P * C), 256, 0, s>>>((const float*)x, (float*)y, P, C, Ctot, coff, accumulate);
+    else
+        put_channels_kernel<<<grid_for(P * C), 256, 0, s>>>((const bf16*)x, (bf16*)y, P, C, Ctot, coff);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_to_bf16(const float* x, void* y, int64_t n, int B, const float* scale, void* stream) {
+    if (!x || !y || n <= 0 || B <= 0) return set_error(KGB_ERR_VALUE, "unet_to_bf16: bad arguments");
+    to_bf16_kernel<<<grid_for(n * B), 256, 0, (cudaStream_t)stream>>>(x, (bf16*)y, n, B, scale);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_image_rms(const float* x, int64_t n, int B, float* scale, void* stream) {
+    if (!x || !scale || n <= 0 || B <= 0) return set_error(KGB_ERR_VALUE, "unet_image_rms: bad arguments");
+    image_rms_kernel<<<B, 512, 0, (cudaStream_t)stream>>>(x, n, scale);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_mse(const float* y, const float* t, float* grad, int64_t n, double* partials, double* loss,
+                 void* stream) {
+    if (!y || !t || !partials || !loss || n <= 0) return set_error(KGB_ERR_VALUE, "unet_mse: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    mse_kernel<<<kMseBlocks, 256, 0, s>>>(y, t, grad, n, partials);
+    mse_final_kernel<<<1, 32, 0, s>>>(partials, kMseBlocks, n, loss);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,
+                  int step, void* stream) {
+    if (!w || !g || !m || !v || n <= 0 || step < 1) return set_error(KGB_ERR_VALUE, "unet_adam: bad arguments");
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    adam_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+}  // extern "C"

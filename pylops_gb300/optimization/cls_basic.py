@@ -31,10 +31,28 @@ __all__ = ["CGLS", "LSQR"]
 # ----------------------------------------------------------------------------
 # helpers
 # ----------------------------------------------------------------------------
-def _is_device_kirchhoff(Op) -> bool:
+def _device_parts(Op):
+    """(Kirchhoff, right diagonal or None) when the solve can run on the
+    device path: a Kirchhoff operator, or ``Kop * Diagonal(p)`` with a real
+    diagonal (a right preconditioner); None otherwise."""
+    from ..basicoperators.diagonal import Diagonal
+    from ..linearoperator import _ProductLinearOperator
     from ..waveeqprocessing.kirchhoff import Kirchhoff
 
-    return isinstance(Op, Kirchhoff)
+    if isinstance(Op, Kirchhoff):
+        return Op, None
+    if isinstance(Op, _ProductLinearOperator):
+        A, B = Op.args
+        if isinstance(A, Kirchhoff) and isinstance(B, Diagonal) and not B.complex:
+            d = B.diag.detach().cpu().numpy() if is_torch(B.diag) else np.asarray(B.diag)
+            if B._bshape is not None:
+                d = np.broadcast_to(d.reshape(B._bshape), B.dims)
+            return A, np.ascontiguousarray(d, dtype=np.float32).reshape(-1)
+    return None
+
+
+def _is_device_kirchhoff(Op) -> bool:
+    return _device_parts(Op) is not None
 
 
 def _dot(a, b) -> float:
@@ -78,9 +96,14 @@ class _DeviceSolver:
         self.Op = Op
         self.kind = kind
         self.stream = torch.cuda.Stream()
+        kop, diag = _device_parts(Op)
         h = ctypes.c_void_p()
-        _native.check(_native.lib().kgb_solver_create(ctypes.byref(h), Op.native_handle, kind))
+        _native.check(_native.lib().kgb_solver_create(ctypes.byref(h), kop.native_handle, kind))
         self.h = h
+        self.diag = None
+        if diag is not None:
+            self.diag = torch.as_tensor(diag, device="cuda")
+            _native.check(_native.lib().kgb_solver_set_diagonal(h, self.diag.data_ptr()))
         self.out = np.zeros(16)
 
     def __del__(self):

@@ -302,6 +302,32 @@ class Kirchhoff(LinearOperator):
         (one trace per warp), 2 warp-binned (two traces per warp)."""
         _native.check(_native.lib().kgb_kirchhoff_set_variant(self._h, int(variant)))
 
+    def autotune(self, variants=(0, 1, 2), reps: int = 3) -> dict:
+        """Time the forward for each spread variant on this operator's
+        tables (random model, CUDA events on the current stream), keep the
+        fastest and return {variant: ms}.  All variants give the same result
+        to float32 rounding; which is fastest depends on the geometry (how
+        many image points each trace collects and how they bin in time)."""
+        import torch
+
+        self._sync_tables()
+        m = torch.randn(self.ni, device="cuda", generator=torch.Generator(device="cuda").manual_seed(0))
+        d = torch.empty(self.shape[0], device="cuda")
+        times = {}
+        for v in variants:
+            self.set_spread_variant(v)
+            self.apply_into(m, d)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                self.apply_into(m, d)
+            e1.record()
+            e1.synchronize()
+            times[v] = e0.elapsed_time(e1) / reps
+        best = min(times, key=times.get)
+        self.set_spread_variant(best)
+        return times
+
     @property
     def frac_bits(self) -> int:
         return self.info()["frac_bits"]
@@ -339,6 +365,22 @@ class Kirchhoff(LinearOperator):
             _native.check(fn(self._h, xd.data_ptr(), yd.data_ptr(), torch.cuda.current_stream().cuda_stream))
             y = yd.cpu().numpy()
         return y.astype(self.dtype, copy=False)
+
+    def apply_into(self, x, out, adjoint: bool = False) -> None:
+        """Forward (or adjoint) of a contiguous float32 CUDA tensor into the
+        preallocated float32 CUDA tensor ``out``, on torch's current stream,
+        without allocating."""
+        import torch
+
+        if not (is_torch(x) and is_torch(out)) or x.dtype != torch.float32 or out.dtype != torch.float32 \
+                or not (x.is_cuda and out.is_cuda and x.is_contiguous() and out.is_contiguous()):
+            raise TypeError("apply_into takes contiguous float32 CUDA tensors")
+        n_in, n_out = (self.shape[0], self.shape[1]) if adjoint else (self.shape[1], self.shape[0])
+        if x.numel() != n_in or out.numel() != n_out:
+            raise ValueError(f"apply_into: sizes {x.numel()} -> {out.numel()}, expected {n_in} -> {n_out}")
+        self._sync_tables()
+        fn = _native.lib().kgb_kirchhoff_adjoint if adjoint else _native.lib().kgb_kirchhoff_forward
+        _native.check(fn(self._h, x.data_ptr(), out.data_ptr(), torch.cuda.current_stream().cuda_stream))
 
     def _matvec(self, x):
         """Forward (``kirchhoff.py:1048-1094``)."""

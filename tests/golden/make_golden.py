@@ -220,6 +220,25 @@ def main():
                         pylops_version=str(pylops.__version__))
     print("wrote traveltime_ana")
 
+    # 11) right-preconditioned LSQR with a warm start: lsqr(K * Diagonal(p), d, x0=z0)
+    from pylops.basicoperators import Diagonal
+
+    K = Kirchhoff(z, x, t, s2d, r2d, v0, wav, wavc, mode="analytic", dynamic=True,
+                  angleaperture=None, engine="numpy")
+    refl = np.zeros((PAR["nx"], PAR["nz"]))
+    refl[:, PAR["nz"] // 2] = 1
+    refl[:, 3 * PAR["nz"] // 4] = 1
+    d = K @ refl.ravel()
+    p = (1.0 + 0.1 * np.arange(PAR["nz"]))[np.newaxis, :] * np.ones((PAR["nx"], 1))
+    z0 = 0.3 * refl.ravel() / p.ravel()
+    its = []
+    out = lsqr(K * Diagonal(p.ravel()), d, x0=z0, niter=10, damp=0.0, atol=0.0, btol=1e-3,
+               callback=lambda xx: its.append(np.array(xx).copy()))
+    np.savez_compressed(os.path.join(OUT, "solvers_precond.npz"), d=d, p=p.ravel(), z0=z0,
+                        x=out[0], istop=out[1], iiter=out[2], r1=out[3], cost=out[10],
+                        iterates=np.array(its))
+    print("wrote solvers_precond")
+
 
 if __name__ == "__main__":
     sys.exit(main())

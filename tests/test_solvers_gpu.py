@@ -128,3 +128,32 @@ def test_lsm_two_reflectors_like_reference_test():
             dinv = (lsm.Demop * minv.ravel().astype(np.float32)).reshape(6, 4, nt)
             np.testing.assert_array_almost_equal(d / d.max(), dinv / d.max(), decimal=2)
             np.testing.assert_array_almost_equal(refl / refl.max(), minv / refl.max(), decimal=1)
+
+
+def test_right_preconditioned_lsqr_with_warm_start_tracks_reference():
+    """lsqr(Kop * Diagonal(p), d, x0=z0) runs on the device path (the diagonal
+    is folded into the captured iteration) and follows the reference's
+    iterates; the generic host-loop path on a scaled copy agrees."""
+    import torch
+
+    from pylops_gb300.basicoperators import Diagonal
+    from pylops_gb300.optimization import lsqr
+    from pylops_gb300.optimization.cls_basic import _is_device_kirchhoff
+
+    g = load("solvers_precond")
+    K = _op()
+    Op = K * Diagonal(g["p"].astype(np.float32), dtype="float32")
+    assert _is_device_kirchhoff(Op)
+    its = []
+    d = g["d"].astype(np.float32)
+    z0 = g["z0"].astype(np.float32)
+    out = lsqr(Op, d, x0=z0, niter=10, atol=0.0, btol=1e-3, callback=lambda x: its.append(np.array(x).copy()))
+    assert out[2] == int(g["iiter"]) and out[1] == int(g["istop"])
+    for k in range(len(its)):
+        assert rel(its[k], g["iterates"][k]) < 1e-4, (k, rel(its[k], g["iterates"][k]))
+    np.testing.assert_allclose(out[10], g["cost"], rtol=1e-4)
+    graph = lsqr(Op, d, x0=z0, niter=10, atol=0.0, btol=1e-3)
+    assert np.array_equal(graph[0], out[0])
+    generic = lsqr(1.0 * Op, torch.as_tensor(d, device="cuda"), x0=torch.as_tensor(z0, device="cuda"), niter=10,
+                   atol=0.0, btol=1e-3)[0]
+    assert rel(generic.cpu().numpy(), out[0]) < 1e-4

@@ -1,0 +1,112 @@
+"""U-Net preconditioner kernels against PyTorch CPU autograd (float32) on the
+same weights; the reference rounds weights, the network input and every
+hidden activation to bf16 like the GPU path, so the remaining differences
+are the bf16 rounding of the backward operands."""
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf(x):
+    return x.to(torch.bfloat16).to(torch.float32)
+
+
+def ref_forward(net, weights, x):
+    """Same topology as pylops_gb300.learned.UNet, NCHW, torch CPU."""
+    import torch.nn.functional as F
+
+    scale = 1.0 / torch.sqrt(torch.mean(x.double() ** 2, dim=(1, 2))).float()
+    h = _bf(x * scale[:, None, None])[:, None]
+
+    def conv(i, inp):
+        c = net.convs[i]
+        w, b = weights[i]
+        y = F.conv2d(inp, _bf(w), b, stride=c.stride, padding=c.ks // 2)
+        if c.relu:
+            y = torch.relu(y)
+        return _bf(y) if i != net.head else y
+
+    skips = []
+    for l, (a, b) in enumerate(net.enc):
+        h = conv(b, conv(a, h))
+        skips.append(h)
+    for l in range(net.levels - 2, -1, -1):
+        a, b = net.dec[l]
+        up = h.repeat_interleave(2, dim=2).repeat_interleave(2, dim=3)
+        h = conv(b, conv(a, torch.cat([up, skips[l]], dim=1)))
+    return conv(net.head, h)[:, 0]
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+@pytest.mark.parametrize("levels,base,B,H,W", [(3, 8, 2, 16, 32), (4, 16, 1, 32, 16)])
+def test_unet_forward_and_gradients_match_cpu_autograd(levels, base, B, H, W):
+    from pylops_gb300.learned.unet import UNet
+
+    net = UNet(levels=levels, base=base, seed=3)
+    g = torch.Generator().manual_seed(5)
+    x = torch.randn(B, H, W, generator=g)
+    t = 0.5 * torch.randn(B, H, W, generator=g)
+    out = net.forward(x.cuda()).cpu()
+    loss = float(net.loss_and_grad(x.cuda(), t.cuda()))
+    grads = net.gradients()
+    net.check_errors()
+
+    ws = [(torch.tensor(w, requires_grad=True), torch.tensor(b, requires_grad=True)) for w, b in net.get_weights()]
+    ref = ref_forward(net, ws, x)
+    ref_loss = torch.mean((ref - t) ** 2)
+    ref_loss.backward()
+    assert _rel(out.numpy(), ref.detach().numpy()) < 1e-2
+    assert abs(loss - float(ref_loss)) / float(ref_loss) < 1e-2
+    for i, ((gw, gb), (w, b)) in enumerate(zip(grads, ws)):
+        ew = _rel(gw, w.grad.numpy())
+        eb = _rel(gb, b.grad.numpy())
+        assert ew < 5e-2, f"layer {i} weight gradient error {ew:.3e}"
+        assert eb < 5e-2, f"layer {i} bias gradient error {eb:.3e}"
+
+
+def test_unet_training_is_deterministic_and_lowers_the_loss():
+    from pylops_gb300.learned.unet import UNet
+
+    g = torch.Generator().manual_seed(11)
+    x = torch.randn(4, 32, 32, generator=g).cuda()
+    t = torch.relu(x)  # a pointwise map of the input: learnable
+    a, b = UNet(levels=3, base=8, seed=0), UNet(levels=3, base=8, seed=0)
+    losses = []
+    for _ in range(60):
+        la = float(a.train_step(x, t, lr=3e-3))
+        lb = float(b.train_step(x, t, lr=3e-3))
+        assert la == lb
+        losses.append(la)
+    assert torch.equal(a.params, b.params)
+    assert losses[-1] < 0.3 * losses[0], losses[::10]
+    a.check_errors()
+
+
+def test_splitk_gemm_matches_fp32_reference():
+    from pylops_gb300 import _native
+
+    g = torch.Generator().manual_seed(2)
+    for M, N, K, splits in [(32, 288, 4096, 0), (1, 32, 2048, 7), (64, 9, 1024, 3), (128, 200, 520, 1)]:
+        A = torch.randn(M, K, generator=g).to(torch.bfloat16)
+        B = torch.randn(N, K, generator=g).to(torch.bfloat16)
+        ldc = N + 8
+        C = torch.full((M, ldc), 7.0, device="cuda")
+        work = torch.empty(1 << 20, device="cuda")
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        Ad, Bd = A.cuda(), B.cuda()
+        _native.check(_native.lib().kgb_gemm_bf16_tn_splitk(
+            Ad.data_ptr(), Bd.data_ptr(), C.data_ptr(), M, N, K, K, K, ldc, splits, work.data_ptr(), work.numel(),
+            err.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        ref = A.float() @ B.float().T
+        got = C.cpu()
+        assert int(err.item()) == 0
+        assert _rel(got[:, :N].numpy(), ref.numpy()) < 1e-5
+        assert torch.all(got[:, N:] == 7.0)
