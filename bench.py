@@ -503,6 +503,69 @@ def run_batch(args):
     }))
 
 
+def run_lsm(args):
+    """Learned-preconditioned LSM workload: 2-D dynamic eikonal Kirchhoff,
+    v(z) = 1500 + 0.6 z on 256 x 512 at 5 m, 48 sources, 256 receivers,
+    nt = 1201 at 2 ms, 15 Hz Ricker.  The BF16 U-Net is trained on
+    --lsm-train pairs that the operator generates from seeded random models;
+    a step is one held-out model solved to a 1e-2 relative data residual.
+    value = median wall time of the learned solve (plain GPU LSQR beside it)."""
+    import torch
+
+    from pylops_gb300.learned import experiment
+
+    clocks = ClockSampler()
+    clocks.start()
+    out, ctx = experiment.run(n_train=args.lsm_train, n_test=args.steps, steps=args.lsm_steps, batch=8,
+                              niter=600, variants=("plain", "warm", "learned"),
+                              log=lambda *a: print(*a, file=sys.stderr, flush=True), return_objects=True)
+    clk = clocks.stop()
+    op, tests = ctx["op"], ctx["tests"]
+    learned, _ = ctx["solvers"]["learned"]
+    v = out["variants"]
+    # end to end: host data in, host model out, through LearnedLSM.solve
+    e2e_s = []
+    for m in tests[:min(8, len(tests))]:
+        d = (op @ torch.as_tensor(m.reshape(-1), device="cuda")).cpu().numpy()
+        _, info = learned.solve(d, tol=1e-2, niter=600)
+        e2e_s.append(info.seconds)
+    e2e = statistics.median(e2e_s)
+    # tensor-core roofline of a training step (convolution GEMMs)
+    step_s = out["train_seconds"] / args.lsm_steps
+    achieved = out["network_flops_per_train_image"] * 8 / step_s / 1e12
+    peaks = _peaks()
+    peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops") or 1700.0
+    line = {
+        "metric": "LSM seconds to 1e-2 relative data residual, learned vs plain GPU LSQR",
+        "value": round(v["learned"]["seconds_median"], 4), "unit": "s", "n_gpus": 1, "steps": args.steps,
+        "warmup": 1, "ms_per_step": round(v["learned"]["seconds_median"] * 1e3, 2), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 operator, bf16 network", "data": "synthetic",
+        "config": {"workload": "learned_lsm_2d_eikonal_dyn_256x512_48x256_nt1201", "train_pairs": args.lsm_train,
+                   "train_steps": args.lsm_steps, "batch": 8, "held_out_models": args.steps, "tol": 1e-2,
+                   "l2": "operator tables (478 MB) larger than L2"},
+        "plain_lsqr": v["plain"], "warm_start_only": v["warm"], "learned": v["learned"],
+        "speedup_vs_plain_median": round(v["learned"]["speedup_vs_plain_median"], 3),
+        "train": {k: out.get(k) for k in ("pairs_seconds", "train_seconds", "train_loss_first", "train_loss_last",
+                                          "inference_ms")},
+        "e2e": {"value": round(e2e, 4), "unit": "s", "h2d_bytes_per_step": int(op.shape[0] * 4),
+                "d2h_bytes_per_step": int(op.shape[1] * 4)},
+        "roofline": {"bound": "tensor", "kernel": "U-Net training step (tcgen05 GEMMs + unfold)",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
+                     "frac": round(achieved / peak, 4), "traffic": None},
+        "gpu_launches": int(v["learned"]["gpu_launches_median"]),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        m = tests[0].reshape(-1).astype(np.float64)
+        dd = np.random.default_rng(0).standard_normal(op.shape[0])
+        rec, _, _, _ = cpu_baseline(op, m, dd, target_s=args.cpu_seconds)
+        its = v["plain"]["iterations_median"]
+        per_it = compulsory_bytes(op.ni, op.ns, op.nr, op.nt) / (rec["value"] * 1e9)
+        line["cpu_baseline"] = {"value": round(per_it * its, 2), "unit": "s", "cores": rec["cores"], "kind": "port",
+                                "sample": rec["sample"] + f"; x {its:.0f} plain LSQR iterations"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -515,8 +578,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch"],
-                    help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems")
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm"],
+                    help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems; "
+                         "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models)")
+    ap.add_argument("--lsm-train", type=int, default=4096)
+    ap.add_argument("--lsm-steps", type=int, default=3000)
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--cgls-iters", type=int, default=20)
     args = ap.parse_args()
@@ -526,6 +592,8 @@ def main():
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "lsm":
+        run_lsm(args)
     else:
         run_gpu(args)
 

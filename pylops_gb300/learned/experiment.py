@@ -62,7 +62,7 @@ def _summary(infos, errs):
 def run(n_train: int = 4096, n_test: int = 64, steps: int = 2000, batch: int = 8, lr: float = 1e-3,
         tol: float = 1e-2, niter: int = 600, seed: int = 0, levels: int = 4, base: int = 32,
         variants=("plain", "warm", "learned"), steps_net: int = 4, step_ratio: float = 0.7, log=print,
-        op=None, net_state: dict = None, save_net: str = None) -> dict:
+        op=None, net_state: dict = None, save_net: str = None, return_objects: bool = False):
     import torch
 
     out = {"config": {"n_train": n_train, "n_test": n_test, "steps": steps, "batch": batch, "lr": lr,
@@ -145,6 +145,10 @@ def run(n_train: int = 4096, n_test: int = 64, steps: int = 2000, batch: int = 8
     for v in variants:
         if base_t:
             out["variants"][v]["speedup_vs_plain_median"] = base_t / out["variants"][v]["seconds_median"]
+        out["variants"][v]["gpu_launches_median"] = float(np.median([i.gpu_launches for i in res[v][0]]))
+    out["network_flops_per_train_image"] = net.flops(nx, nz, training=True)
+    if return_objects:
+        return out, {"op": op, "net": net, "tests": tests, "solvers": solvers}
     return out
 
 

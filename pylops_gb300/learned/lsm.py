@@ -169,6 +169,7 @@ class SolveInfo:
     network_steps: int = 0
     network_residual: float = 1.0
     operator_pairs: int = 0
+    gpu_launches: int = 0
     cost: List[float] = field(default_factory=list)
 
 
@@ -250,6 +251,9 @@ class LearnedLSM:
         c = np.zeros(0)
         rel = 1.0
         pairs = 0
+        info = op.info()
+        fa = info["kernels_forward"] + info["kernels_adjoint"]
+        self._launches = 1  # the |d|^2 dot
         src = d
         for j in range(nmax):
             op.apply_into(src, g, adjoint=True)
@@ -257,6 +261,7 @@ class LearnedLSM:
             q = torch.empty_like(d)
             op.apply_into(p, q)
             pairs += 1
+            self._launches += fa + self.net.launches_per_forward + len(Q) + 2
             vals = self._dots([(q, v) for v in Q] + [(q, q), (q, d)])
             G[j, :j] = G[:j, j] = vals[:j]
             G[j, j] = vals[j]
@@ -273,27 +278,38 @@ class LearnedLSM:
             if rel <= tol or j == nmax - 1:
                 break
             self._lincomb(r, d, 1.0, Q, -c)  # r = d - sum c_j K p_j
+            self._launches += 1
             src = r
         if not P:
             return None, 1.0, 0, pairs
         x = torch.empty(op.ni, dtype=torch.float32, device="cuda")
         self._lincomb(x, None, 0.0, P, c)
+        self._launches += 1
         return x, rel, len(P), pairs
 
     def solve(self, d, tol: float = 1e-2, niter: int = 500, use_net: bool = True) -> tuple:
-        """Returns ``(x, SolveInfo)``; x is the model (float32 CUDA tensor)."""
+        """Returns ``(x, SolveInfo)``.  ``d`` is a CUDA tensor (x is then a
+        float32 CUDA tensor) or a host array (staged through pinned memory
+        inside the timed region; x is then a numpy array)."""
         import torch
 
         from ..basicoperators import Diagonal
         from ..optimization.cls_basic import LSQR
 
         op = self.op
-        dd = d.to(device="cuda", dtype=torch.float32).reshape(-1).contiguous()
+        host = not torch.is_tensor(d)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        if host:  # host data: pinned staging copy inside the timed region
+            dd = torch.from_numpy(np.ascontiguousarray(d, dtype=np.float32).reshape(-1)).pin_memory().to(
+                "cuda", non_blocking=True)
+        else:
+            dd = d.to(device="cuda", dtype=torch.float32).reshape(-1).contiguous()
         x0, rel0, nsteps, pairs = None, 1.0, 0, 0
+        self._launches = 0
         if use_net and self.net is not None:
             x0, rel0, nsteps, pairs = self.network_phase(dd, tol)
+        launches = self._launches
         iiter, istop, cost = 0, 1, [rel0]
         x = x0
         if rel0 > tol:
@@ -305,13 +321,25 @@ class LearnedLSM:
                                                                 niter=niter, calc_var=False)
             x = z if self._diag_dev is None else z * self._diag_dev
             pairs += int(iiter) + 1
+            info = op.info()
+            F = info["kernels_forward"] + (0 if self._diag_dev is None else 1)
+            A = info["kernels_adjoint"] + (0 if self._diag_dev is None else 1)
+            # setup: state, |u|, beta, scale, [K x0, subtract], K^H u, |v|, alfa, scale, copy, target;
+            # one iteration: K v, u update, beta, scale, K^H u, v update, rotation, x/w update, tail
+            launches += 10 + A + (F + 1 if x0 is not None else 0) + int(iiter) * (7 + F + A)
+        if host:
+            x = x.cpu().numpy()
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
+        if host:
+            x = torch.as_tensor(x, device="cuda")
         kx = torch.empty_like(dd)
         op.apply_into(x.contiguous(), kx)
         r = torch.empty_like(dd)
         self._lincomb(r, kx, 1.0, [dd], [-1.0])
         rr, d2 = self._dots([(r, r), (dd, dd)])
         res = math.sqrt(rr / d2) if d2 > 0 else 0.0
-        return x, SolveInfo(int(iiter), secs, res, int(istop), nsteps, rel0, pairs,
+        if host:
+            x = x.cpu().numpy()
+        return x, SolveInfo(int(iiter), secs, res, int(istop), nsteps, rel0, pairs, launches,
                             [float(v) for v in np.asarray(cost)])

@@ -185,6 +185,33 @@ class UNet:
         self.step_count = int(sd.get("step", 0))
         self._refresh_weights()
 
+    @property
+    def launches_per_forward(self) -> int:
+        """Kernel launches of one ``forward``: input RMS and bf16 cast, an
+        unfold (except for the 1x1 head) and a GEMM per convolution, an
+        upsample and a skip copy per decoder level."""
+        unfolds = sum(1 for c in self.convs if not (c.ks == 1 and c.stride == 1 and c.cin % 8 == 0))
+        return (2 if self.normalize else 1) + unfolds + len(self.convs) + 2 * len(self.dec)
+
+    def flops(self, H: int, W: int, training: bool = False) -> float:
+        """Algorithmic multiply-add flops (2 per MAC) of the convolutions for
+        one H x W image: forward, or forward + weight and data gradients."""
+        hw = [(H >> l, W >> l) for l in range(self.levels)]
+        lvl = {}
+        for l, (a, b) in enumerate(self.enc):
+            lvl[a] = lvl[b] = l
+        for l, (a, b) in self.dec.items():
+            lvl[a] = lvl[b] = l
+        lvl[self.head] = 0
+        total = 0.0
+        for i, c in enumerate(self.convs):
+            h, w = hw[lvl[i]]
+            f = 2.0 * h * w * c.cout * c.kc
+            total += f
+            if training:
+                total += f + (f if i != 0 else 0.0)
+        return total
+
     # ------------------------------------------------------------ buffers
     def _workspace(self, B: int, H: int, W: int):
         import torch
