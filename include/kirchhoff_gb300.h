@@ -251,7 +251,8 @@ int kgb_gemm_bf16_tn_splitk(const void* A_dev, const void* B_dev, float* C_dev, 
  *  weights      bf16 W (Cout x Kpad) and, if Wt != NULL, Wt (Cin x Kg) with
  *               Wt[ci][tap*Cout + co] = W[co][tap*Cin + ci], from float32 W;
  *  relu_grad    g = dy * (y > 0) (relu) or dy, as bf16;
- *  rowsum       out[r] = sum_c in[r][c] (bf16 in, bias gradients);
+ *  rowsum       out[r] = sum_c in[r][c] (bf16 in, bias gradients; work:
+ *               rows x 64 floats of scratch);
  *  upsample     nearest x2 of x into channels [coff, coff+C) of y (Ctot
  *               channels), or (grad) its adjoint from float32 dy;
  *  channels     put (bf16 x into channels of y) or take (float32 channels of
@@ -268,7 +269,7 @@ int kgb_unet_transpose(const void* in, void* out, int64_t rows, int cols, int64_
                        void* stream);
 int kgb_unet_weights(const float* W, void* Wb, void* Wt, int Cout, int Cin, int ks, int Kpad, int Kg, void* stream);
 int kgb_unet_relu_grad(const float* dy, const void* y, void* g, int64_t n, int relu, void* stream);
-int kgb_unet_rowsum(const void* in, float* out, int rows, int64_t cols, void* stream);
+int kgb_unet_rowsum(const void* in, float* out, int rows, int64_t cols, float* work, void* stream);
 int kgb_unet_upsample(const void* x, void* y, int B, int H, int W, int C, int Ctot, int coff, int grad,
                       void* stream);
 int kgb_unet_channels(const void* x, void* y, int64_t P, int C, int Ctot, int coff, int take, int accumulate,

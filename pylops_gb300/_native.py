@@ -80,7 +80,7 @@ _SIGNATURES = {
     "kgb_unet_transpose": ([c_vp, c_vp, c_i64, c_int, c_i64, c_i64, c_int, c_vp], c_int),
     "kgb_unet_weights": ([c_vp, c_vp, c_vp] + [c_int] * 5 + [c_vp], c_int),
     "kgb_unet_relu_grad": ([c_vp, c_vp, c_vp, c_i64, c_int, c_vp], c_int),
-    "kgb_unet_rowsum": ([c_vp, c_vp, c_int, c_i64, c_vp], c_int),
+    "kgb_unet_rowsum": ([c_vp, c_vp, c_int, c_i64, c_vp, c_vp], c_int),
     "kgb_unet_upsample": ([c_vp, c_vp] + [c_int] * 7 + [c_vp], c_int),
     "kgb_unet_channels": ([c_vp, c_vp, c_i64, c_int, c_int, c_int, c_int, c_int, c_vp], c_int),
     "kgb_unet_to_bf16": ([c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),

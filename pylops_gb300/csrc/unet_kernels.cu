@@ -110,6 +110,55 @@ __global__ void unfold_t_kernel(const bf16* __restrict__ x, bf16* __restrict__ c
     }
 }
 
+// Vector form of unfold_t for C % 8 == 0 and P % 8 == 0: each thread moves
+// an 8-pixel x 8-channel block of one tap (eight 16-byte loads, an 8 x 8
+// transpose of 16-bit values in registers, eight 16-byte stores).
+// Consecutive threads take consecutive pixel groups, so a warp stores 512
+// contiguous bytes of a colT row.
+__global__ void unfold_t_vec_kernel(const bf16* __restrict__ x, bf16* __restrict__ colT, int H, int W, int C, int Ho,
+                                    int Wo, int ks, int s, int64_t P) {
+    const int pad = ks >> 1;
+    const int cgn = C >> 3;
+    const int64_t pgn = P >> 3;
+    const int64_t total = (int64_t)ks * ks * cgn * pgn;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pg = i % pgn;
+        const int64_t rest = i / pgn;
+        const int cg = (int)(rest % cgn);
+        const int tap = (int)(rest / cgn);
+        const int ky = tap / ks, kx = tap - ky * ks;
+        uint32_t v[8][4];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int64_t p = pg * 8 + j;
+            const int wo = (int)(p % Wo);
+            const int64_t t = p / Wo;
+            const int ho = (int)(t % Ho);
+            const int b = (int)(t / Ho);
+            const int h = ho * s + ky - pad, w = wo * s + kx - pad;
+            uint4 u = make_uint4(0, 0, 0, 0);
+            if (h >= 0 && h < H && w >= 0 && w < W)
+                u = __ldg(reinterpret_cast<const uint4*>(x + (((int64_t)b * H + h) * W + w) * C + cg * 8));
+            v[j][0] = u.x;
+            v[j][1] = u.y;
+            v[j][2] = u.z;
+            v[j][3] = u.w;
+        }
+        // channel k of pixel j is the (k & 1) half of word k >> 1 of v[j]
+        bf16* dst = colT + ((int64_t)tap * C + cg * 8) * P + pg * 8;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t sel = (k & 1) ? 0x7632u : 0x5410u;  // high or low halves of two words
+            uint4 o;
+            o.x = __byte_perm(v[0][k >> 1], v[1][k >> 1], sel);
+            o.y = __byte_perm(v[2][k >> 1], v[3][k >> 1], sel);
+            o.z = __byte_perm(v[4][k >> 1], v[5][k >> 1], sel);
+            o.w = __byte_perm(v[6][k >> 1], v[7][k >> 1], sel);
+            *reinterpret_cast<uint4*>(dst + (int64_t)k * P) = o;
+        }
+    }
+}
+
 // out[c][r] = in[r][c]; rows x cols, in leading dimension ldi, out ldo.
 template <typename TI, typename TO>
 __global__ void transpose_kernel(const TI* __restrict__ in, TO* __restrict__ out, int64_t rows, int cols, int64_t ldi,
@@ -161,19 +210,33 @@ __global__ void relu_grad_kernel(const float* __restrict__ dy, const bf16* __res
     }
 }
 
-// out[r] = sum_c in[r][c] (bias gradient from g^T), fixed reduction order
-__global__ void rowsum_kernel(const bf16* __restrict__ in, float* __restrict__ out, int64_t cols) {
-    const int r = blockIdx.x;
+// Row sums of a bf16 matrix (bias gradients from g^T) in two passes with a
+// fixed order: block (r, k) sums chunk k of row r into work[r][k], then one
+// thread per row adds the chunks in order.
+constexpr int kRowChunks = 64;
+__global__ void rowsum_partial_kernel(const bf16* __restrict__ in, float* __restrict__ work, int64_t cols) {
+    const int r = blockIdx.x, k = blockIdx.y;
+    const int64_t chunk = (cols + kRowChunks - 1) / kRowChunks;
+    const int64_t c0 = (int64_t)k * chunk, c1 = min(cols, c0 + chunk);
+    const bf16* row = in + (int64_t)r * cols;
     float acc = 0.f;
-    for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) acc += __bfloat162float(in[r * cols + c]);
-    __shared__ float sh[512];
+    for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) acc += __bfloat162float(row[c]);
+    __shared__ float sh[256];
     sh[threadIdx.x] = acc;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[r] = sh[0];
+    if (threadIdx.x == 0) work[r * kRowChunks + k] = sh[0];
+}
+
+__global__ void rowsum_final_kernel(const float* __restrict__ work, float* __restrict__ out, int rows) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    float acc = 0.f;
+    for (int k = 0; k < kRowChunks; ++k) acc += work[r * kRowChunks + k];
+    out[r] = acc;
 }
 
 // nearest x2 upsampling of x (B x H x W x C) into channels [coff, coff+C)
@@ -329,9 +392,15 @@ int kgb_unet_unfold_t(const void* x, void* colT, int B, int H, int W, int C, int
     const int Ho = (H + 2 * pad - ks) / stride + 1, Wo = (W + 2 * pad - ks) / stride + 1;
     const int64_t P = (int64_t)B * Ho * Wo;
     if ((P + 31) / 32 > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "unet_unfold_t: too many pixels");
-    dim3 grid((unsigned)((P + 31) / 32), (unsigned)((C + 31) / 32), (unsigned)(ks * ks)), block(32, 8);
-    unfold_t_kernel<<<grid, block, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, B, H, W, C, Ho, Wo, ks,
-                                                              stride, P);
+    if (C % 8 == 0 && P % 8 == 0 && ((uintptr_t)x & 15) == 0 && ((uintptr_t)colT & 15) == 0) {
+        const int64_t n = (int64_t)ks * ks * (C / 8) * (P / 8);
+        unfold_t_vec_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, H, W, C, Ho,
+                                                                            Wo, ks, stride, P);
+    } else {
+        dim3 grid((unsigned)((P + 31) / 32), (unsigned)((C + 31) / 32), (unsigned)(ks * ks)), block(32, 8);
+        unfold_t_kernel<<<grid, block, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, B, H, W, C, Ho, Wo,
+                                                                  ks, stride, P);
+    }
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -370,9 +439,11 @@ int kgb_unet_relu_grad(const float* dy, const void* y, void* g, int64_t n, int r
     return KGB_OK;
 }
 
-int kgb_unet_rowsum(const void* in, float* out, int rows, int64_t cols, void* stream) {
-    if (!in || !out || rows <= 0 || cols <= 0) return set_error(KGB_ERR_VALUE, "unet_rowsum: bad arguments");
-    rowsum_kernel<<<rows, 512, 0, (cudaStream_t)stream>>>((const bf16*)in, out, cols);
+int kgb_unet_rowsum(const void* in, float* out, int rows, int64_t cols, float* work, void* stream) {
+    if (!in || !out || !work || rows <= 0 || cols <= 0) return set_error(KGB_ERR_VALUE, "unet_rowsum: bad arguments");
+    dim3 grid((unsigned)rows, (unsigned)kRowChunks);
+    rowsum_partial_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const bf16*)in, work, cols);
+    rowsum_final_kernel<<<(rows + 127) / 128, 128, 0, (cudaStream_t)stream>>>(work, out, rows);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

@@ -309,7 +309,8 @@ class UNet:
             gT = g
         else:
             _native.check(L.kgb_unet_transpose(g.data_ptr(), gT.data_ptr(), P_out, c.cout, c.cout, P_out, 0, s))
-        _native.check(L.kgb_unet_rowsum(gT.data_ptr(), self._db(c).data_ptr(), c.cout, P_out, s))
+        _native.check(L.kgb_unet_rowsum(gT.data_ptr(), self._db(c).data_ptr(), c.cout, P_out, ws["work"].data_ptr(),
+                                         s))
         _native.check(L.kgb_unet_unfold_t(x.data_ptr(), col.data_ptr(), B, H, W, c.cin, c.ks, c.stride, s))
         _native.check(L.kgb_gemm_bf16_tn_splitk(gT.data_ptr(), col.data_ptr(), self._dw(c).data_ptr(), c.cout, c.kc,
                                                 P_out, P_out, P_out, c.kpad, 0, ws["work"].data_ptr(),
