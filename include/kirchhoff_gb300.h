@@ -66,6 +66,18 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op);
 int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* trav_srcs_host,
                                   const double* trav_recs_host);
 
+/* Single traveltime table: trav (ni, ns*nr) float64 in the reference layout
+ * (trav[ii][is*nr + ir], the `trav` array of mode='byot').  Kinematic
+ * operators only (a dynamic operator returns KGB_ERR_NOT_IMPLEMENTED, as the
+ * reference raises).  The index is the reference's int(t/dt) and the
+ * fraction t/dt - int(t/dt) (kept to 2^-19 samples or better); stored
+ * trace-major in HBM, 4 bytes per entry (8 if any time is negative).  The
+ * operator then spreads and gathers with this table instead of per-source
+ * and per-receiver tables.
+ * Replaces: itrav/travd (kirchhoff.py:396-398) and _trav_kirch_matvec /
+ * _trav_kirch_rmatvec (kirchhoff.py:684-725). */
+int kgb_kirchhoff_set_traveltime_table(kgb_kirchhoff* op, const double* trav);
+
 /* Upload the dynamic-mode tables (reference layout, float64): amplitudes and
  * angles (ni, ns) / (ni, nr), velocity (ni), aperture [min, max], angle
  * aperture [min, max] in radians, the 21-sample aperture taper and the

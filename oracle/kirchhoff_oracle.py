@@ -263,6 +263,40 @@ def kirch_rmatvec(d, ns, nr, nt, ni, dt, trav_srcs, trav_recs, dyn=None):
     return img
 
 
+def single_table_index(trav, dt):
+    """``itrav = (trav / dt).astype('int32')``, ``travd = trav / dt - itrav``
+    (``kirchhoff.py:396-398``) for a single table of shape (ni, ns*nr)."""
+    tt = np.asarray(trav, dtype=np.float64) / dt
+    it = tt.astype(np.int32)
+    return it, tt - it
+
+
+def trav_matvec(x, nsnr, nt, ni, itrav, travd):
+    """Single-table forward spreading, ``Kirchhoff._trav_kirch_matvec``
+    (``kirchhoff.py:684-704``); y of shape (nsnr, nt)."""
+    x = np.asarray(x, dtype=np.float64).ravel()
+    y = np.zeros((nsnr, nt))
+    for k in range(nsnr):
+        it, w = itrav[:, k].astype(np.int64), travd[:, k]
+        ok = (it >= 0) & (it < nt - 1)
+        y[k] += np.bincount(it[ok], weights=x[ok] * (1 - w[ok]), minlength=nt)[:nt]
+        y[k] += np.bincount(it[ok] + 1, weights=x[ok] * w[ok], minlength=nt)[:nt]
+    return y
+
+
+def trav_rmatvec(d, nsnr, nt, ni, itrav, travd):
+    """Single-table adjoint gathering, ``Kirchhoff._trav_kirch_rmatvec``
+    (``kirchhoff.py:707-725``); image of length ni."""
+    d = np.asarray(d, dtype=np.float64).reshape(nsnr, nt)
+    img = np.zeros(ni)
+    for k in range(nsnr):
+        it, w = itrav[:, k].astype(np.int64), travd[:, k]
+        ok = (it >= 0) & (it < nt - 1)
+        itc = np.where(ok, it, 0)
+        img += np.where(ok, d[k, itc] * (1 - w) + d[k, np.minimum(itc + 1, nt - 1)] * w, 0.0)
+    return img
+
+
 # ----------------------------------------------------------------------------
 # operator wrapper (constructor semantics of kirchhoff.py:234-455)
 # ----------------------------------------------------------------------------

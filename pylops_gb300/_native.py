@@ -46,6 +46,7 @@ _SIGNATURES = {
     "kgb_kirchhoff_create": ([ctypes.POINTER(c_vp), c_int, c_int, c_int, c_i64, c_int, c_dbl, c_int, c_dp, c_int, c_int], c_int),
     "kgb_kirchhoff_destroy": ([c_vp], c_int),
     "kgb_kirchhoff_set_traveltimes": ([c_vp, c_dp, c_dp], c_int),
+    "kgb_kirchhoff_set_traveltime_table": ([c_vp, c_dp], c_int),
     "kgb_kirchhoff_set_dynamic": ([c_vp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_i64p, c_i64p], c_int),
     "kgb_kirchhoff_forward": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),

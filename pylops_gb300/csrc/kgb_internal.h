@@ -56,6 +56,12 @@ struct KirchDev {
     // which the row's weight is exactly zero, packed lo | hi << 16
     const uint32_t* srng;  // [ns][ncol]
     const uint32_t* rrng;  // [nr][ncol]
+    // single traveltime table (one entry per image point and trace, mode
+    // 'byot' with trav of shape (ni, ns*nr)): tq1[tr][ii] is the fixed-point
+    // sample count (tw1 == nullptr) or, for tables with negative times, the
+    // truncated index int(t/dt) with the fraction in tw1[tr][ii]
+    const int32_t* tq1;
+    const float* tw1;
 };
 
 // Launchers (kirchhoff_kernels.cu).  All asynchronous on `stream`.
@@ -117,6 +123,8 @@ struct kgb_kirchhoff {
     int4* rtab = nullptr;
     uint32_t* srng = nullptr;
     uint32_t* rrng = nullptr;
+    int32_t* tq1 = nullptr;    // single traveltime table (trace-major), see KirchDev
+    float* tw1 = nullptr;
     float* dcorr = nullptr;    // scratch: correlated data for the adjoint, interleaved pairs (2 x ndata)
     float* partial = nullptr;  // scratch: per-receiver-split partial images
     int64_t partial_elems = 0;
@@ -133,6 +141,7 @@ struct kgb_kirchhoff {
         K.nonneg = nonneg ? 1 : 0; K.wmax = wmax; K.mv = mv; K.absmax = absmax;
         K.spread_variant = spread_variant;
         K.stab = stab; K.rtab = rtab; K.srng = srng; K.rrng = rrng;
+        K.tq1 = tq1; K.tw1 = tw1;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

@@ -166,7 +166,7 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     cudaSetDevice(op->device);
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
                     op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
-                    op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng};
+                    op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng, op->tq1, op->tw1};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);
@@ -225,6 +225,87 @@ int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* ts, const dou
     (void)mins; (void)minr;
     op->trav_ready = true;
     return repack(op);
+}
+
+int kgb_kirchhoff_set_traveltime_table(kgb_kirchhoff* op, const double* trav) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (!trav) return set_error(KGB_ERR_VALUE, "set_traveltime_table: null table");
+    if (op->dynamic)
+        return set_error(KGB_ERR_NOT_IMPLEMENTED,
+                         "separate traveltime tables must be provided when selecting mode=dynamic");
+    const int64_t ni = op->ni;
+    const int nsnr = (int)op->npair();
+    const int64_t n = ni * nsnr;
+    const double inv_dt = 1.0 / op->dt;
+    double maxs = 0.0, mins = INFINITY;
+    int64_t bad = -1;
+#pragma omp parallel for reduction(max : maxs) reduction(max : bad) reduction(min : mins)
+    for (int64_t k = 0; k < n; ++k) {
+        const double u = trav[k] * inv_dt;
+        if (!isfinite(u)) bad = std::max(bad, k);
+        else {
+            maxs = std::max(maxs, fabs(u));
+            mins = std::min(mins, u);
+        }
+    }
+    if (bad >= 0)
+        return set_error(KGB_ERR_VALUE, "set_traveltime_table: non-finite traveltime at flat index %lld",
+                         (long long)bad);
+    // fixed point (index exact, fraction to 2^-F) when every time is >= 0;
+    // otherwise the truncated index and the fraction separately, which keeps
+    // the reference's -1 < t/dt < 0 case (index 0, negative fraction)
+    const bool fixed = mins >= 0.0;
+    const int F = choose_frac_bits(std::min(maxs, (double)op->nt + 2.0), op->nt);
+    const double scale = ldexp(1.0, F);
+    const int64_t fmax = ((int64_t)1 << F) - 1;
+    int rc;
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    if (!op->tq1 && (rc = dev_alloc(&op->tq1, (size_t)n, "alloc traveltime table"))) return rc;
+    if (!fixed && !op->tw1 && (rc = dev_alloc(&op->tw1, (size_t)n, "alloc traveltime fractions"))) return rc;
+    if (fixed && op->tw1) {
+        cudaFree(op->tw1);
+        op->tw1 = nullptr;
+    }
+    // (ni, nsnr) -> (nsnr, ni), a chunk of traces at a time
+    const int C = (int)std::max<int64_t>(1, std::min<int64_t>(nsnr, (int64_t)(64 << 20) / std::max<int64_t>(ni, 1)));
+    std::vector<int32_t> q((size_t)C * ni);
+    std::vector<float> wv(fixed ? 0 : (size_t)C * ni);
+    for (int j0 = 0; j0 < nsnr; j0 += C) {
+        const int nj = std::min(C, nsnr - j0);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < ni; ++i) {
+            const double* row = trav + (size_t)i * nsnr + j0;
+            for (int j = 0; j < nj; ++j) {
+                const double u = row[j] * inv_dt;
+                // itrav = (trav / dt).astype(int32): truncation toward zero
+                const double ut = std::max(-1073741824.0, std::min(1073741824.0, u));
+                const int32_t it = (int32_t)ut;
+                int32_t v;
+                if (fixed) {
+                    if (it >= op->nt) {
+                        v = INT32_MAX;  // outside the trace: never valid
+                    } else {
+                        int64_t fq = llrint((u - it) * scale);
+                        fq = std::max<int64_t>(0, std::min(fq, fmax));
+                        v = (int32_t)(((int64_t)it << F) + fq);
+                    }
+                } else {
+                    v = it;
+                    wv[(size_t)j * ni + i] = (float)(u - it);
+                }
+                q[(size_t)j * ni + i] = v;
+            }
+        }
+        KGB_CUDA_TRY(cudaMemcpy(op->tq1 + (size_t)j0 * ni, q.data(), (size_t)nj * ni * sizeof(int32_t),
+                                cudaMemcpyHostToDevice));
+        if (!fixed)
+            KGB_CUDA_TRY(cudaMemcpy(op->tw1 + (size_t)j0 * ni, wv.data(), (size_t)nj * ni * sizeof(float),
+                                    cudaMemcpyHostToDevice));
+    }
+    op->frac_bits = F;
+    op->nonneg = true;
+    op->trav_ready = true;
+    return KGB_OK;
 }
 
 int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const double* amp_r,

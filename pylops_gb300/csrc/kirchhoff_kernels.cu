@@ -744,6 +744,230 @@ int spread_dispatch(const KirchDev& K, bool dynamic, bool gate, const float* m, 
     return spread_dispatch_nn<false, false>(K, m, y, h, L, fuse, stream, prep);
 }
 
+// ---------------------------------------------------------------------------
+// Single traveltime table (kirchhoff.py:396-398, 684-725): one table entry
+// per (image point, trace), t/dt = itrav + travd with itrav = int(t/dt).
+// The table is the whole input of the operator (4 bytes per pair-point, read
+// once per application), so both directions stream it from HBM with
+// evict-first loads; they are HBM-bound by design.
+// ---------------------------------------------------------------------------
+template <bool FIXED>
+__device__ __forceinline__ bool single_entry(const KirchDev& K, const FixedPoint<true>& fp, int q, float wf, int& it,
+                                             float& w) {
+    if (FIXED) {
+        if (!fp.valid(q)) return false;
+        it = fp.index(q);
+        w = fp.frac(q, it);
+        return true;
+    }
+    it = q;
+    w = wf;
+    return (unsigned)q < (unsigned)(K.nt - 1);
+}
+
+// Adjoint: one thread per image point, traces [t0, t1) of its split in
+// order; four table entries in flight per thread.
+template <bool FIXED>
+__global__ void __launch_bounds__(256)
+gather1_kernel(const KirchDev K, const FixedPoint<true> fp, const float2* __restrict__ d2, float* __restrict__ out,
+               int tr_per_split) {
+    const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (ii >= K.ni) return;
+    const int nsnr = K.ns * K.nr;
+    const int t0 = blockIdx.y * tr_per_split;
+    const int t1 = min(nsnr, t0 + tr_per_split);
+    const int32_t* __restrict__ tq = K.tq1 + ii;
+    const float* __restrict__ tw = FIXED ? nullptr : K.tw1 + ii;
+    float acc = 0.f;
+    int tr = t0;
+    for (; tr + 4 <= t1; tr += 4) {
+        int q[4];
+        float wf[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            q[u] = __ldcs(tq + (size_t)(tr + u) * K.ni);
+            wf[u] = FIXED ? 0.f : __ldcs(tw + (size_t)(tr + u) * K.ni);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int it;
+            float w;
+            if (single_entry<FIXED>(K, fp, q[u], wf[u], it, w)) {
+                const float2 p = __ldg(d2 + (size_t)(tr + u) * K.nt + it);
+                acc = fmaf(p.x, 1.f - w, acc);
+                acc = fmaf(p.y, w, acc);
+            }
+        }
+    }
+    for (; tr < t1; ++tr) {
+        int it;
+        float w;
+        const int q = __ldcs(tq + (size_t)tr * K.ni);
+        const float wf = FIXED ? 0.f : __ldcs(tw + (size_t)tr * K.ni);
+        if (single_entry<FIXED>(K, fp, q, wf, it, w)) {
+            const float2 p = __ldg(d2 + (size_t)tr * K.nt + it);
+            acc = fmaf(p.x, 1.f - w, acc);
+            acc = fmaf(p.y, w, acc);
+        }
+    }
+    out[(size_t)blockIdx.y * K.ni + ii] = acc;
+}
+
+// Forward: one CTA per R consecutive traces, the 64-bit fixed-point
+// shared-memory accumulation of spread_kernel (order-independent, so
+// deterministic), then the wavelet epilogue.
+template <bool FIXED, int R>
+__global__ void __launch_bounds__(kSpreadThreads, 2)
+spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ y, const float* __restrict__ h, int L,
+               int nt_pad, int fuse) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad);
+    float* hs = ftr + nt_pad;
+    const int tid = threadIdx.x;
+    const int nt = K.nt;
+    const int nsnr = K.ns * K.nr;
+    const int tr0 = blockIdx.x * R;
+    if (tr0 >= nsnr) return;
+    const int ntr = min(R, nsnr - tr0);
+    for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
+    if (fuse)
+        for (int k = tid; k < L; k += blockDim.x) hs[k] = h[k];
+    // |v (1 - w)| <= 2 |v| on the negative-time path: one bit of headroom
+    const int e = spread_scale_exponent(__uint_as_float(*K.absmax) * (FIXED ? 1.f : 2.f), K.ni);
+    const float S = ldexpf(1.f, e);
+    __syncthreads();
+    for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
+        const float v = __ldg(K.mv + ii) * S;
+        if (v == 0.f) continue;
+        int q[R];
+        float wf[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            q[r] = r < ntr ? __ldcs(K.tq1 + (size_t)(tr0 + r) * K.ni + ii) : -1;
+            wf[r] = (!FIXED && r < ntr) ? __ldcs(K.tw1 + (size_t)(tr0 + r) * K.ni + ii) : 0.f;
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            int it;
+            float w;
+            if (r < ntr && single_entry<FIXED>(K, fp, q[r], wf[r], it, w)) {
+                const float v1 = v * w;
+                const float v0 = v - v1;
+                unsigned long long* a = acc + (size_t)r * nt_pad + it;
+                atomicAdd(a, (unsigned long long)__float2ll_rn(v0));
+                atomicAdd(a + 1, (unsigned long long)__float2ll_rn(v1));
+            }
+        }
+    }
+    __syncthreads();
+    const float invS = ldexpf(1.f, -e);
+    const int c = (L - 1) / 2;
+    for (int r = 0; r < ntr; ++r) {
+        for (int n = tid; n < nt; n += blockDim.x) ftr[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        __syncthreads();
+        float* __restrict__ yrow = y + (size_t)(tr0 + r) * nt;
+        for (int n = tid; n < nt; n += blockDim.x) {
+            float o;
+            if (fuse) {
+                const int kmin = max(0, n + c - (nt - 1));
+                const int kmax = min(L - 1, n + c);
+                o = 0.f;
+                for (int k = kmin; k <= kmax; ++k) o = fmaf(hs[k], ftr[n + c - k], o);
+            } else {
+                o = ftr[n];
+            }
+            __stcs(yrow + n, o);
+        }
+        __syncthreads();
+    }
+}
+
+template <bool FIXED, int R>
+int spread1_launch_r(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse, size_t smem,
+                     int nt_pad, cudaStream_t stream, bool prepare_only) {
+    auto kern = spread1_kernel<FIXED, R>;
+    if (prepare_only) {
+        KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return KGB_OK;
+    }
+    int rc = launch_prepass<false>(K, m, stream);
+    if (rc) return rc;
+    const FixedPoint<true> fp = make_fp<true>(K.frac_bits, K.nt);
+    const int64_t blocks = ((int64_t)K.ns * K.nr + R - 1) / R;
+    kern<<<(unsigned)blocks, kSpreadThreads, smem, stream>>>(K, fp, y, h, L, nt_pad, fuse ? 1 : 0);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+template <bool FIXED>
+int spread1_dispatch_t(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
+                       cudaStream_t stream, bool prep) {
+    const int Lpad = (L + 3) & ~3;
+    const int nt_pad = (K.nt + 3) & ~3;
+    const size_t fixed = (size_t)(nt_pad + Lpad) * sizeof(float);
+    auto need = [&](int r) { return fixed + (size_t)r * nt_pad * 8; };
+    int R = 8;
+    while (R > 1 && need(R) > 110 * 1024) R >>= 1;
+    while (R > 1 && ((int64_t)K.ns * K.nr + R - 1) / R < 2 * num_sms()) R >>= 1;
+    if (need(R) > 220 * 1024)
+        return set_error(KGB_ERR_NOT_IMPLEMENTED, "spread: nt=%d too long for one trace in shared memory", K.nt);
+    if (prep) {  // every shape a later call may choose
+        int rc = KGB_OK;
+        for (int r : {8, 4, 2, 1}) {
+            if (need(r) > 220 * 1024) continue;
+            switch (r) {
+                case 8: rc = spread1_launch_r<FIXED, 8>(K, m, y, h, L, fuse, need(8), nt_pad, stream, true); break;
+                case 4: rc = spread1_launch_r<FIXED, 4>(K, m, y, h, L, fuse, need(4), nt_pad, stream, true); break;
+                case 2: rc = spread1_launch_r<FIXED, 2>(K, m, y, h, L, fuse, need(2), nt_pad, stream, true); break;
+                default: rc = spread1_launch_r<FIXED, 1>(K, m, y, h, L, fuse, need(1), nt_pad, stream, true);
+            }
+            if (rc) return rc;
+        }
+        return KGB_OK;
+    }
+    switch (R) {
+        case 8: return spread1_launch_r<FIXED, 8>(K, m, y, h, L, fuse, need(8), nt_pad, stream, false);
+        case 4: return spread1_launch_r<FIXED, 4>(K, m, y, h, L, fuse, need(4), nt_pad, stream, false);
+        case 2: return spread1_launch_r<FIXED, 2>(K, m, y, h, L, fuse, need(2), nt_pad, stream, false);
+        default: return spread1_launch_r<FIXED, 1>(K, m, y, h, L, fuse, need(1), nt_pad, stream, false);
+    }
+}
+
+__global__ void sum_splits_kernel(const float* __restrict__ partial, float* __restrict__ img, int64_t ni, int nsplit) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += (int64_t)gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        for (int k = 0; k < nsplit; ++k) acc += partial[(size_t)k * ni + i];
+        img[i] = acc;
+    }
+}
+
+template <bool FIXED>
+int gather1_launch_t(const KirchDev& K, const float2* d2, float* img, float* partial, int64_t cap,
+                     cudaStream_t stream) {
+    const FixedPoint<true> fp = make_fp<true>(K.frac_bits, K.nt);
+    const int nsnr = K.ns * K.nr;
+    const int64_t blocks = (K.ni + 255) / 256;
+    // split over traces until two waves of 8 blocks per SM are resident
+    int split = (int)std::max<int64_t>(1, (2 * 8 * (int64_t)num_sms() + blocks - 1) / blocks);
+    split = std::min(split, std::max(1, nsnr / 64));
+    if (partial == nullptr) split = 1;
+    else split = (int)std::min<int64_t>(split, cap / K.ni);
+    split = std::max(split, 1);
+    const int per = (nsnr + split - 1) / split;
+    split = (nsnr + per - 1) / per;
+    float* out = split > 1 ? partial : img;
+    dim3 grid((unsigned)blocks, (unsigned)split);
+    gather1_kernel<FIXED><<<grid, 256, 0, stream>>>(K, fp, d2, out, per);
+    KGB_CUDA_TRY(cudaGetLastError());
+    if (split > 1) {
+        const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
+        sum_splits_kernel<<<nb, 256, 0, stream>>>(partial, img, K.ni, split);
+        KGB_CUDA_TRY(cudaGetLastError());
+    }
+    return KGB_OK;
+}
+
 size_t wavelet_smem(int L, int nt) {
     const int Lpad = (L + 3) & ~3;
     return (size_t)(Lpad + 2 * ((nt + 3) & ~3)) * sizeof(float);
@@ -771,6 +995,10 @@ int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, fl
                   float* partial, int64_t cap, cudaStream_t stream) {
     if (K.ni <= 0 || K.ns <= 0 || K.nr <= 0) return KGB_OK;
     const float2* d2 = reinterpret_cast<const float2*>(d);
+    if (K.tq1) {
+        if (K.tw1) return gather1_launch_t<false>(K, d2, img, partial, cap, stream);
+        return gather1_launch_t<true>(K, d2, img, partial, cap, stream);
+    }
     if (dynamic) {
         if (gate) {
             if (K.nonneg) return gather_launch_t<true, true, true>(K, d2, img, partial, cap, stream);
@@ -786,6 +1014,10 @@ int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, fl
 int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,
                   const float* h, int L, bool fuse_wavelet, cudaStream_t stream) {
     if (K.ns <= 0 || K.nr <= 0 || K.nt <= 0) return KGB_OK;
+    if (K.tq1) {
+        if (K.tw1) return spread1_dispatch_t<false>(K, m, y, h, L, fuse_wavelet, stream, false);
+        return spread1_dispatch_t<true>(K, m, y, h, L, fuse_wavelet, stream, false);
+    }
     return spread_dispatch(K, dynamic, gate, m, y, h, L, fuse_wavelet, stream, false);
 }
 
@@ -798,6 +1030,8 @@ int prepare_kernels(const KirchDev& K0, int L) {
             for (int gate = 0; gate < 2; ++gate)
                 if ((rc = spread_dispatch(K, dyn, gate, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     }
+    if ((rc = spread1_dispatch_t<true>(K, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
+    if ((rc = spread1_dispatch_t<false>(K, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     const size_t smem = wavelet_smem(L, K.nt);
     if (smem <= 227 * 1024)
         KGB_CUDA_TRY(cudaFuncSetAttribute(wavelet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -31,7 +31,7 @@ __all__ = ["Kirchhoff"]
 
 logger = logging.getLogger(__name__)
 
-_TABLE_ATTRS = ("trav_srcs", "trav_recs", "amp_srcs", "amp_recs", "angle_srcs", "angle_recs",
+_TABLE_ATTRS = ("trav", "trav_srcs", "trav_recs", "amp_srcs", "amp_recs", "angle_srcs", "angle_recs",
                 "vel", "aperture", "angleaperture", "aperturetap", "six", "rix")
 
 
@@ -176,10 +176,6 @@ class Kirchhoff(LinearOperator):
         else:
             raise NotImplementedError("method must be analytic, eikonal or byot")
 
-        if not self.travsrcrec:
-            raise NotImplementedError(
-                "engine='cuda' not implemented for traveltimes provided in one table")
-
         # angles with the vertical (kirchhoff.py:364-393)
         if self.dynamic:
             ni_ = int(np.prod(dims))
@@ -197,6 +193,12 @@ class Kirchhoff(LinearOperator):
                 sgn = np.sign(gs[1]) if ns == nr else np.sign(gr[1])
                 self.angle_recs = (sgn * np.arccos(gr[-1] / np.sqrt(np.sum(gr ** 2, axis=0)))
                                    ).reshape(ni_, nr)
+
+        # single-table traveltimes: index and fraction (kirchhoff.py:395-398);
+        # the device copy is made from `trav` itself (same truncation)
+        if not self.travsrcrec:
+            self.itrav = (np.asarray(self.trav) / self.dt).astype("int32")
+            self.travd = np.asarray(self.trav) / self.dt - self.itrav
 
         # wavelet (kirchhoff.py:395-409)
         if wavfilter:
@@ -258,7 +260,13 @@ class Kirchhoff(LinearOperator):
             return
         L = _native.lib()
         f64 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64))  # noqa: E731
-        if {"trav_srcs", "trav_recs"} & self._dirty:
+        if not getattr(self, "travsrcrec", True):
+            if "trav" in self._dirty:
+                tt = f64(self.trav)
+                if tt.size != self.ni * self.nsnr:
+                    raise ValueError("traveltime table must be (ni, ns*nr)")
+                _native.check(L.kgb_kirchhoff_set_traveltime_table(self._h, _native.dptr(tt)))
+        elif {"trav_srcs", "trav_recs"} & self._dirty:
             ts, tr = f64(self.trav_srcs), f64(self.trav_recs)
             if ts.size != self.ni * self.ns or tr.size != self.ni * self.nr:
                 raise ValueError("traveltime tables must be (ni, ns) and (ni, nr)")

@@ -239,6 +239,27 @@ def main():
                         iterates=np.array(its))
     print("wrote solvers_precond")
 
+    # 12) single traveltime table: mode='byot' with trav of shape (ni, ns*nr)
+    # (kirchhoff.py:396-398, 684-725); a second table shifted so that some
+    # times are negative (itrav truncates toward zero: -1 < t/dt < 0 -> 0)
+    rng2 = np.random.default_rng(123)
+    ts, tr, _, _, _, _ = Kirchhoff._traveltime_table(z, x, s2d, r2d, v0, mode="analytic")
+    tt = (ts[:, :, None] + tr[:, None, :]).reshape(ts.shape[0], -1)
+    tt = tt * (1.0 + 0.2 * np.cos(np.arange(tt.shape[0]) / 5.0))[:, None]
+    for name, table in (("k2d_single", tt), ("k2d_single_neg", tt - 0.5 * tt.mean())):
+        K = Kirchhoff(z, x, t, s2d, r2d, v0, wav, wavc, mode="byot", trav=table, engine="numpy")
+        xin = rng2.standard_normal(K.ni)
+        din = rng2.standard_normal(K.shape[0])
+        spread = K._kirch_matvec(xin, np.zeros((K.nsnr, K.nt)), K.nsnr, K.nt, K.ni, K.itrav, K.travd)
+        gather = K._kirch_rmatvec(din.reshape(K.nsnr, K.nt), np.zeros(K.ni), K.nsnr, K.nt, K.ni, K.itrav,
+                                  K.travd)
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), trav_table=table, m_in=xin, d_in=din,
+                            fwd=np.asarray(K @ xin), adj=np.asarray(K.H @ din), spread=spread, gather=gather,
+                            itrav=K.itrav, travd=K.travd, wav=np.asarray(K.wav), wavc=wavc, ns=K.ns, nr=K.nr,
+                            nt=K.nt, ni=int(K.ni), dt=float(K.dt), nz=K.nz, dynamic=False, vel_scalar=v0,
+                            **geom2d())
+        print("wrote", name)
+
 
 if __name__ == "__main__":
     sys.exit(main())

@@ -127,3 +127,27 @@ def test_c_oracle_matches_reference(name):
     assert rel(C.gather(g["d_in"]), g["gather"]) < max(tol, 1e-12)
     assert rel(C.matvec(g["m_in"]), g["fwd"]) < tol
     assert rel(C.rmatvec(g["d_in"]), g["adj"]) < tol
+
+
+@pytest.mark.parametrize("name", ["k2d_single", "k2d_single_neg"])
+def test_single_table_oracle_matches_reference(name):
+    """mode='byot' with one (ni, ns*nr) table: index/fraction, spreading,
+    gathering and the full operator with the wavelet."""
+    from oracle.kirchhoff_oracle import (conv_same, pad_wavelet, single_table_index, trav_matvec,
+                                         trav_rmatvec)
+
+    g = load(name)
+    nsnr, nt, ni = int(g["ns"]) * int(g["nr"]), int(g["nt"]), int(g["ni"])
+    it, w = single_table_index(g["trav_table"], float(g["dt"]))
+    assert np.array_equal(it, g["itrav"])
+    np.testing.assert_allclose(w, g["travd"], rtol=0, atol=1e-12)
+    if name.endswith("neg"):
+        assert np.any((it == 0) & (w < 0)), "negative-time quirk not exercised"
+    y = trav_matvec(g["m_in"], nsnr, nt, ni, it, w)
+    assert rel(y, g["spread"]) < 1e-12
+    img = trav_rmatvec(g["d_in"], nsnr, nt, ni, it, w)
+    assert rel(img, g["gather"]) < 1e-12
+    h = pad_wavelet(g["wav"], int(g["wavc"]))
+    assert rel(conv_same(y, h).ravel(), g["fwd"]) < 1e-10
+    dc = conv_same(np.asarray(g["d_in"]).reshape(nsnr, nt), h[::-1].copy())
+    assert rel(trav_rmatvec(dc, nsnr, nt, ni, it, w), g["adj"]) < 1e-10
