@@ -503,6 +503,113 @@ def run_batch(args):
     }))
 
 
+def run_single(args):
+    """Single traveltime table workload (mode='byot' with trav of shape
+    (ni, ns*nr)): the 300 x 800 grid at 5 m with v(z) = 1500 + 0.5 z,
+    64 sources x 100 receivers at the surface (6400 traces), nt = 1501 at
+    2 ms, 15 Hz Ricker; a 6.1 GB table in HBM.  A step is one forward and one
+    adjoint; value = compulsory GB/s (4 bytes per table entry, model and data
+    once per application).  The table is read once per application, so this
+    is the HBM-bound mode of the operator."""
+    import torch
+
+    from oracle.kirchhoff_oracle import conv_same, pad_wavelet, single_table_index, trav_matvec
+    from pylops_gb300.utils.wavelets import ricker
+    from pylops_gb300.waveeqprocessing import Kirchhoff
+
+    nz, nx, nt, dt = 300, 800, 1501, 0.002
+    ns, nr = 64, args.single_receivers
+    # the float64 host table is 8 * ni * ns * nr bytes: keep it within a third of free memory
+    try:
+        free = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_AVPHYS_PAGES")
+    except (ValueError, OSError):
+        free = 0
+    while free and nr > 8 and 3 * 8 * nx * nz * ns * nr > free:
+        nr //= 2
+    z, x, t = np.arange(nz) * 5.0, np.arange(nx) * 5.0, np.arange(nt) * dt
+    srcs = np.vstack((np.linspace(x[0], x[-1], ns), np.zeros(ns)))
+    recs = np.vstack((np.linspace(x[0], x[-1], nr), np.zeros(nr)))
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    v = (1500.0 + 0.5 * Z).ravel()
+    t0 = time.perf_counter()
+    ts = np.sqrt((X.ravel()[:, None] - srcs[0][None]) ** 2 + Z.ravel()[:, None] ** 2) / v[:, None]
+    tr = np.sqrt((X.ravel()[:, None] - recs[0][None]) ** 2 + Z.ravel()[:, None] ** 2) / v[:, None]
+    table = (ts[:, :, None] + tr[:, None, :]).reshape(nx * nz, ns * nr)
+    wav, _, wc = ricker(t[:41], f0=15)
+    K = Kirchhoff(z, x, t, srcs, recs, 1500.0, wav, wc, mode="byot", trav=table, engine="cuda", dtype="float32")
+    K.native_handle
+    t_setup = time.perf_counter() - t0
+    g = torch.Generator(device="cuda").manual_seed(0)
+    m = torch.randn(K.ni, device="cuda", generator=g)
+    d = torch.randn(K.shape[0], device="cuda", generator=g)
+    y = torch.empty_like(d)
+    img = torch.empty_like(m)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        K.apply_into(m, y)
+        K.apply_into(d, img, adjoint=True)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for a, b, c in ev:
+        a.record(stream)
+        K.apply_into(m, y)
+        b.record(stream)
+        K.apply_into(d, img, adjoint=True)
+        c.record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step = e0.elapsed_time(e1) / 1e3 / args.steps
+    fwd_ms = statistics.median(a.elapsed_time(b) for a, b, _ in ev)
+    adj_ms = statistics.median(b.elapsed_time(c) for _, b, c in ev)
+    B = 2 * (4 * K.ni * K.nsnr + 4 * K.ni + 4 * K.nsnr * K.nt)
+    table_bytes = 4 * K.ni * K.nsnr
+    peaks = _peaks()
+    # the gather (adjoint) streams the table once: its bytes / its time
+    ach = (table_bytes + 4 * K.ni + 8 * K.nsnr * K.nt) / (adj_ms / 1e3) / 1e9
+    # end to end with host buffers
+    mh, dh = m.cpu().numpy(), d.cpu().numpy()
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        _ = K @ mh
+        _ = K.H @ dh
+    e2e = (time.perf_counter() - te) / args.steps
+    line = {
+        "metric": "Kirchhoff single-table fwd+adj GB/s vs HBM peak", "value": round(B / step / 1e9, 2),
+        "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(step * 1e3, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "single_table_2d_300x800_64x%d_nt1501" % nr, "table_gb": round(table_bytes / 1e9, 3),
+                   "l2": "table larger than L2", "setup_s": round(t_setup, 1)},
+        "kernel_ms": {"forward": round(fwd_ms, 3), "adjoint": round(adj_ms, 3)},
+        "hbm_fraction": round(B / step / 1e9 / peaks["hbm_gbs"], 4),
+        "roofline": {"bound": "hbm", "kernel": "gather1 (adjoint)", "achieved": round(ach, 1),
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(ach / peaks["hbm_gbs"], 4),
+                     "traffic": None},
+        "e2e": {"value": round(B / e2e / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * (K.ni + K.shape[0]),
+                "d2h_bytes_per_step": 4 * (K.ni + K.shape[0])},
+        "gpu_launches": args.steps * (K.info()["kernels_forward"] + K.info()["kernels_adjoint"]),
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        ntr = 32
+        it, w = single_table_index(table[:, :ntr], dt)
+        tc = time.perf_counter()
+        trav_matvec(mh.astype(np.float64), ntr, nt, K.ni, it, w)
+        tcs = time.perf_counter() - tc
+        per_step = 2 * tcs * K.nsnr / ntr
+        line["cpu_baseline"] = {"value": round(B / per_step / 1e9, 4), "unit": "GB/s", "cores": 1, "kind": "port",
+                                "sample": f"NumPy oracle forward spreading of {ntr} of {K.nsnr} traces, "
+                                          f"{tcs:.1f} s, x2 for the adjoint, scaled to one step"}
+    print(json.dumps(line))
+
+
 def run_lsm(args):
     """Learned-preconditioned LSM workload: 2-D dynamic eikonal Kirchhoff,
     v(z) = 1500 + 0.6 z on 256 x 512 at 5 m, 48 sources, 256 receivers,
@@ -578,9 +685,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single"],
                     help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems; "
-                         "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models)")
+                         "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models); "
+                         "single: the single-traveltime-table (HBM-streaming) mode")
+    ap.add_argument("--single-receivers", type=int, default=100)
     ap.add_argument("--lsm-train", type=int, default=4096)
     ap.add_argument("--lsm-steps", type=int, default=3000)
     ap.add_argument("--batch-problems", type=int, default=256)
@@ -594,6 +703,8 @@ def main():
         run_batch(args)
     elif args.workload == "lsm":
         run_lsm(args)
+    elif args.workload == "single":
+        run_single(args)
     else:
         run_gpu(args)
 

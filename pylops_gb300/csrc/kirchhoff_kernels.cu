@@ -354,6 +354,75 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     }
 }
 
+// Add one warp's contributions (lane: v0 at bin it, v1 at it + 1, if
+// contrib) to a trace in shared memory, in a fixed order:
+//  * bins strictly increasing over a run of consecutive lanes: straight
+//    adds, bin it in one pass and it + 1 in the next;
+//  * bins non-decreasing: lanes sharing a bin are contiguous; a segmented
+//    warp scan (5 shuffle steps) sums each segment and its last lane adds;
+//  * otherwise lanes sharing a bin are found with __match_any_sync and
+//    summed by the bin's lowest lane in lane order.
+__device__ __forceinline__ void warp_bin_add(float* trc, bool contrib, int it, float v0, float v1, int lane) {
+    const unsigned cm = __ballot_sync(FULL, contrib);
+    if (cm == 0u) return;
+    if (!contrib) it = 0;
+    const unsigned lower = (1u << lane) - 1u;
+    const int first = __ffs(cm) - 1;
+    const int last = 31 - __clz(cm);
+    const unsigned sh = cm >> first;
+    const bool run = (sh & (sh + 1u)) == 0u;
+    const int prev_it = __shfl_up_sync(FULL, it, 1);
+    const bool strict = !contrib || lane == first || it > prev_it;
+    const bool nondec = !contrib || lane == first || it >= prev_it;
+    if (run && __all_sync(FULL, strict)) {
+        if (contrib) trc[it] += v0;
+        __syncwarp();
+        if (contrib) trc[it + 1] += v1;
+        __syncwarp();
+    } else if (run && __all_sync(FULL, nondec)) {
+        const bool head = contrib && (lane == first || it != prev_it);
+        const unsigned hm = __ballot_sync(FULL, head);
+        const int start = 31 - __clz(hm & (lower | (1u << lane)));
+        float s0 = v0, s1 = v1;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const float a0 = __shfl_up_sync(FULL, s0, off);
+            const float a1 = __shfl_up_sync(FULL, s1, off);
+            if (contrib && lane - off >= start) {
+                s0 += a0;
+                s1 += a1;
+            }
+        }
+        const int next_it = __shfl_down_sync(FULL, it, 1);
+        const bool tail = contrib && (lane == last || next_it != it);
+        if (tail) trc[it] += s0;
+        __syncwarp();
+        if (tail) trc[it + 1] += s1;
+        __syncwarp();
+    } else {
+        const unsigned key = contrib ? (unsigned)it : (0x80000000u | (unsigned)lane);
+        const unsigned peers = __match_any_sync(FULL, key);
+        unsigned rest = peers & (peers - 1u);
+        const int maxc = __reduce_max_sync(FULL, (unsigned)__popc(rest));
+        float s0 = v0, s1 = v1;
+        for (int k = 0; k < maxc; ++k) {
+            const int src = rest ? (__ffs(rest) - 1) : lane;
+            const float b0 = __shfl_sync(FULL, v0, src);
+            const float b1 = __shfl_sync(FULL, v1, src);
+            if (rest) {
+                s0 += b0;
+                s1 += b1;
+                rest &= rest - 1u;
+            }
+        }
+        const bool lead = contrib && ((peers & lower) == 0u);
+        if (lead) trc[it] += s0;
+        __syncwarp();
+        if (lead) trc[it + 1] += s1;
+        __syncwarp();
+    }
+}
+
 // Spreading, warp-binned variant: each warp owns RT traces (one source, RT
 // receivers) in shared memory and walks the image one depth column at a time,
 // 32 consecutive depths per step, lane = depth.  Down a column the time
@@ -393,7 +462,6 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
 #pragma unroll
     for (int r = 0; r < RT; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
     const int64_t ncol = K.ni / nz;
-    const unsigned lower = (1u << lane) - 1u;
     for (int64_t col = 0; col < ncol; ++col) {
         for (int iz0 = 0; iz0 < nz; iz0 += 32) {
             const int iz = iz0 + lane;
@@ -429,50 +497,13 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
                 }
                 const bool tv = inb && val != 0.f && fp.valid(s);
                 const int it = tv ? fp.index(s) : 0;
-                const bool contrib = tv && val != 0.f;
-                const unsigned cm = __ballot_sync(FULL, contrib);
-                if (cm == 0u) continue;
                 float v0 = 0.f, v1 = 0.f;
-                if (contrib) {
+                if (tv) {
                     const float w = fp.frac(s, it);
                     v1 = val * w;
                     v0 = val - v1;
                 }
-                float* tr = traces + r * nt_pad;
-                // the contributing lanes form one run of consecutive lanes with
-                // strictly increasing bins?
-                const int first = __ffs(cm) - 1;
-                const unsigned sh = cm >> first;
-                const bool run = (sh & (sh + 1u)) == 0u;
-                const int prev_it = __shfl_up_sync(FULL, it, 1);
-                const bool ok = !contrib || lane == first || it > prev_it;
-                if (run && __all_sync(FULL, ok)) {
-                    if (contrib) tr[it] += v0;
-                    __syncwarp();
-                    if (contrib) tr[it + 1] += v1;
-                    __syncwarp();
-                } else {
-                    const unsigned key = contrib ? (unsigned)it : (0x80000000u | (unsigned)lane);
-                    const unsigned peers = __match_any_sync(FULL, key);
-                    unsigned rest = peers & (peers - 1u);
-                    const int maxc = __reduce_max_sync(FULL, (unsigned)__popc(rest));
-                    float s0 = v0, s1 = v1;
-                    for (int k = 0; k < maxc; ++k) {
-                        const int src = rest ? (__ffs(rest) - 1) : lane;
-                        const float a0 = __shfl_sync(FULL, v0, src);
-                        const float a1 = __shfl_sync(FULL, v1, src);
-                        if (rest) {
-                            s0 += a0;
-                            s1 += a1;
-                            rest &= rest - 1u;
-                        }
-                    }
-                    const bool lead = contrib && ((peers & lower) == 0u);
-                    if (lead) tr[it] += s0;
-                    __syncwarp();
-                    if (lead) tr[it + 1] += s1;
-                    __syncwarp();
-                }
+                warp_bin_add(traces + r * nt_pad, tv, it, v0, v1, lane);
             }
         }
     }
@@ -813,6 +844,155 @@ gather1_kernel(const KirchDev K, const FixedPoint<true> fp, const float2* __rest
     out[(size_t)blockIdx.y * K.ni + ii] = acc;
 }
 
+// Adjoint, vector form (ni % 4 == 0): one thread per 4 consecutive image
+// points, one 16-byte table load per trace, the next 4 traces' entries
+// loaded while the current ones are used.  Same per-point summation order
+// as gather1_kernel.
+template <bool FIXED>
+__device__ __forceinline__ void gather1_accumulate(const KirchDev& K, const FixedPoint<true>& fp,
+                                                   const float2* __restrict__ drow, int q, float wf, float& acc) {
+    int it;
+    float w;
+    if (single_entry<FIXED>(K, fp, q, wf, it, w)) {
+        const float2 p = __ldg(drow + it);
+        acc = fmaf(p.x, 1.f - w, acc);
+        acc = fmaf(p.y, w, acc);
+    }
+}
+
+template <bool FIXED>
+__global__ void __launch_bounds__(256)
+gather1_vec_kernel(const KirchDev K, const FixedPoint<true> fp, const float2* __restrict__ d2, float* __restrict__ out,
+                   int tr_per_split) {
+    const int64_t i4 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i4 * 4 >= K.ni) return;
+    const int nsnr = K.ns * K.nr;
+    const int t0 = blockIdx.y * tr_per_split;
+    const int t1 = min(nsnr, t0 + tr_per_split);
+    const int4* __restrict__ tq = reinterpret_cast<const int4*>(K.tq1) + i4;
+    const float4* __restrict__ tw = FIXED ? nullptr : reinterpret_cast<const float4*>(K.tw1) + i4;
+    const int64_t rs = K.ni / 4;  // row stride in 16-byte units
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    constexpr int U = 4;
+    int4 qn[U];
+    float4 wn[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const bool ok = t0 + u < t1;
+        qn[u] = ok ? __ldcs(tq + (size_t)(t0 + u) * rs) : make_int4(-1, -1, -1, -1);
+        wn[u] = (!FIXED && ok) ? __ldcs(tw + (size_t)(t0 + u) * rs) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int tr = t0; tr < t1; tr += U) {
+        int4 q[U];
+        float4 wf[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            q[u] = qn[u];
+            wf[u] = wn[u];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool ok = tr + U + u < t1;
+            qn[u] = ok ? __ldcs(tq + (size_t)(tr + U + u) * rs) : make_int4(-1, -1, -1, -1);
+            wn[u] = (!FIXED && ok) ? __ldcs(tw + (size_t)(tr + U + u) * rs) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (tr + u >= t1) break;
+            const float2* drow = d2 + (size_t)(tr + u) * K.nt;
+            gather1_accumulate<FIXED>(K, fp, drow, q[u].x, wf[u].x, a0);
+            gather1_accumulate<FIXED>(K, fp, drow, q[u].y, wf[u].y, a1);
+            gather1_accumulate<FIXED>(K, fp, drow, q[u].z, wf[u].z, a2);
+            gather1_accumulate<FIXED>(K, fp, drow, q[u].w, wf[u].w, a3);
+        }
+    }
+    reinterpret_cast<float4*>(out + (size_t)blockIdx.y * K.ni)[i4] = make_float4(a0, a1, a2, a3);
+}
+
+// Forward, warp-binned: one warp per trace walking the image one depth
+// column at a time, 32 consecutive depths per step (lane = depth).  When
+// the contributing lanes' time bins increase strictly (the usual case down a
+// column) they add straight into the warp's shared-memory trace, bin it in
+// one pass and it + 1 in the next; otherwise lanes sharing a bin are summed
+// by the bin's lowest lane in lane order (__match_any_sync).  No atomics,
+// fixed order: deterministic.  Each table entry is read once.
+template <bool FIXED>
+__global__ void __launch_bounds__(256)
+spread1_binned_kernel(const KirchDev K, const FixedPoint<true> fp, const float* __restrict__ m, float* __restrict__ y,
+                      const float* __restrict__ h, int L, int Lpad, int nt_pad, int fuse) {
+    extern __shared__ __align__(16) float smem_f[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    float* hs = smem_f;
+    float* trc = smem_f + Lpad + (size_t)warp * nt_pad;
+    if (fuse)
+        for (int k = threadIdx.x; k < L; k += blockDim.x) hs[k] = h[k];
+    __syncthreads();
+    const int tr = blockIdx.x * nw + warp;
+    if (tr >= K.ns * K.nr) return;
+    const int nt = K.nt, nz = K.nz;
+    for (int k = lane; k < nt_pad; k += 32) trc[k] = 0.f;
+    __syncwarp();
+    const int64_t ncol = K.ni / nz;
+    const int cpc = (nz + 31) / 32;  // 32-depth chunks per column
+    const int64_t nchunk = ncol * cpc;
+    const int32_t* __restrict__ tq = K.tq1 + (size_t)tr * K.ni;
+    const float* __restrict__ tw = FIXED ? nullptr : K.tw1 + (size_t)tr * K.ni;
+    // U chunks per step, all their loads issued before any is used
+    constexpr int U = 4;
+    int64_t colg = 0;  // (column, chunk) of the group's first chunk, advanced without divisions
+    int jg = 0;
+    for (int64_t c0 = 0; c0 < nchunk; c0 += U) {
+        float vv[U], ww[U];
+        int qq[U];
+        int64_t col = colg;
+        int j = jg;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int iz = j * 32 + lane;
+            const bool inb = c0 + u < nchunk && iz < nz;
+            const int64_t ii = col * nz + iz;
+            vv[u] = inb ? __ldg(m + ii) : 0.f;
+            qq[u] = inb ? __ldcs(tq + ii) : -1;
+            ww[u] = (!FIXED && inb) ? __ldcs(tw + ii) : 0.f;
+            if (++j == cpc) {
+                j = 0;
+                ++col;
+            }
+        }
+        colg = col;
+        jg = j;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const float v = vv[u];
+            int it = 0;
+            float w = 0.f;
+            const bool contrib = v != 0.f && single_entry<FIXED>(K, fp, qq[u], ww[u], it, w);
+            float v0 = 0.f, v1 = 0.f;
+            if (contrib) {
+                v1 = v * w;
+                v0 = v - v1;
+            }
+            warp_bin_add(trc, contrib, it, v0, v1, lane);
+        }
+    }
+    const int c = (L - 1) / 2;
+    float* __restrict__ yrow = y + (size_t)tr * nt;
+    for (int n = lane; n < nt; n += 32) {
+        float o;
+        if (fuse) {
+            const int kmin = max(0, n + c - (nt - 1));
+            const int kmax = min(L - 1, n + c);
+            o = 0.f;
+            for (int k = kmin; k <= kmax; ++k) o = fmaf(hs[k], trc[n + c - k], o);
+        } else {
+            o = trc[n];
+        }
+        __stcs(yrow + n, o);
+    }
+}
+
 // Forward: one CTA per R consecutive traces, the 64-bit fixed-point
 // shared-memory accumulation of spread_kernel (order-independent, so
 // deterministic), then the wavelet epilogue.
@@ -901,10 +1081,38 @@ int spread1_launch_r(const KirchDev& K, const float* m, float* y, const float* h
 }
 
 template <bool FIXED>
+int spread1_binned_launch(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
+                          cudaStream_t stream, bool prepare_only) {
+    auto kern = spread1_binned_kernel<FIXED>;
+    const int Lpad = (L + 3) & ~3;
+    const int nt_pad = (K.nt + 3) & ~3;
+    const int warps = 8;
+    const size_t smem = (size_t)(Lpad + (size_t)warps * nt_pad) * sizeof(float);
+    if (smem > 227 * 1024)
+        return set_error(KGB_ERR_NOT_IMPLEMENTED, "spread: nt=%d too long for the binned variant", K.nt);
+    if (prepare_only) {
+        KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        return KGB_OK;
+    }
+    const FixedPoint<true> fp = make_fp<true>(K.frac_bits, K.nt);
+    const int64_t blocks = ((int64_t)K.ns * K.nr + warps - 1) / warps;
+    kern<<<(unsigned)blocks, warps * 32, smem, stream>>>(K, fp, m, y, h, L, Lpad, nt_pad, fuse ? 1 : 0);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+template <bool FIXED>
 int spread1_dispatch_t(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                        cudaStream_t stream, bool prep) {
     const int Lpad = (L + 3) & ~3;
     const int nt_pad = (K.nt + 3) & ~3;
+    const bool binned_fits = (size_t)(Lpad + 8 * (size_t)nt_pad) * 4 <= 227 * 1024;
+    if (prep && binned_fits) {
+        int rc = spread1_binned_launch<FIXED>(K, m, y, h, L, fuse, stream, true);
+        if (rc) return rc;
+    } else if (!prep && K.spread_variant != 0 && binned_fits) {
+        return spread1_binned_launch<FIXED>(K, m, y, h, L, fuse, stream, false);
+    }
     const size_t fixed = (size_t)(nt_pad + Lpad) * sizeof(float);
     auto need = [&](int r) { return fixed + (size_t)r * nt_pad * 8; };
     int R = 8;
@@ -947,7 +1155,11 @@ int gather1_launch_t(const KirchDev& K, const float2* d2, float* img, float* par
                      cudaStream_t stream) {
     const FixedPoint<true> fp = make_fp<true>(K.frac_bits, K.nt);
     const int nsnr = K.ns * K.nr;
-    const int64_t blocks = (K.ni + 255) / 256;
+    // 4 points per thread: 16-byte table rows and float4 stores of the result
+    // (the partial images are cudaMalloc'ed; the caller's image must be
+    // 16-byte aligned for the unsplit case, else the scalar kernel runs)
+    bool vec = K.ni % 4 == 0;
+    const int64_t blocks = vec ? (K.ni / 4 + 255) / 256 : (K.ni + 255) / 256;
     // split over traces until two waves of 8 blocks per SM are resident
     int split = (int)std::max<int64_t>(1, (2 * 8 * (int64_t)num_sms() + blocks - 1) / blocks);
     split = std::min(split, std::max(1, nsnr / 64));
@@ -957,8 +1169,10 @@ int gather1_launch_t(const KirchDev& K, const float2* d2, float* img, float* par
     const int per = (nsnr + split - 1) / split;
     split = (nsnr + per - 1) / per;
     float* out = split > 1 ? partial : img;
-    dim3 grid((unsigned)blocks, (unsigned)split);
-    gather1_kernel<FIXED><<<grid, 256, 0, stream>>>(K, fp, d2, out, per);
+    if (((uintptr_t)out & 15) != 0) vec = false;
+    dim3 grid((unsigned)(vec ? blocks : (K.ni + 255) / 256), (unsigned)split);
+    if (vec) gather1_vec_kernel<FIXED><<<grid, 256, 0, stream>>>(K, fp, d2, out, per);
+    else gather1_kernel<FIXED><<<grid, 256, 0, stream>>>(K, fp, d2, out, per);
     KGB_CUDA_TRY(cudaGetLastError());
     if (split > 1) {
         const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());

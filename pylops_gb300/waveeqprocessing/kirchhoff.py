@@ -194,12 +194,6 @@ class Kirchhoff(LinearOperator):
                 self.angle_recs = (sgn * np.arccos(gr[-1] / np.sqrt(np.sum(gr ** 2, axis=0)))
                                    ).reshape(ni_, nr)
 
-        # single-table traveltimes: index and fraction (kirchhoff.py:395-398);
-        # the device copy is made from `trav` itself (same truncation)
-        if not self.travsrcrec:
-            self.itrav = (np.asarray(self.trav) / self.dt).astype("int32")
-            self.travd = np.asarray(self.trav) / self.dt - self.itrav
-
         # wavelet (kirchhoff.py:395-409)
         if wavfilter:
             self.wav = self._wavelet_reshaping(wav, self.dt, srcs.shape[0], recs.shape[0], self.ndims)
@@ -237,6 +231,21 @@ class Kirchhoff(LinearOperator):
                         else vel * np.ones(int(np.prod(dims))))
         self.cop = _WaveletOperator(self, np.asarray(self.wav), self.wavcenter, dtype)
         self._create_native()
+
+    # single-table traveltimes: index and fraction (kirchhoff.py:395-398),
+    # computed on first access (the device copy is made from `trav` itself,
+    # with the same truncation)
+    @property
+    def itrav(self):
+        if getattr(self, "travsrcrec", True):
+            raise AttributeError("itrav exists for a single traveltime table only")
+        return (np.asarray(self.trav) / self.dt).astype("int32")
+
+    @property
+    def travd(self):
+        if getattr(self, "travsrcrec", True):
+            raise AttributeError("travd exists for a single traveltime table only")
+        return np.asarray(self.trav) / self.dt - self.itrav
 
     # ---------------------------------------------------------------- native
     def __setattr__(self, name, value):

@@ -59,13 +59,15 @@ def test_single_table_dynamic_raises_like_reference():
                   trav=g["trav_table"], dynamic=True, amp=g["trav_table"], engine="cuda")
 
 
-def test_single_table_medium_size_against_oracle():
-    """300 x 200 image, 16 x 64 traces, nt = 700: a 245 MB table."""
+@pytest.mark.parametrize("nx,nz", [(300, 200), (301, 199)])
+def test_single_table_medium_size_against_oracle(nx, nz):
+    """300 x 200 image (an odd-sized one too: the scalar gather), 16 x 64
+    traces, nt = 700: a 245 MB table; both forward variants."""
     from oracle.kirchhoff_oracle import conv_same, pad_wavelet, single_table_index, trav_matvec, trav_rmatvec
     from pylops_gb300.utils.wavelets import ricker
     from pylops_gb300.waveeqprocessing import Kirchhoff
 
-    nz, nx, nt, dt = 200, 300, 700, 0.002
+    nt, dt = 700, 0.002
     z, x, t = np.arange(nz) * 5.0, np.arange(nx) * 5.0, np.arange(nt) * dt
     ns, nr = 16, 64
     srcs = np.vstack((np.linspace(x[0], x[-1], ns), np.zeros(ns)))
@@ -83,6 +85,8 @@ def test_single_table_medium_size_against_oracle():
     it, w = single_table_index(table, dt)
     h = pad_wavelet(wav, wc)
     yo = conv_same(trav_matvec(m, ns * nr, nt, K.ni, it, w), h).ravel()
-    assert rel(K @ m.astype(np.float32), yo) < 1e-5
+    for variant in (0, 1):
+        K.set_spread_variant(variant)
+        assert rel(K @ m.astype(np.float32), yo) < 1e-5, variant
     io = trav_rmatvec(conv_same(d.reshape(ns * nr, nt), h[::-1].copy()), ns * nr, nt, K.ni, it, w)
     assert rel(K.H @ d.astype(np.float32), io) < 1e-5
