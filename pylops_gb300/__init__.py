@@ -10,7 +10,10 @@ from .linearoperator import LinearOperator, aslinearoperator
 from . import utils
 from . import waveeqprocessing
 from . import optimization
+from . import basicoperators
+from .torchoperator import TorchOperator
 
 __version__ = "0.1.0"
 
-__all__ = ["LinearOperator", "aslinearoperator", "utils", "waveeqprocessing", "optimization"]
+__all__ = ["LinearOperator", "aslinearoperator", "utils", "waveeqprocessing", "optimization", "basicoperators",
+           "TorchOperator"]

@@ -59,6 +59,28 @@ class _Conv:
         return (H + 2 * p - self.ks) // self.stride + 1, (W + 2 * p - self.ks) // self.stride + 1
 
 
+class _CountingLib:
+    """The native library with a count of the kernels each entry point
+    launches (two for the split-K GEMM, the row sums and the MSE, one for
+    the others)."""
+
+    _KERNELS = {"kgb_gemm_bf16_tn_splitk": 2, "kgb_unet_rowsum": 2, "kgb_unet_mse": 2}
+
+    def __init__(self, owner):
+        self._owner = owner
+
+    def __getattr__(self, name):
+        fn = getattr(_native.lib(), name)
+        n = self._KERNELS.get(name, 1)
+        owner = self._owner
+
+        def call(*args):
+            owner.launches += n
+            return fn(*args)
+
+        return call
+
+
 class UNet:
     """U-Net of ``levels`` levels and ``base`` channels; weights live on the
     current CUDA device.  ``forward(x)`` maps a float32 batch (B, H, W) to
@@ -114,6 +136,7 @@ class UNet:
         self.adam_m = torch.zeros_like(self.params)
         self.adam_v = torch.zeros_like(self.params)
         self.step_count = 0
+        self.launches = 0  # kernels launched by this network so far
         for c in convs:
             c.Wb = torch.empty((c.cout, c.kpad), dtype=torch.bfloat16, device=dev)
             c.Wt = torch.empty((c.cin, c.kg), dtype=torch.bfloat16, device=dev)
@@ -125,6 +148,9 @@ class UNet:
         self._loss = torch.zeros(1, dtype=torch.float64, device=dev)
 
     # ------------------------------------------------------------ helpers
+    def _lib(self):
+        return _CountingLib(self)
+
     @staticmethod
     def _stream():
         import torch
@@ -144,7 +170,7 @@ class UNet:
         return self.grads[c.b_off:c.b_off + c.cout]
 
     def _refresh_weights(self):
-        L = _native.lib()
+        L = self._lib()
         s = self._stream()
         for c in self.convs:
             _native.check(L.kgb_unet_weights(self._w(c).data_ptr(), c.Wb.data_ptr(), c.Wt.data_ptr(), c.cout, c.cin,
@@ -276,7 +302,7 @@ class UNet:
     # ------------------------------------------------------------ layers
     def _conv_forward(self, i: int, ws, B: int):
         c = self.convs[i]
-        L, s = _native.lib(), self._stream()
+        L, s = self._lib(), self._stream()
         x, li = self._in_of(i, ws)
         lo = ws["lvl"][i]
         (H, W), (Ho, Wo) = ws["hw"][li], ws["hw"][lo]
@@ -296,7 +322,7 @@ class UNet:
         """Weight/bias gradients of conv i from ws['dy'][i]; data gradient
         into dx (float32, input pixels x cin) unless dx is None."""
         c = self.convs[i]
-        L, s = _native.lib(), self._stream()
+        L, s = self._lib(), self._stream()
         x, li = self._in_of(i, ws)
         lo = ws["lvl"][i]
         (H, W), (Ho, Wo) = ws["hw"][li], ws["hw"][lo]
@@ -331,7 +357,7 @@ class UNet:
         B, H, W = x.shape
         xx = x.to(device=self.device, dtype=torch.float32).contiguous()
         ws = self._workspace(B, H, W)
-        L, s = _native.lib(), self._stream()
+        L, s = self._lib(), self._stream()
         if self.normalize:
             _native.check(L.kgb_unet_image_rms(xx.data_ptr(), H * W, B, ws["scale"].data_ptr(), s))
             scale = ws["scale"].data_ptr()
@@ -341,7 +367,7 @@ class UNet:
         return ws, B, H, W
 
     def _forward_all(self, ws, B):
-        L, s = _native.lib(), self._stream()
+        L, s = self._lib(), self._stream()
         for l, (a, b) in enumerate(self.enc):
             self._conv_forward(a, ws, B)
             self._conv_forward(b, ws, B)
@@ -373,7 +399,7 @@ class UNet:
 
     def backward_from(self, ws, B):
         """All parameter gradients from ws['dy'][head] (float32)."""
-        L, s = _native.lib(), self._stream()
+        L, s = self._lib(), self._stream()
         dec_first = self.dec[0][1] if self.levels > 1 else self.enc[0][1]
         self._conv_backward(self.head, ws, B, ws["dy"][dec_first])
         pending = {}
@@ -410,7 +436,7 @@ class UNet:
         ws, B, H, W = self._prepare(x)
         self._forward_all(ws, B)
         tt = t.to(device=self.device, dtype=torch.float32).contiguous()
-        L, s = _native.lib(), self._stream()
+        L, s = self._lib(), self._stream()
         n = B * H * W
         _native.check(L.kgb_unet_mse(ws["y"][self.head].data_ptr(), tt.data_ptr(), ws["dy"][self.head].data_ptr(),
                                      n, self._partials.data_ptr(), self._loss.data_ptr(), s))
@@ -418,7 +444,7 @@ class UNet:
         return self._loss[0]
 
     def adam_step(self, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
-        L, s = _native.lib(), self._stream()
+        L, s = self._lib(), self._stream()
         self.step_count += 1
         _native.check(L.kgb_unet_adam(self.params.data_ptr(), self.grads.data_ptr(), self.adam_m.data_ptr(),
                                       self.adam_v.data_ptr(), self.nparams_padded, lr, b1, b2, eps, self.step_count,

@@ -260,6 +260,30 @@ def main():
                             **geom2d())
         print("wrote", name)
 
+    # 13) preconditioned inversion (cls_leastsquares.py:768-1021): CGLS on Op @ P,
+    # x = P p, on the dynamic operator of case 11 and on a dense matrix
+    from pylops.basicoperators import MatrixMult
+    from pylops.optimization.leastsquares import preconditioned_inversion
+
+    K = Kirchhoff(z, x, t, s2d, r2d, v0, wav, wavc, mode="analytic", dynamic=True,
+                  angleaperture=None, engine="numpy")
+    refl = np.zeros((PAR["nx"], PAR["nz"]))
+    refl[:, PAR["nz"] // 2] = 1
+    refl[:, 3 * PAR["nz"] // 4] = 1
+    d = K @ refl.ravel()
+    p = 1.0 + 0.1 * np.tile(np.arange(PAR["nz"]), PAR["nx"])
+    xk = preconditioned_inversion(K, d, Diagonal(p), engine="pylops", niter=8, tol=1e-10)
+    rng3 = np.random.default_rng(7)
+    A = rng3.standard_normal((40, 25))
+    pa = rng3.uniform(0.5, 2.0, 25)
+    ya = A @ rng3.standard_normal(25)
+    xa_s = preconditioned_inversion(MatrixMult(A), ya, Diagonal(pa), engine="scipy", iter_lim=30)
+    xa_p = preconditioned_inversion(MatrixMult(A), ya, Diagonal(pa), engine="pylops", niter=12, tol=1e-12)
+    np.savez_compressed(os.path.join(OUT, "precond_inversion.npz"), d=d, p=p, xk=xk[0], xk_iit=xk[2],
+                        xk_r1=xk[3], A=A, pa=pa, ya=ya, xa_scipy=xa_s[0], xa_scipy_iit=xa_s[2],
+                        xa_pylops=xa_p[0], xa_pylops_iit=xa_p[2], xa_pylops_r1=xa_p[3])
+    print("wrote precond_inversion")
+
 
 if __name__ == "__main__":
     sys.exit(main())
