@@ -350,7 +350,7 @@ def run_gpu(args):
         "spread_variant": best,
         "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": hbm,
                      "unit": "GB/s", "frac": round(achieved / hbm, 5) if hbm else None,
-                     "traffic": None, "peak_source": "measured" if hbm else "fallback",
+                     "traffic": _traffic(top, WORKLOAD), "peak_source": "measured" if hbm else "fallback",
                      "note": "compulsory bytes / launch time; the kernel is issue/gather bound, not HBM bound"},
         "gpu_launches": args.steps * (K.info()["kernels_forward"] + 1 + K.info()["kernels_adjoint"] - 1),
         "clocks": clk,
@@ -379,6 +379,20 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+
+
+def _traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` on `workload` recorded from an ncu
+    capture in profiles/dram_traffic_per_launch.txt, or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            parts = ln.split()
+            if len(parts) == 3 and not ln.startswith("#") and parts[0] == kernel and parts[1] == workload:
+                return int(parts[2])
+    return None
 
 
 def _peaks():
@@ -610,6 +624,76 @@ def run_single(args):
     print(json.dumps(line))
 
 
+def run_unet(args):
+    """U-Net training throughput: the 4-level, 32-channel BF16 network of the
+    learned preconditioner on batches of 8 images of 512 x 256 (the learned-LSM
+    image size), random inputs and targets.  A step is one training step
+    (forward, MSE, backward, Adam).  value = algorithmic TFLOP/s of the
+    convolutions (forward + weight and data gradients, 2 flops per MAC)."""
+    import torch
+
+    from pylops_gb300.learned.unet import UNet
+
+    B, H, W = 8, 512, 256
+    net = UNet(levels=4, base=32, seed=0)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn(B, H, W, device="cuda", generator=g)
+    t = torch.randn(B, H, W, device="cuda", generator=g)
+    for _ in range(args.warmup):
+        net.train_step(x, t)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler()
+    clocks.start()
+    l0 = net.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        net.train_step(x, t)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = net.launches - l0
+    step = e0.elapsed_time(e1) / 1e3 / args.steps
+    flops = net.flops(H, W, training=True) * B
+    # inference of one image (the solve's use)
+    xi = x[:1]
+    net.forward(xi)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(20):
+        net.forward(xi)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    inf_ms = e0.elapsed_time(e1) / 20
+    # end to end: host batch in, loss out
+    xh, th = x.cpu().numpy(), t.cpu().numpy()
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        xd = torch.from_numpy(xh).pin_memory().to("cuda", non_blocking=True)
+        td = torch.from_numpy(th).pin_memory().to("cuda", non_blocking=True)
+        float(net.train_step(xd, td))
+    e2e = (time.perf_counter() - te) / args.steps
+    peaks = _peaks()
+    peak = peaks.get("bf16_tflops_sustained") or 1700.0
+    ach = flops / step / 1e12
+    print(json.dumps({
+        "metric": "U-Net (learned preconditioner) training TFLOP/s", "value": round(ach, 2), "unit": "TFLOP/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": "unet4x32_train_batch8_512x256", "flops_per_step": flops,
+                   "l2": "activations and unfold buffers larger than L2"},
+        "images_per_s": round(B / step, 1), "inference_ms_per_image": round(inf_ms, 3),
+        "roofline": {"bound": "tensor", "kernel": "training step (tcgen05 GEMMs + unfold kernels)",
+                     "achieved": round(ach, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(ach / peak, 4),
+                     "traffic": None},
+        "e2e": {"value": round(flops / e2e / 1e12, 2), "unit": "TFLOP/s", "h2d_bytes_per_step": 2 * x.numel() * 4,
+                "d2h_bytes_per_step": 8},
+        "gpu_launches": launches, "clocks": clk,
+    }))
+
+
 def run_lsm(args):
     """Learned-preconditioned LSM workload: 2-D dynamic eikonal Kirchhoff,
     v(z) = 1500 + 0.6 z on 256 x 512 at 5 m, 48 sources, 256 receivers,
@@ -685,10 +769,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single", "unet"],
                     help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems; "
                          "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models); "
-                         "single: the single-traveltime-table (HBM-streaming) mode")
+                         "single: the single-traveltime-table (HBM-streaming) mode; unet: U-Net training")
     ap.add_argument("--single-receivers", type=int, default=100)
     ap.add_argument("--lsm-train", type=int, default=4096)
     ap.add_argument("--lsm-steps", type=int, default=3000)
@@ -705,6 +789,8 @@ def main():
         run_lsm(args)
     elif args.workload == "single":
         run_single(args)
+    elif args.workload == "unet":
+        run_unet(args)
     else:
         run_gpu(args)
 
