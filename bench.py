@@ -694,6 +694,78 @@ def run_unet(args):
     }))
 
 
+def run_nsconv(args):
+    """Image-domain Hessian (NonStationaryConvolve2D): a 512 x 256 image (the
+    learned-LSM grid) with 41 x 41 point-spread filters on a 16 x 8 coarse
+    grid.  A step is one forward and one adjoint.  value = image points per
+    second (both directions); the kernels are FMA-bound gathers (each output
+    point reads 41 x 41 inputs from shared memory and interpolates 4 filters)."""
+    import torch
+
+    from oracle.nsconv2d_oracle import nsconv2d
+    from pylops_gb300.signalprocessing import NonStationaryConvolve2D
+
+    nx, nz, hx = 512, 256, 41
+    ihx, ihz = np.arange(16, nx, 32), np.arange(16, nz, 32)
+    rng = np.random.default_rng(0)
+    hs = rng.standard_normal((len(ihx), len(ihz), hx, hx)).astype(np.float32)
+    C = NonStationaryConvolve2D(dims=(nx, nz), hs=hs, ihx=ihx, ihz=ihz, dtype="float32")
+    x = torch.randn(nx * nz, device="cuda")
+    for _ in range(args.warmup):
+        C @ x
+        C.H @ x
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler()
+    clocks.start()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    fw, ad = [], []
+    for _ in range(args.steps):
+        e0.record(stream)
+        C @ x
+        e1.record(stream)
+        C.H @ x
+        e2.record(stream)
+        torch.cuda.synchronize()
+        fw.append(e0.elapsed_time(e1))
+        ad.append(e1.elapsed_time(e2))
+    clk = clocks.stop()
+    step = (statistics.median(fw) + statistics.median(ad)) / 1e3
+    xh = x.cpu().numpy()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        C @ xh
+        C.H @ xh
+    e2e = (time.perf_counter() - te) / args.steps
+    B = 2 * (8 * nx * nz + hs.nbytes)
+    peaks = _peaks()
+    line = {
+        "metric": "NonStationaryConvolve2D fwd+adj image points/s", "value": round(2 * nx * nz / step, 1),
+        "unit": "points/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(step * 1e3, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "nsconv2d_512x256_psf41x41_16x8", "l2": "inputs smaller than L2 (re-read per step)"},
+        "kernel_ms": {"forward": round(statistics.median(fw), 4), "adjoint": round(statistics.median(ad), 4)},
+        "flops_per_step": 2 * 2 * 5 * nx * nz * hx * hx,
+        "roofline": {"bound": "hbm", "kernel": "nsconv2d forward", "achieved": round(B / 2 / (statistics.median(fw) / 1e3) / 1e9, 2),
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(B / 2 / (statistics.median(fw) / 1e3) / 1e9 / peaks["hbm_gbs"], 5), "traffic": None,
+                     "note": "FMA-bound gather; compulsory bytes are tiny"},
+        "e2e": {"value": round(2 * nx * nz / e2e, 1), "unit": "points/s", "h2d_bytes_per_step": 8 * nx * nz,
+                "d2h_bytes_per_step": 8 * nx * nz},
+        "gpu_launches": 2 * args.steps, "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        rows = 8
+        tc = time.perf_counter()
+        nsconv2d(xh.reshape(nx, nz)[:rows + hx], hs[:2], ihx[:2], ihz, adjoint=True)
+        tcs = time.perf_counter() - tc
+        per = tcs / ((rows + hx) * nz)
+        line["cpu_baseline"] = {"value": round(1 / per, 1), "unit": "points/s", "cores": 1, "kind": "port",
+                                "sample": f"float64 NumPy oracle adjoint on {rows + hx} x {nz} points, {tcs:.1f} s"}
+    print(json.dumps(line))
+
+
 def run_lsm(args):
     """Learned-preconditioned LSM workload: 2-D dynamic eikonal Kirchhoff,
     v(z) = 1500 + 0.6 z on 256 x 512 at 5 m, 48 sources, 256 receivers,
@@ -769,10 +841,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single", "unet"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single", "unet", "nsconv"],
                     help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems; "
                          "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models); "
-                         "single: the single-traveltime-table (HBM-streaming) mode; unet: U-Net training")
+                         "single: the single-traveltime-table (HBM-streaming) mode; unet: U-Net training; "
+                         "nsconv: the non-stationary convolution (image-domain Hessian)")
     ap.add_argument("--single-receivers", type=int, default=100)
     ap.add_argument("--lsm-train", type=int, default=4096)
     ap.add_argument("--lsm-steps", type=int, default=3000)
@@ -791,6 +864,8 @@ def main():
         run_single(args)
     elif args.workload == "unet":
         run_unet(args)
+    elif args.workload == "nsconv":
+        run_nsconv(args)
     else:
         run_gpu(args)
 

@@ -293,6 +293,20 @@ int kgb_unet_mse(const float* y, const float* t, float* grad, int64_t n, double*
 int kgb_unet_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,
                   int step, void* stream);
 
+/* ---- 2-D non-stationary convolution (image-domain Hessian with PSFs) ----
+ * x, y: (nx, nz) float32 device arrays (z fastest); hs: (nhx, nhz, hx, hz)
+ * float32 device filters on the coarse grid (ohx + k dhx, ohz + l dhz),
+ * hx and hz odd.  adjoint = 0: forward (the filter of each input point
+ * spread around it), 1: adjoint.  Bilinear interpolation of the four
+ * neighbouring filters, edge filters with weights 1/2 outside the coarse
+ * grid.  Both directions are gathers (deterministic, no atomics); y is
+ * overwritten.
+ * Replaces: NonStationaryConvolve2D._matvec_rmatvec and its numba-CUDA
+ * kernel (signalprocessing/nonstatconvolve2d.py:177-300,
+ * _nonstatconvolve2d_cuda.py:6-111). */
+int kgb_nsconv2d_apply(const float* x_dev, float* y_dev, const float* hs_dev, int nx, int nz, int nhx, int nhz,
+                       int hx, int hz, double ohx, double ohz, double dhx, double dhz, int adjoint, void* stream);
+
 /* ---- table builder ------------------------------------------------------
  * First-arrival traveltimes (and, if dist_out != NULL, distances) from npts
  * point sources by fast marching on a regular grid of ndim (2 or 3) axes

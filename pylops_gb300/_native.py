@@ -61,6 +61,7 @@ _SIGNATURES = {
     "kgb_dot_f64": ([c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
     "kgb_solver_create": ([ctypes.POINTER(c_vp), c_vp, c_int], c_int),
     "kgb_solver_destroy": ([c_vp], c_int),
+    "kgb_nsconv2d_apply": ([c_vp, c_vp, c_vp] + [c_int] * 6 + [c_dbl] * 4 + [c_int, c_vp], c_int),
     "kgb_lincomb_f32": ([c_vp, c_vp, c_dbl, c_vp, c_vp, c_int, c_i64, c_vp], c_int),
     "kgb_solver_set_diagonal": ([c_vp, c_vp], c_int),
     "kgb_solver_setup": ([c_vp, c_vp, c_vp, c_dp, c_int, c_vp], c_int),

@@ -284,6 +284,22 @@ def main():
                         xa_pylops=xa_p[0], xa_pylops_iit=xa_p[2], xa_pylops_r1=xa_p[3])
     print("wrote precond_inversion")
 
+    # 14) 2-D non-stationary convolution (signalprocessing/nonstatconvolve2d.py),
+    # filters on a coarse grid that leaves image points outside it on every side
+    from pylops.signalprocessing import NonStationaryConvolve2D
+
+    rng4 = np.random.default_rng(11)
+    nxc, nzc = 60, 80
+    ihx = np.arange(5, 55, 12)
+    ihz = np.arange(3, 77, 14)
+    hsc = rng4.standard_normal((len(ihx), len(ihz), 9, 11))
+    C = NonStationaryConvolve2D(dims=(nxc, nzc), hs=hsc, ihx=ihx, ihz=ihz, engine="numpy")
+    xc = rng4.standard_normal((nxc, nzc))
+    yc = rng4.standard_normal((nxc, nzc))
+    np.savez_compressed(os.path.join(OUT, "nsconv2d.npz"), hs=hsc, ihx=ihx, ihz=ihz, x_in=xc, y_in=yc,
+                        fwd=(C @ xc.ravel()).reshape(nxc, nzc), adj=(C.H @ yc.ravel()).reshape(nxc, nzc))
+    print("wrote nsconv2d")
+
 
 if __name__ == "__main__":
     sys.exit(main())

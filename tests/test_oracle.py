@@ -151,3 +151,11 @@ def test_single_table_oracle_matches_reference(name):
     assert rel(conv_same(y, h).ravel(), g["fwd"]) < 1e-10
     dc = conv_same(np.asarray(g["d_in"]).reshape(nsnr, nt), h[::-1].copy())
     assert rel(trav_rmatvec(dc, nsnr, nt, ni, it, w), g["adj"]) < 1e-10
+
+
+def test_nsconv2d_oracle_matches_reference():
+    from oracle.nsconv2d_oracle import nsconv2d
+
+    g = load("nsconv2d")
+    assert rel(nsconv2d(g["x_in"], g["hs"], g["ihx"], g["ihz"]), g["fwd"]) < 1e-12
+    assert rel(nsconv2d(g["y_in"], g["hs"], g["ihx"], g["ihz"], adjoint=True), g["adj"]) < 1e-12
