@@ -780,7 +780,7 @@ def run_lsm(args):
     clocks = ClockSampler()
     clocks.start()
     out, ctx = experiment.run(n_train=args.lsm_train, n_test=args.steps, steps=args.lsm_steps, batch=8,
-                              niter=600, variants=("plain", "warm", "learned"),
+                              niter=600, variants=("plain", "warm", "learned", "psf"),
                               log=lambda *a: print(*a, file=sys.stderr, flush=True), return_objects=True)
     clk = clocks.stop()
     op, tests = ctx["op"], ctx["tests"]
@@ -807,6 +807,7 @@ def run_lsm(args):
                    "train_steps": args.lsm_steps, "batch": 8, "held_out_models": args.steps, "tol": 1e-2,
                    "l2": "operator tables (478 MB) larger than L2"},
         "plain_lsqr": v["plain"], "warm_start_only": v["warm"], "learned": v["learned"],
+        "psf_image_domain_warm_start": v["psf"],
         "speedup_vs_plain_median": round(v["learned"]["speedup_vs_plain_median"], 3),
         "train": {k: out.get(k) for k in ("pairs_seconds", "train_seconds", "train_loss_first", "train_loss_last",
                                           "inference_ms")},

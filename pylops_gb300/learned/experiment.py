@@ -21,7 +21,7 @@ import time
 
 import numpy as np
 
-from .lsm import LearnedLSM, illumination_diagonal, make_pairs, random_reflectivity, train
+from .lsm import LearnedLSM, illumination_diagonal, make_pairs, point_spread_functions, random_reflectivity, train
 from .unet import UNet
 
 __all__ = ["lsm_operator", "run"]
@@ -113,12 +113,20 @@ def run(n_train: int = 4096, n_test: int = 64, steps: int = 2000, batch: int = 8
     nx, nz = op.dims
     tests = [random_reflectivity(nx, nz, rng) for _ in range(n_test)]
     diag = illumination_diagonal(op)
+    psf_op = None
+    if "psf" in variants:
+        from ..signalprocessing import NonStationaryConvolve2D
+
+        psfx, psfz = np.arange(16, nx, 32), np.arange(16, nz, 32)
+        hs = point_spread_functions(op, psfx, psfz, (31, 31))
+        psf_op = NonStationaryConvolve2D(dims=(nx, nz), hs=hs, ihx=psfx, ihz=psfz, dtype="float32")
     solvers = {
         "plain": (LearnedLSM(op), False),
         "diag": (LearnedLSM(op, diag=diag), False),
         "warm": (LearnedLSM(op, net=net, steps=0), True),
         "learned": (LearnedLSM(op, net=net, steps=steps_net, step_ratio=step_ratio), True),
         "learned+diag": (LearnedLSM(op, net=net, diag=diag, steps=steps_net, step_ratio=step_ratio), True),
+        "psf": (LearnedLSM(op, psf=psf_op, psf_iters=10), True),
     }
     # warm up every variant once (graph capture, workspaces)
     d = torch.empty(op.shape[0], dtype=torch.float32, device="cuda")

@@ -30,7 +30,8 @@ import numpy as np
 from .. import _native
 from .unet import UNet
 
-__all__ = ["random_reflectivity", "make_pairs", "train", "illumination_diagonal", "LearnedLSM", "SolveInfo"]
+__all__ = ["random_reflectivity", "make_pairs", "train", "illumination_diagonal", "point_spread_functions",
+           "LearnedLSM", "SolveInfo"]
 
 
 def random_reflectivity(nx: int, nz: int, rng: np.random.Generator, dx: float = 5.0, dz: float = 5.0,
@@ -154,6 +155,37 @@ def illumination_diagonal(op, eps: float = 1e-3) -> np.ndarray:
     return (1.0 / np.sqrt(diag + eps * diag.max())).astype(np.float32)
 
 
+def point_spread_functions(op, psfx, psfz, psfsize=(31, 31)):
+    """Point-spread functions of the Hessian ``K^H K`` of a 2-D Kirchhoff
+    operator, the filters of an image-domain Hessian
+    (``NonStationaryConvolve2D``): unit scatterers at the grid ``psfx`` x
+    ``psfz`` (indices), one forward and one adjoint, and a ``psfsize``
+    window around each scatterer (the workflow of ``tutorials/ilsm.py``).
+    The grid spacing must exceed the window so windows do not overlap.
+    Returns a float32 CUDA tensor (len(psfx), len(psfz), *psfsize)."""
+    import torch
+
+    nx, nz = op.dims
+    hx, hz = psfsize
+    psfx, psfz = np.asarray(psfx), np.asarray(psfz)
+    if np.any(np.diff(psfx) < hx) or np.any(np.diff(psfz) < hz):
+        raise ValueError("point scatterers closer than the PSF window")
+    if psfx.min() < hx // 2 or psfz.min() < hz // 2 or psfx.max() + hx // 2 >= nx or psfz.max() + hz // 2 >= nz:
+        raise ValueError("PSF windows must lie inside the image")
+    m = torch.zeros((nx, nz), dtype=torch.float32, device="cuda")
+    m[torch.as_tensor(psfx, device="cuda")[:, None], torch.as_tensor(psfz, device="cuda")[None, :]] = 1.0
+    d = torch.empty(op.shape[0], dtype=torch.float32, device="cuda")
+    img = torch.empty(op.ni, dtype=torch.float32, device="cuda")
+    op.apply_into(m.reshape(-1), d)
+    op.apply_into(d, img, adjoint=True)
+    img = img.view(nx, nz)
+    hs = torch.empty((len(psfx), len(psfz), hx, hz), dtype=torch.float32, device="cuda")
+    for i, px in enumerate(psfx):
+        for j, pz in enumerate(psfz):
+            hs[i, j] = img[px - hx // 2:px + hx // 2 + 1, pz - hz // 2:pz + hz // 2 + 1]
+    return hs
+
+
 @dataclass
 class SolveInfo:
     """Outcome of one solve: LSQR iterations, wall time (s, device-
@@ -196,11 +228,13 @@ class LearnedLSM:
     the warm start does not lower the residual."""
 
     def __init__(self, op, net: Optional[UNet] = None, diag: Optional[np.ndarray] = None, steps: int = 4,
-                 step_ratio: float = 0.7):
+                 step_ratio: float = 0.7, psf=None, psf_iters: int = 10):
         import torch
 
         self.op = op
         self.net = net
+        self.psf = psf  # image-domain Hessian (NonStationaryConvolve2D): classical warm start
+        self.psf_iters = int(psf_iters)
         self.steps = int(steps)
         self.step_ratio = float(step_ratio)
         self.diag = None if diag is None else np.ascontiguousarray(diag, dtype=np.float32)
@@ -287,6 +321,33 @@ class LearnedLSM:
         self._launches += 1
         return x, rel, len(P), pairs
 
+    def psf_phase(self, d):
+        """Classical warm start: CGLS on the image-domain Hessian
+        (``psf``, ``psf_iters`` iterations) from the migrated image, scaled by
+        the least-squares fit of its data to d.  Returns (x0 or None, rel,
+        operator pairs)."""
+        import torch
+
+        from ..optimization.basic import cgls
+
+        op = self.op
+        img = torch.empty(op.ni, dtype=torch.float32, device="cuda")
+        op.apply_into(d, img, adjoint=True)
+        u = cgls(self.psf, img, niter=self.psf_iters, tol=0.0)[0].contiguous()
+        info = op.info()
+        self._launches += info["kernels_adjoint"] + 2 * self.psf_iters + info["kernels_forward"]
+        Ku = torch.empty_like(d)
+        op.apply_into(u, Ku)
+        kd, kk, dd = self._dots([(Ku, d), (Ku, Ku), (d, d)])
+        self._launches += 3
+        if kk <= 0 or dd <= 0:
+            return None, 1.0, 1
+        alpha = kd / kk
+        rel = math.sqrt(max(dd - alpha * kd, 0.0) / dd)
+        if rel >= 1.0:
+            return None, 1.0, 1
+        return u.mul_(alpha), rel, 1
+
     def solve(self, d, tol: float = 1e-2, niter: int = 500, use_net: bool = True) -> tuple:
         """Returns ``(x, SolveInfo)``.  ``d`` is a CUDA tensor (x is then a
         float32 CUDA tensor) or a host array (staged through pinned memory
@@ -309,6 +370,8 @@ class LearnedLSM:
         self._launches = 0
         if use_net and self.net is not None:
             x0, rel0, nsteps, pairs = self.network_phase(dd, tol)
+        elif use_net and self.psf is not None:
+            x0, rel0, pairs = self.psf_phase(dd)
         launches = self._launches
         iiter, istop, cost = 0, 1, [rel0]
         x = x0
