@@ -144,6 +144,7 @@ def cpu_baseline(K, m, d, target_s=10.0):
 
     build()
     C = COracle(K, _padded_wavelet(K))
+    _cpu_step(C, m, d, 0, 1)  # first call: thread start-up, page faults
     t0 = time.perf_counter()
     _cpu_step(C, m, d, 0, 1)
     t1 = time.perf_counter() - t0
