@@ -248,6 +248,19 @@ int kgb_gemm_bf16_tn_splitk(const void* A_dev, const void* B_dev, float* C_dev, 
                             int ldb, int ldc, int splits, float* work_dev, int64_t work_elems, int* err_dev,
                             void* stream);
 
+/* Implicit 3x3 stride-1 convolution (zero padding 1) on the tensor cores:
+ * y[p][n] = sum_{tap, c} w[n][tap*Cp + c] x[pixel(p) + sgn*(ky-1, kx-1)][c]
+ * (+ bias[n], ReLU if flags & 1, bf16 output if flags & 2, else float32),
+ * x NHWC bf16 (B x H x W x C, C % 8 == 0), w bf16 (N x 9*Cp) with Cp = C
+ * rounded up to 64 (zero columns), tap = ky*3 + kx, sgn = +1 (flip = 0,
+ * forward) or -1 (flip = 1: the transposed convolution that gives a data
+ * gradient).  The input is read by 4-D TMA boxes shifted per tap (the
+ * padding is the boxes' zero fill): no unfolded copy.  W must divide 128
+ * (with H a multiple of 128/W) or be a multiple of 128.  No reference
+ * counterpart. */
+int kgb_conv3x3_bf16(const void* x_dev, const void* w_dev, void* y_dev, int B, int H, int W, int C, int N, int flip,
+                     const float* bias_dev, int flags, int* err_dev, void* stream);
+
 /* ---- U-Net helper kernels (NHWC bf16 activations) ------------------------
  * No reference counterpart (the learned preconditioner is new).  A ks x ks
  * convolution (ks 1 or 3, padding ks/2, stride 1 or 2) with weights
@@ -262,6 +275,10 @@ int kgb_gemm_bf16_tn_splitk(const void* A_dev, const void* B_dev, float* C_dev, 
  *  transpose    out[c][r] = in[r][c] (kind 0 bf16, 1 float32);
  *  weights      bf16 W (Cout x Kpad) and, if Wt != NULL, Wt (Cin x Kg) with
  *               Wt[ci][tap*Cout + co] = W[co][tap*Cin + ci], from float32 W;
+ *  weights_implicit  bf16 weights of kgb_conv3x3_bf16 from float32 W
+ *               (Cout x Kpad, 3x3): Wi (Cout x 9*Cpi) and, if Wti != NULL,
+ *               Wti (Cin x 9*Cpo) for the data gradient, Cpi / Cpo = Cin /
+ *               Cout rounded up to 64, zero padded;
  *  relu_grad    g = dy * (y > 0) (relu) or dy, as bf16;
  *  rowsum       out[r] = sum_c in[r][c] (bf16 in, bias gradients; work:
  *               rows x 64 floats of scratch);
@@ -280,6 +297,7 @@ int kgb_unet_unfold_t(const void* x, void* colT, int B, int H, int W, int C, int
 int kgb_unet_transpose(const void* in, void* out, int64_t rows, int cols, int64_t ldi, int64_t ldo, int kind,
                        void* stream);
 int kgb_unet_weights(const float* W, void* Wb, void* Wt, int Cout, int Cin, int ks, int Kpad, int Kg, void* stream);
+int kgb_unet_weights_implicit(const float* W, void* Wi, void* Wti, int Cout, int Cin, int Kpad, void* stream);
 int kgb_unet_relu_grad(const float* dy, const void* y, void* g, int64_t n, int relu, void* stream);
 int kgb_unet_rowsum(const void* in, float* out, int rows, int64_t cols, float* work, void* stream);
 int kgb_unet_upsample(const void* x, void* y, int B, int H, int W, int C, int Ctot, int coff, int grad,

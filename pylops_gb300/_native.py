@@ -77,10 +77,12 @@ _SIGNATURES = {
     "kgb_gemm_bf16_tn": ([c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_vp, c_int, c_vp, c_vp], c_int),
     "kgb_gemm_bf16_tn_splitk": ([c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_vp, c_i64,
                                  c_vp, c_vp], c_int),
+    "kgb_conv3x3_bf16": ([c_vp, c_vp, c_vp] + [c_int] * 6 + [c_vp, c_int, c_vp, c_vp], c_int),
     "kgb_unet_unfold": ([c_vp, c_vp] + [c_int] * 10 + [c_vp], c_int),
     "kgb_unet_unfold_t": ([c_vp, c_vp] + [c_int] * 6 + [c_vp], c_int),
     "kgb_unet_transpose": ([c_vp, c_vp, c_i64, c_int, c_i64, c_i64, c_int, c_vp], c_int),
     "kgb_unet_weights": ([c_vp, c_vp, c_vp] + [c_int] * 5 + [c_vp], c_int),
+    "kgb_unet_weights_implicit": ([c_vp, c_vp, c_vp, c_int, c_int, c_int, c_vp], c_int),
     "kgb_unet_relu_grad": ([c_vp, c_vp, c_vp, c_i64, c_int, c_vp], c_int),
     "kgb_unet_rowsum": ([c_vp, c_vp, c_int, c_i64, c_vp, c_vp], c_int),
     "kgb_unet_upsample": ([c_vp, c_vp] + [c_int] * 7 + [c_vp], c_int),

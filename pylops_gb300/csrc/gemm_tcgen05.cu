@@ -68,6 +68,26 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// 4-D tiled load (implicit convolution: channels, width, height, image).
+// Coordinates other than the innermost may be negative or past the end: the
+// box is zero-filled there (the convolution's padding).
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0, int c1,
+                                            int c2, int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6}], [%2];"
+        ::"r"(dst), "l"(map), "r"(bar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+        : "memory");
+}
+
+// Geometry of an implicit 3x3 stride-1 convolution over NHWC bf16 input:
+// an M tile of 128 output pixels is a box of bh rows x bw columns of one
+// image; k-tile g is (tap = g / cblk, channel block g % cblk) and reads the
+// input shifted by sgn * (ky - 1, kx - 1) (sgn = -1: the transposed
+// convolution of the data gradient).
+struct ConvGeom {
+    int H, W, cblk, sgn;
+};
+
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle.
 // start address >> 4 in bits [0,14); leading byte offset (unused for
 // swizzled K-major, 1) in [16,30); stride byte offset = 1024 B between
@@ -95,11 +115,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-template <int BN>
+template <int BN, bool CONV>
 __global__ void __launch_bounds__(128, 1)
 gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, void* __restrict__ C,
                int M, int N, int K, int ldc, const float* __restrict__ bias, int flags, int* __restrict__ err,
-               int kt_per, int64_t split_stride) {
+               int kt_per, int64_t split_stride, const ConvGeom cg) {
     constexpr int A_BYTES = BM * BK * 2;
     constexpr int B_BYTES = BN * BK * 2;
     extern __shared__ uint8_t smem_dyn[];
@@ -146,6 +166,14 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
 
     if (warp == 0 && lane == 0) {
         // producer
+        int img = 0, h0 = 0, w0 = 0;
+        if (CONV) {
+            const int hw = cg.H * cg.W;
+            img = m0 / hw;
+            const int r = m0 - img * hw;
+            h0 = r / cg.W;
+            w0 = r - h0 * cg.W;
+        }
         for (int kt = 0; kt < ktiles; ++kt) {
             const int s = kt % STAGES;
             if (kt >= STAGES && !mbar_wait(bar_empty + 8 * s, ((kt / STAGES) - 1) & 1)) {
@@ -153,7 +181,15 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                 break;
             }
             mbar_expect_tx(bar_full + 8 * s, A_BYTES + B_BYTES);
-            tma_load_2d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, (kt0 + kt) * BK, m0);
+            if (CONV) {
+                const int g = kt0 + kt;
+                const int tap = g / cg.cblk, cb = g - tap * cg.cblk;
+                const int ky = tap / 3, kx = tap - ky * 3;
+                tma_load_4d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, cb * BK, w0 + cg.sgn * (kx - 1),
+                            h0 + cg.sgn * (ky - 1), img);
+            } else {
+                tma_load_2d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, (kt0 + kt) * BK, m0);
+            }
             tma_load_2d(sB + s * B_BYTES, &tmB, bar_full + 8 * s, (kt0 + kt) * BK, n0);
         }
     } else if (warp == 1 && lane == 0) {
@@ -282,22 +318,43 @@ int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int
     return KGB_OK;
 }
 
+// NHWC bf16 activations (B images of H x W pixels, C channels) as a 4-D
+// tensor {C, W, H, B}; box {64 channels, bw, bh, 1} = 128 pixels of one
+// image, each a 128-byte row of the shared-memory tile (the layout of the
+// 2-D A tile).
+int make_map_nhwc(CUtensorMap* map, const void* base, int B, int H, int W, int C, int bw, int bh) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_error(KGB_ERR_CUDA, "conv: cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)bw, (cuuint32_t)bh, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(KGB_ERR_VALUE, "conv: tensor map rejected (CUresult %d)", (int)r);
+    return KGB_OK;
+}
+
 template <int BN>
 size_t gemm_smem() {
     return 1024 + (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * STAGES + 1) + 16;
 }
 
-template <int BN>
+template <int BN, bool CONV = false>
 int gemm_launch(const CUtensorMap& ma, const CUtensorMap& mb, void* C, int M, int N, int K, int ldc, const float* bias,
-                int flags, int* err, int splits, int kt_per, int64_t split_stride, cudaStream_t s) {
+                int flags, int* err, int splits, int kt_per, int64_t split_stride, cudaStream_t s,
+                ConvGeom cg = ConvGeom{1, 1, 1, 1}) {
     static bool attr = false;
     const size_t smem = gemm_smem<BN>();
     if (!attr) {
-        KGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tn_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        KGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tn_kernel<BN, CONV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
         attr = true;
     }
     dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)((N + BN - 1) / BN), (unsigned)splits);
-    gemm_tn_kernel<BN><<<grid, 128, smem, s>>>(ma, mb, C, M, N, K, ldc, bias, flags, err, kt_per, split_stride);
+    gemm_tn_kernel<BN, CONV><<<grid, 128, smem, s>>>(ma, mb, C, M, N, K, ldc, bias, flags, err, kt_per, split_stride,
+                                                     cg);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -377,4 +434,40 @@ extern "C" int kgb_gemm_bf16_tn_splitk(const void* A, const void* B, float* C, i
     splitk_sum_kernel<<<grid, 256, 0, s>>>(work, C, M, N, ldc, splits);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
+}
+
+extern "C" int kgb_conv3x3_bf16(const void* x, const void* w, void* y, int B, int H, int W, int C, int N, int flip,
+                                const float* bias, int flags, int* err_dev, void* stream) {
+    if (!x || !w || !y) return set_error(KGB_ERR_VALUE, "conv: null pointer");
+    if (B <= 0 || H <= 0 || W <= 0 || C <= 0 || N <= 0) return set_error(KGB_ERR_VALUE, "conv: sizes must be positive");
+    if (C % 8) return set_error(KGB_ERR_VALUE, "conv: channels must be a multiple of 8 (16-byte pixel rows)");
+    if (((uintptr_t)x | (uintptr_t)w) & 15) return set_error(KGB_ERR_VALUE, "conv: x and w must be 16-byte aligned");
+    // 128-pixel M tiles as boxes of whole rows (W <= 128) or row segments (W >= 128)
+    int bw, bh;
+    if (W >= BM) {
+        if (W % BM) return set_error(KGB_ERR_VALUE, "conv: width %d is neither a divisor nor a multiple of 128", W);
+        bw = BM;
+        bh = 1;
+    } else {
+        if (BM % W || H % (BM / W))
+            return set_error(KGB_ERR_VALUE, "conv: %d x %d image does not tile into 128-pixel boxes", H, W);
+        bw = W;
+        bh = BM / W;
+    }
+    const int cblk = (C + BK - 1) / BK;
+    const int K = 9 * cblk * BK;
+    const int64_t M = (int64_t)B * H * W;
+    if (M > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "conv: too many pixels");
+    const int BN = N <= 64 ? 64 : 128;
+    CUtensorMap ma, mb;
+    int rc;
+    if ((rc = make_map_nhwc(&ma, x, B, H, W, C, bw, bh))) return rc;
+    if ((rc = make_map(&mb, w, N, K, K, BN))) return rc;
+    flags = (flags & 3) | vector_flag(y, N, flags);
+    const ConvGeom cg{H, W, cblk, flip ? -1 : 1};
+    cudaStream_t s = (cudaStream_t)stream;
+    const int ktiles = K / BK;
+    if (BN == 64)
+        return gemm_launch<64, true>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
+    return gemm_launch<128, true>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
 }

@@ -200,6 +200,31 @@ __global__ void weights_kernel(const float* __restrict__ Wm, bf16* __restrict__ 
     }
 }
 
+// bf16 weights of the implicit 3x3 convolutions: Wi (Cout x 9*Cpi) for the
+// forward and Wti (Cin x 9*Cpo) for the data gradient, channel blocks
+// padded to 64 (Cpi, Cpo) with zeros.
+__global__ void weights_implicit_kernel(const float* __restrict__ Wm, bf16* __restrict__ Wi, bf16* __restrict__ Wti,
+                                        int Cout, int Cin, int Kpad, int Cpi, int Cpo) {
+    const int64_t nI = (int64_t)Cout * 9 * Cpi, nT = Wti ? (int64_t)Cin * 9 * Cpo : 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nI + nT; i += (int64_t)gridDim.x * blockDim.x) {
+        float v = 0.f;
+        if (i < nI) {
+            const int co = (int)(i / (9 * Cpi));
+            const int q = (int)(i - (int64_t)co * 9 * Cpi);
+            const int tap = q / Cpi, c = q - tap * Cpi;
+            if (c < Cin) v = Wm[(int64_t)co * Kpad + tap * Cin + c];
+            Wi[i] = __float2bfloat16(v);
+        } else {
+            const int64_t j = i - nI;
+            const int ci = (int)(j / (9 * Cpo));
+            const int q = (int)(j - (int64_t)ci * 9 * Cpo);
+            const int tap = q / Cpo, co = q - tap * Cpo;
+            if (co < Cout) v = Wm[(int64_t)co * Kpad + tap * Cin + ci];
+            Wti[j] = __float2bfloat16(v);
+        }
+    }
+}
+
 // g = dy (.) (y > 0)  (relu) or dy, rounded to bf16
 __global__ void relu_grad_kernel(const float* __restrict__ dy, const bf16* __restrict__ y, bf16* __restrict__ g,
                                  int64_t n, int relu) {
@@ -428,6 +453,17 @@ int kgb_unet_weights(const float* Wm, void* Wb, void* Wt, int Cout, int Cin, int
     const int64_t n = (int64_t)Cout * Kpad + (Wt ? (int64_t)Cin * Kg : 0);
     weights_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(Wm, (bf16*)Wb, (bf16*)Wt, Cout, Cin, ks * ks, Kpad,
                                                                   Kg);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_weights_implicit(const float* Wm, void* Wi, void* Wti, int Cout, int Cin, int Kpad, void* stream) {
+    if (!Wm || !Wi || Cout <= 0 || Cin <= 0 || Kpad < 9 * Cin)
+        return set_error(KGB_ERR_VALUE, "unet_weights_implicit: bad arguments");
+    const int Cpi = (Cin + 63) / 64 * 64, Cpo = (Cout + 63) / 64 * 64;
+    const int64_t n = (int64_t)Cout * 9 * Cpi + (Wti ? (int64_t)Cin * 9 * Cpo : 0);
+    weights_implicit_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(Wm, (bf16*)Wi, (bf16*)Wti, Cout, Cin, Kpad,
+                                                                           Cpi, Cpo);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

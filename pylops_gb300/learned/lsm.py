@@ -291,11 +291,13 @@ class LearnedLSM:
         src = d
         for j in range(nmax):
             op.apply_into(src, g, adjoint=True)
+            l0 = self.net.launches
             p = self.net.forward(g.view(nx, nz)).reshape(-1).contiguous()
+            self._launches += self.net.launches - l0
             q = torch.empty_like(d)
             op.apply_into(p, q)
             pairs += 1
-            self._launches += fa + self.net.launches_per_forward + len(Q) + 2
+            self._launches += fa + len(Q) + 2
             vals = self._dots([(q, v) for v in Q] + [(q, q), (q, d)])
             G[j, :j] = G[:j, j] = vals[:j]
             G[j, j] = vals[j]

@@ -37,6 +37,11 @@ def _rup(n: int, k: int = 8) -> int:
     return (n + k - 1) // k * k
 
 
+def _tileable(H: int, W: int) -> bool:
+    """Can 128-pixel M tiles be TMA boxes of one image (kgb_conv3x3_bf16)?"""
+    return (W >= 128 and W % 128 == 0) or (W < 128 and 128 % W == 0 and H % (128 // W) == 0)
+
+
 class _Conv:
     """One convolution layer: shapes, parameter offsets, bf16 weight copies."""
 
@@ -49,6 +54,12 @@ class _Conv:
         self.b_off = 0
         self.Wb = None                      # bf16 (cout x kpad)
         self.Wt = None                      # bf16 (cin x kg)
+        # 3x3 stride-1 convolutions over >= 8 channels also run as implicit
+        # GEMMs (kgb_conv3x3_bf16) with weights in 64-channel blocks
+        self.implicit = ks == 3 and stride == 1 and cin % 8 == 0
+        self.implicit_dx = self.implicit and cout % 8 == 0
+        self.Wi = None                      # bf16 (cout x 9 * rup(cin, 64))
+        self.Wti = None                     # bf16 (cin x 9 * rup(cout, 64))
 
     @property
     def nparams(self) -> int:
@@ -88,8 +99,10 @@ class UNet:
     Adam step.  H and W must be divisible by 2^(levels-1) and the number of
     pixels of the coarsest level (B H W / 4^(levels-1)) by 8."""
 
-    def __init__(self, levels: int = 4, base: int = 32, seed: int = 0, normalize: bool = True):
+    def __init__(self, levels: int = 4, base: int = 32, seed: int = 0, normalize: bool = True, implicit: bool = True):
         import torch
+
+        self.implicit = bool(implicit)  # implicit-GEMM 3x3 convolutions where the geometry allows
 
         if levels < 1:
             raise ValueError("levels must be >= 1")
@@ -140,6 +153,10 @@ class UNet:
         for c in convs:
             c.Wb = torch.empty((c.cout, c.kpad), dtype=torch.bfloat16, device=dev)
             c.Wt = torch.empty((c.cin, c.kg), dtype=torch.bfloat16, device=dev)
+            if c.implicit:
+                c.Wi = torch.empty((c.cout, 9 * _rup(c.cin, 64)), dtype=torch.bfloat16, device=dev)
+                if c.implicit_dx:
+                    c.Wti = torch.empty((c.cin, 9 * _rup(c.cout, 64)), dtype=torch.bfloat16, device=dev)
         self._refresh_weights()
         self._ws = None
         self._ws_key = None
@@ -175,6 +192,10 @@ class UNet:
         for c in self.convs:
             _native.check(L.kgb_unet_weights(self._w(c).data_ptr(), c.Wb.data_ptr(), c.Wt.data_ptr(), c.cout, c.cin,
                                              c.ks, c.kpad, c.kg, s))
+            if c.implicit:
+                _native.check(L.kgb_unet_weights_implicit(self._w(c).data_ptr(), c.Wi.data_ptr(),
+                                                          c.Wti.data_ptr() if c.Wti is not None else None, c.cout,
+                                                          c.cin, c.kpad, s))
 
     def get_weights(self) -> List[tuple]:
         """Per layer (W (cout, cin, ks, ks), b (cout,)) as float32 numpy arrays
@@ -210,14 +231,6 @@ class UNet:
         self.normalize = bool(sd.get("normalize", True))
         self.step_count = int(sd.get("step", 0))
         self._refresh_weights()
-
-    @property
-    def launches_per_forward(self) -> int:
-        """Kernel launches of one ``forward``: input RMS and bf16 cast, an
-        unfold (except for the 1x1 head) and a GEMM per convolution, an
-        upsample and a skip copy per decoder level."""
-        unfolds = sum(1 for c in self.convs if not (c.ks == 1 and c.stride == 1 and c.cin % 8 == 0))
-        return (2 if self.normalize else 1) + unfolds + len(self.convs) + 2 * len(self.dec)
 
     def flops(self, H: int, W: int, training: bool = False) -> float:
         """Algorithmic multiply-add flops (2 per MAC) of the convolutions for
@@ -309,12 +322,18 @@ class UNet:
         P_out = ws["P"][lo]
         if c.ks == 1 and c.stride == 1 and c.cin % 8 == 0:
             A, lda = x, c.cin
+        elif self.implicit and c.implicit and _tileable(Ho, Wo):
+            A, lda = None, 0
         else:
             A, lda = ws["col"], c.kpad
             _native.check(L.kgb_unet_unfold(x.data_ptr(), A.data_ptr(), B, H, W, c.cin, Ho, Wo, c.ks, c.stride, 0,
                                             c.kpad, s))
         y = ws["y"][i]
         flags = (1 if c.relu else 0) | (2 if i != self.head else 0)
+        if self.implicit and c.implicit and _tileable(Ho, Wo):
+            _native.check(L.kgb_conv3x3_bf16(x.data_ptr(), c.Wi.data_ptr(), y.data_ptr(), B, H, W, c.cin, c.cout, 0,
+                                             self._b(c).data_ptr(), flags, self._err.data_ptr(), s))
+            return
         _native.check(L.kgb_gemm_bf16_tn(A.data_ptr(), c.Wb.data_ptr(), y.data_ptr(), P_out, c.cout, c.kpad, lda,
                                          c.kpad, c.cout, self._b(c).data_ptr(), flags, self._err.data_ptr(), s))
 
@@ -342,6 +361,11 @@ class UNet:
                                                 P_out, P_out, P_out, c.kpad, 0, ws["work"].data_ptr(),
                                                 ws["work_elems"], self._err.data_ptr(), s))
         if dx is None:
+            return
+        if self.implicit and c.implicit_dx and _tileable(H, W):
+            # the transposed convolution straight from g (no unfold)
+            _native.check(L.kgb_conv3x3_bf16(g.data_ptr(), c.Wti.data_ptr(), dx.data_ptr(), B, H, W, c.cout, c.cin, 1,
+                                             None, 0, self._err.data_ptr(), s))
             return
         _native.check(L.kgb_unet_unfold(g.data_ptr(), col.data_ptr(), B, Ho, Wo, c.cout, H, W, c.ks, c.stride, 1,
                                         c.kg, s))

@@ -46,7 +46,7 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
-@pytest.mark.parametrize("levels,base,B,H,W", [(3, 8, 2, 16, 32), (4, 16, 1, 32, 16)])
+@pytest.mark.parametrize("levels,base,B,H,W", [(3, 8, 2, 16, 32), (4, 16, 1, 32, 16), (4, 16, 1, 64, 256)])
 def test_unet_forward_and_gradients_match_cpu_autograd(levels, base, B, H, W):
     from pylops_gb300.learned.unet import UNet
 
@@ -110,3 +110,51 @@ def test_splitk_gemm_matches_fp32_reference():
         assert int(err.item()) == 0
         assert _rel(got[:, :N].numpy(), ref.numpy()) < 1e-5
         assert torch.all(got[:, N:] == 7.0)
+
+
+@pytest.mark.parametrize("B,H,W,C,N,flip", [(2, 16, 32, 32, 32, 0), (1, 8, 256, 96, 64, 0), (2, 32, 64, 64, 96, 1),
+                                            (1, 64, 128, 40, 128, 1)])
+def test_implicit_conv3x3_matches_conv2d(B, H, W, C, N, flip):
+    """kgb_conv3x3_bf16 (4-D TMA boxes shifted per tap, zero fill as padding)
+    against torch conv2d on the same bf16-rounded operands; flip = 1 is the
+    transposed convolution (kernel flipped in both axes)."""
+    import torch.nn.functional as F
+
+    from pylops_gb300 import _native
+
+    g = torch.Generator().manual_seed(B * 1000 + C + N)
+    x = _bf(torch.randn(B, H, W, C, generator=g))
+    w = _bf(torch.randn(N, C, 3, 3, generator=g) / (3 * C ** 0.5))
+    bias = torch.randn(N, generator=g)
+    Cp = (C + 63) // 64 * 64
+    wi = torch.zeros(N, 9, Cp)
+    wi[:, :, :C] = w.permute(0, 2, 3, 1).reshape(N, 9, C)
+    xd = x.to(torch.bfloat16).cuda().contiguous()
+    wd = wi.reshape(N, 9 * Cp).to(torch.bfloat16).cuda().contiguous()
+    y = torch.empty(B * H * W, N, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    bd = bias.cuda()
+    _native.check(_native.lib().kgb_conv3x3_bf16(xd.data_ptr(), wd.data_ptr(), y.data_ptr(), B, H, W, C, N, flip,
+                                                 None if flip else bd.data_ptr(), 0, err.data_ptr(),
+                                                 torch.cuda.current_stream().cuda_stream))
+    ref = F.conv2d(x.permute(0, 3, 1, 2), w.flip(2, 3) if flip else w, None if flip else bias, padding=1)
+    ref = ref.permute(0, 2, 3, 1).reshape(B * H * W, N)
+    assert int(err.item()) == 0
+    assert _rel(y.cpu().numpy(), ref.numpy()) < 1e-5
+
+
+def test_unet_implicit_and_explicit_paths_agree():
+    from pylops_gb300.learned.unet import UNet
+
+    g = torch.Generator().manual_seed(9)
+    x = torch.randn(2, 64, 32, generator=g).cuda()
+    t = torch.randn(2, 64, 32, generator=g).cuda()
+    a, b = UNet(levels=4, base=16, seed=2, implicit=True), UNet(levels=4, base=16, seed=2, implicit=False)
+    ya, yb = a.forward(x), b.forward(x)
+    assert _rel(ya.cpu().numpy(), yb.cpu().numpy()) < 1e-2
+    la, lb = float(a.loss_and_grad(x, t)), float(b.loss_and_grad(x, t))
+    assert abs(la - lb) / lb < 1e-2
+    for (wa, ba), (wb, bb) in zip(a.gradients(), b.gradients()):
+        assert _rel(wa, wb) < 3e-2 and _rel(ba, bb) < 3e-2
+    a.check_errors()
+    b.check_errors()
