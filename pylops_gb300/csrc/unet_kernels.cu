@@ -159,6 +159,27 @@ __global__ void unfold_t_vec_kernel(const bf16* __restrict__ x, bf16* __restrict
     }
 }
 
+// unfold_t for narrow inputs (C < 32, where a 32 x 32 tile would leave
+// most lanes idle): one thread per output element, pixels fastest.
+__global__ void unfold_t_small_kernel(const bf16* __restrict__ x, bf16* __restrict__ colT, int H, int W, int C, int Ho,
+                                      int Wo, int ks, int s, int64_t P) {
+    const int pad = ks >> 1;
+    const int64_t total = (int64_t)ks * ks * C * P;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = i % P;
+        const int k = (int)(i / P);
+        const int tap = k / C, c = k - tap * C;
+        const int ky = tap / ks, kx = tap - ky * ks;
+        const int wo = (int)(p % Wo);
+        const int64_t t = p / Wo;
+        const int ho = (int)(t % Ho);
+        const int b = (int)(t / Ho);
+        const int h = ho * s + ky - pad, w = wo * s + kx - pad;
+        colT[i] = (h >= 0 && h < H && w >= 0 && w < W) ? x[(((int64_t)b * H + h) * W + w) * C + c]
+                                                       : __float2bfloat16(0.f);
+    }
+}
+
 // out[c][r] = in[r][c]; rows x cols, in leading dimension ldi, out ldo.
 template <typename TI, typename TO>
 __global__ void transpose_kernel(const TI* __restrict__ in, TO* __restrict__ out, int64_t rows, int cols, int64_t ldi,
@@ -277,6 +298,23 @@ __global__ void upsample_kernel(const bf16* __restrict__ x, bf16* __restrict__ y
         const int h = (int)(t % (2 * H));
         const int b = (int)(t / (2 * H));
         y[(((int64_t)b * 2 * H + h) * 2 * W + w) * Ctot + coff + c] = x[(((int64_t)b * H + h / 2) * W + w / 2) * C + c];
+    }
+}
+
+// vector form (C, Ctot, coff multiples of 8, 16-byte aligned): 8 channels
+// (16 bytes) per thread
+__global__ void upsample_vec_kernel(const uint4* __restrict__ x, uint4* __restrict__ y, int B, int H, int W, int C8,
+                                    int Ctot8, int coff8) {
+    const int64_t total = (int64_t)B * 2 * H * 2 * W * C8;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C8);
+        int64_t t = i / C8;
+        const int w = (int)(t % (2 * W));
+        t /= 2 * W;
+        const int h = (int)(t % (2 * H));
+        const int b = (int)(t / (2 * H));
+        y[(((int64_t)b * 2 * H + h) * 2 * W + w) * Ctot8 + coff8 + c] =
+            __ldg(x + (((int64_t)b * H + h / 2) * W + w / 2) * C8 + c);
     }
 }
 
@@ -421,6 +459,10 @@ int kgb_unet_unfold_t(const void* x, void* colT, int B, int H, int W, int C, int
         const int64_t n = (int64_t)ks * ks * (C / 8) * (P / 8);
         unfold_t_vec_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, H, W, C, Ho,
                                                                             Wo, ks, stride, P);
+    } else if (C < 32) {
+        const int64_t n = (int64_t)ks * ks * C * P;
+        unfold_t_small_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, H, W, C, Ho,
+                                                                             Wo, ks, stride, P);
     } else {
         dim3 grid((unsigned)((P + 31) / 32), (unsigned)((C + 31) / 32), (unsigned)(ks * ks)), block(32, 8);
         unfold_t_kernel<<<grid, block, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, B, H, W, C, Ho, Wo,
@@ -492,8 +534,14 @@ int kgb_unet_upsample(const void* x, void* y, int B, int H, int W, int C, int Ct
         const int64_t n = (int64_t)B * H * W * C;
         upsample_grad_kernel<<<grid_for(n), 256, 0, s>>>((const float*)x, (float*)y, B, H, W, C, Ctot, coff);
     } else {
-        const int64_t n = (int64_t)B * 4 * H * W * C;
-        upsample_kernel<<<grid_for(n), 256, 0, s>>>((const bf16*)x, (bf16*)y, B, H, W, C, Ctot, coff);
+        if (C % 8 == 0 && Ctot % 8 == 0 && coff % 8 == 0 && (((uintptr_t)x | (uintptr_t)y) & 15) == 0) {
+            const int64_t n = (int64_t)B * 4 * H * W * (C / 8);
+            upsample_vec_kernel<<<grid_for(n), 256, 0, s>>>((const uint4*)x, (uint4*)y, B, H, W, C / 8, Ctot / 8,
+                                                            coff / 8);
+        } else {
+            const int64_t n = (int64_t)B * 4 * H * W * C;
+            upsample_kernel<<<grid_for(n), 256, 0, s>>>((const bf16*)x, (bf16*)y, B, H, W, C, Ctot, coff);
+        }
     }
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
