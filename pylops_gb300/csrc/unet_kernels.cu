@@ -113,8 +113,8 @@ __global__ void unfold_t_kernel(const bf16* __restrict__ x, bf16* __restrict__ c
 // Vector form of unfold_t for C % 8 == 0 and P % 8 == 0: each thread moves
 // an 8-pixel x 8-channel block of one tap (eight 16-byte loads, an 8 x 8
 // transpose of 16-bit values in registers, eight 16-byte stores).
-// Consecutive threads take consecutive pixel groups, so a warp stores 512
-// contiguous bytes of a colT row.
+// Consecutive threads take the channel groups of consecutive pixel groups,
+// so a warp's loads cover whole pixels and its stores runs of 8 pixels.
 __global__ void unfold_t_vec_kernel(const bf16* __restrict__ x, bf16* __restrict__ colT, int H, int W, int C, int Ho,
                                     int Wo, int ks, int s, int64_t P) {
     const int pad = ks >> 1;
@@ -122,10 +122,12 @@ __global__ void unfold_t_vec_kernel(const bf16* __restrict__ x, bf16* __restrict
     const int64_t pgn = P >> 3;
     const int64_t total = (int64_t)ks * ks * cgn * pgn;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t pg = i % pgn;
-        const int64_t rest = i / pgn;
-        const int cg = (int)(rest % cgn);
-        const int tap = (int)(rest / cgn);
+        // channel group fastest: a warp loads whole pixels (contiguous
+        // channel groups) and stores 8 runs of consecutive pixels per row
+        const int cg = (int)(i % cgn);
+        const int64_t rest = i / cgn;
+        const int64_t pg = rest % pgn;
+        const int tap = (int)(rest / pgn);
         const int ky = tap / ks, kx = tap - ky * ks;
         uint32_t v[8][4];
 #pragma unroll
