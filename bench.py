@@ -767,6 +767,131 @@ def run_nsconv(args):
     print(json.dumps(line))
 
 
+def run_config4(args):
+    """The 3-D workload: analytic constant velocity 2500 m/s, dynamic, 100 x 100
+    x 120 grid at 10 m, 16 sources on a 4 x 4 and 400 receivers on a 20 x 20
+    surface grid, nt = 1001 at 4 ms, 20 Hz Ricker, traveltimes exact and
+    amplitude (weight) tables in bf16 (`--weights float32` to keep them in
+    float32).  A step is one forward and one adjoint; value = compulsory GB/s
+    (8-byte records: traveltime + two bf16 weights).  The line also carries 15
+    device LSQR iterations and the error of both directions against the float64
+    C oracle on sampled sources."""
+    import torch
+
+    from oracle.kirch_oracle_c import COracle, build
+    from pylops_gb300.optimization.cls_basic import LSQR
+    from pylops_gb300.utils.wavelets import ricker
+    from pylops_gb300.waveeqprocessing import Kirchhoff
+
+    ny = nx = 100
+    nz = 120
+    y, x, z = np.arange(ny) * 10.0, np.arange(nx) * 10.0, np.arange(nz) * 10.0
+    t = np.arange(1001) * 0.004
+    wav, _, wc = ricker(t[:41], f0=20)
+    sy, sx = np.meshgrid(np.linspace(y[0], y[-1], 4), np.linspace(x[0], x[-1], 4), indexing="ij")
+    ry, rx = np.meshgrid(np.linspace(y[0], y[-1], 20), np.linspace(x[0], x[-1], 20), indexing="ij")
+    srcs = np.vstack((sy.ravel(), sx.ravel(), np.zeros(16)))
+    recs = np.vstack((ry.ravel(), rx.ravel(), np.zeros(400)))
+    t0 = time.perf_counter()
+    K = Kirchhoff(z, x, t, srcs, recs, 2500.0, wav, wc, y=y, mode="analytic", dynamic=True, engine="cuda",
+                  dtype="float32")
+    K.set_weight_precision(args.weights)
+    t_setup = time.perf_counter() - t0
+    variant_ms = K.autotune()
+    # reflectivity: 4 planar dipping reflectors with N(0,1) amplitudes
+    rng = np.random.default_rng(4)
+    refl = np.zeros((ny, nx, nz))
+    Y, X = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    for _ in range(4):
+        z0, dy_, dx_ = rng.uniform(20, nz - 20), rng.uniform(-0.2, 0.2), rng.uniform(-0.2, 0.2)
+        iz = np.round(z0 + dy_ * (Y - ny / 2) + dx_ * (X - nx / 2)).astype(int)
+        ok = (iz >= 0) & (iz < nz)
+        refl[Y[ok], X[ok], iz[ok]] += rng.standard_normal()
+    m = torch.as_tensor(refl.reshape(-1).astype(np.float32), device="cuda")
+    d = torch.empty(K.shape[0], device="cuda")
+    img = torch.empty(K.ni, device="cuda")
+    for _ in range(args.warmup):
+        K.apply_into(m, d)
+        K.apply_into(d, img, adjoint=True)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler()
+    clocks.start()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    fw, ad = [], []
+    for _ in range(args.steps):
+        e0.record(stream)
+        K.apply_into(m, d)
+        e1.record(stream)
+        K.apply_into(d, img, adjoint=True)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        fw.append(e0.elapsed_time(e1))
+        ad.append(e1.elapsed_time(e2))
+    clk = clocks.stop()
+    step = (statistics.median(fw) + statistics.median(ad)) / 1e3
+    rec_bytes = 8 if args.weights == "bfloat16" else 12
+    B = 2 * (rec_bytes * K.ni * (K.ns + K.nr) + 8 * K.ni + 4 * K.nsnr * K.nt)
+    # 15 LSQR iterations on the device (one graph launch)
+    K.apply_into(m, d)
+    torch.cuda.synchronize()
+    tl = time.perf_counter()
+    out = LSQR(K).solve(d, niter=15, atol=0.0, btol=0.0, calc_var=False)
+    torch.cuda.synchronize()
+    t_lsqr = time.perf_counter() - tl
+    xinv = out[0]
+    # error against the float64 oracle on sampled sources
+    build()
+    C = COracle(K, _padded_wavelet(K))
+    g = torch.Generator(device="cuda").manual_seed(1)
+    mr = torch.randn(K.ni, device="cuda", generator=g)
+    dr = torch.randn(K.shape[0], device="cuda", generator=g)
+    yg = torch.empty_like(dr)
+    K.apply_into(mr, yg)
+    mh, dh = mr.cpu().numpy().astype(np.float64), dr.cpu().numpy().astype(np.float64).reshape(K.nsnr, K.nt)
+    ef, ea = [], []
+    for s_ in (3, 12):
+        rows = slice(s_ * K.nr, (s_ + 1) * K.nr)
+        yc, xc = _cpu_step(C, mh, dh, s_, s_ + 1)
+        ef.append(float(np.linalg.norm(yg.view(K.nsnr, K.nt)[rows].cpu().numpy() - yc[rows]) /
+                        np.linalg.norm(yc[rows])))
+        dz = torch.zeros(K.nsnr, K.nt, device="cuda")
+        dz[rows] = dr.view(K.nsnr, K.nt)[rows]
+        xi = torch.empty(K.ni, device="cuda")
+        K.apply_into(dz.view(-1), xi, adjoint=True)
+        ea.append(float(np.linalg.norm(xi.cpu().numpy() - xc) / np.linalg.norm(xc)))
+    peaks = _peaks()
+    mh_ = m.cpu().numpy()
+    te = time.perf_counter()
+    for _ in range(3):
+        dd = K @ mh_
+        K.H @ dd
+    e2e = (time.perf_counter() - te) / 3
+    print(json.dumps({
+        "metric": "Kirchhoff 3-D fwd+adj GB/s vs HBM peak", "value": round(B / step / 1e9, 2), "unit": "GB/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (weights %s)" % args.weights, "data": "synthetic",
+        "config": {"workload": "kirchhoff3d_analytic_dynamic_100x100x120_16x400_nt1001", "weights": args.weights,
+                   "l2": "tables larger than L2", "setup_s": round(t_setup, 1)},
+        "kernel_ms": {"forward": round(statistics.median(fw), 3), "adjoint": round(statistics.median(ad), 3)},
+        "spread_variant_ms": {str(k_): round(v_, 3) for k_, v_ in variant_ms.items()},
+        "hbm_fraction": round(B / step / 1e9 / peaks["hbm_gbs"], 5),
+        "roofline": {"bound": "hbm", "kernel": "spread" if statistics.median(fw) > statistics.median(ad) else "gather",
+                     "achieved": round(B / 2 / (max(statistics.median(fw), statistics.median(ad)) / 1e3) / 1e9, 2),
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(B / 2 / (max(statistics.median(fw), statistics.median(ad)) / 1e3) / 1e9 /
+                                   peaks["hbm_gbs"], 5), "traffic": None},
+        "lsqr_15_iterations_s": round(t_lsqr, 3), "lsqr_r1norm_relative": round(float(out[3]) / float(
+            torch.linalg.norm(d.double())), 5),
+        "error_vs_float64_oracle": {"forward_rel_l2": max(ef), "adjoint_rel_l2": max(ea), "sampled_sources": [3, 12]},
+        "e2e": {"value": round(B / e2e / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * (K.ni + K.shape[0]),
+                "d2h_bytes_per_step": 4 * (K.ni + K.shape[0])},
+        "gpu_launches": args.steps * (K.info()["kernels_forward"] + K.info()["kernels_adjoint"]),
+        "clocks": clk,
+    }))
+
+
 def run_lsm(args):
     """Learned-preconditioned LSM workload: 2-D dynamic eikonal Kirchhoff,
     v(z) = 1500 + 0.6 z on 256 x 512 at 5 m, 48 sources, 256 receivers,
@@ -843,11 +968,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single", "unet", "nsconv"],
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single", "unet", "nsconv", "config4"],
                     help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems; "
                          "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models); "
                          "single: the single-traveltime-table (HBM-streaming) mode; unet: U-Net training; "
-                         "nsconv: the non-stationary convolution (image-domain Hessian)")
+                         "nsconv: the non-stationary convolution (image-domain Hessian); config4: the 3-D workload")
+    ap.add_argument("--weights", default="bfloat16", choices=["bfloat16", "float32"],
+                    help="dynamic weight tables of the 3-D workload")
     ap.add_argument("--single-receivers", type=int, default=100)
     ap.add_argument("--lsm-train", type=int, default=4096)
     ap.add_argument("--lsm-steps", type=int, default=3000)
@@ -868,6 +995,8 @@ def main():
         run_unet(args)
     elif args.workload == "nsconv":
         run_nsconv(args)
+    elif args.workload == "config4":
+        run_config4(args)
     else:
         run_gpu(args)
 

@@ -66,6 +66,16 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op);
 int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* trav_srcs_host,
                                   const double* trav_recs_host);
 
+/* Weight precision of a dynamic operator: bf16 = 1 stores each table entry
+ * as an 8-byte record (fixed-point traveltime, cos and sin half-angle
+ * weights rounded to bf16) instead of 16 bytes; bf16 = 0 (default) keeps
+ * float32 weights.  Traveltimes stay exact.  The bf16 weights change results
+ * by about 1e-3 relative (each weight is rounded to 8 significant bits), so
+ * float32 is the mode that meets the 1e-5 parity with the reference.
+ * Replaces: the float64 amp_* / angle_* tables in the dynamic kernels
+ * (kirchhoff.py:784-1001), at half the table bytes. */
+int kgb_kirchhoff_set_weight_precision(kgb_kirchhoff* op, int bf16);
+
 /* Single traveltime table: trav (ni, ns*nr) float64 in the reference layout
  * (trav[ii][is*nr + ir], the `trav` array of mode='byot').  Kinematic
  * operators only (a dynamic operator returns KGB_ERR_NOT_IMPLEMENTED, as the

@@ -47,6 +47,7 @@ _SIGNATURES = {
     "kgb_kirchhoff_destroy": ([c_vp], c_int),
     "kgb_kirchhoff_set_traveltimes": ([c_vp, c_dp, c_dp], c_int),
     "kgb_kirchhoff_set_traveltime_table": ([c_vp, c_dp], c_int),
+    "kgb_kirchhoff_set_weight_precision": ([c_vp, c_int], c_int),
     "kgb_kirchhoff_set_dynamic": ([c_vp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_i64p, c_i64p], c_int),
     "kgb_kirchhoff_forward": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),

@@ -62,6 +62,10 @@ struct KirchDev {
     // truncated index int(t/dt) with the fraction in tw1[tr][ii]
     const int32_t* tq1;
     const float* tw1;
+    // dynamic mode with bf16 weights: 8-byte records {tq, bf16 wc | bf16 ws << 16}
+    // used instead of stab/rtab when non-null
+    const int2* stab2;  // [ns][ni]
+    const int2* rtab2;  // [nr][ni]
 };
 
 // Launchers (kirchhoff_kernels.cu).  All asynchronous on `stream`.
@@ -81,6 +85,9 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
 int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
                        const float* wrs, int4* stab, int4* rtab, uint32_t* srng, uint32_t* rrng,
                        cudaStream_t stream);
+// The same records with the weights rounded to bf16 (8 bytes each).
+int launch_pack_tables_bf16(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
+                            const float* wrs, int2* stab2, int2* rtab2, cudaStream_t stream);
 // How many float partial images launch_gather may use, and how many receiver
 // splits (partial images) it launches for this geometry.
 int64_t gather_partial_elems(const KirchDev& K);
@@ -123,6 +130,9 @@ struct kgb_kirchhoff {
     int4* rtab = nullptr;
     uint32_t* srng = nullptr;
     uint32_t* rrng = nullptr;
+    int2* stab2 = nullptr;     // bf16-weight records (when bf16_weights), see KirchDev
+    int2* rtab2 = nullptr;
+    bool bf16_weights = false;
     int32_t* tq1 = nullptr;    // single traveltime table (trace-major), see KirchDev
     float* tw1 = nullptr;
     float* dcorr = nullptr;    // scratch: correlated data for the adjoint, interleaved pairs (2 x ndata)
@@ -142,6 +152,7 @@ struct kgb_kirchhoff {
         K.spread_variant = spread_variant;
         K.stab = stab; K.rtab = rtab; K.srng = srng; K.rrng = rrng;
         K.tq1 = tq1; K.tw1 = tw1;
+        K.stab2 = bf16_weights ? stab2 : nullptr; K.rtab2 = bf16_weights ? rtab2 : nullptr;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

@@ -92,6 +92,14 @@ static int repack(kgb_kirchhoff* op) {
     if ((rc = launch_pack_tables(op->view(), op->wsc, op->wss, op->wrc, op->wrs, op->stab, op->rtab, op->srng,
                                  op->rrng, nullptr)))
         return rc;
+    if (op->bf16_weights) {
+        if (!op->stab2 && (rc = dev_alloc(&op->stab2, (size_t)op->ns * op->ni, "alloc bf16 source records"))) return rc;
+        if (!op->rtab2 && (rc = dev_alloc(&op->rtab2, (size_t)op->nr * op->ni, "alloc bf16 receiver records")))
+            return rc;
+        if ((rc = launch_pack_tables_bf16(op->view(), op->wsc, op->wss, op->wrc, op->wrs, op->stab2, op->rtab2,
+                                          nullptr)))
+            return rc;
+    }
     KGB_CUDA_TRY(cudaDeviceSynchronize());
     return KGB_OK;
 }
@@ -166,7 +174,8 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     cudaSetDevice(op->device);
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
                     op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
-                    op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng, op->tq1, op->tw1};
+                    op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng, op->tq1, op->tw1,
+                    op->stab2, op->rtab2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);
@@ -225,6 +234,23 @@ int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* ts, const dou
     (void)mins; (void)minr;
     op->trav_ready = true;
     return repack(op);
+}
+
+int kgb_kirchhoff_set_weight_precision(kgb_kirchhoff* op, int bf16) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (bf16 && !op->dynamic) return set_error(KGB_ERR_VALUE, "bf16 weights need a dynamic operator");
+    if (bf16 != 0 && bf16 != 1) return set_error(KGB_ERR_VALUE, "weight precision: 0 (float32) or 1 (bf16)");
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    const bool was = op->bf16_weights;
+    op->bf16_weights = bf16 == 1;
+    if (op->bf16_weights && !was) {
+        int rc = repack(op);  // builds the bf16 records if the tables are set
+        if (rc) {
+            op->bf16_weights = false;
+            return rc;
+        }
+    }
+    return KGB_OK;
 }
 
 int kgb_kirchhoff_set_traveltime_table(kgb_kirchhoff* op, const double* trav) {

@@ -21,6 +21,7 @@
 // Both directions are deterministic: the adjoint sums each image point in a
 // fixed order; the forward either accumulates exact 64-bit fixed point
 // (integer additions commute) or bins contributions per warp in lane order.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -95,9 +96,16 @@ struct Entry {
 // L2, so the caches keep what is reused: data traces, model, re-read rows).
 template <bool DYN, bool STREAM = false>
 __device__ __forceinline__ Entry load_entry(const int32_t* __restrict__ tq, const int4* __restrict__ tab,
-                                            size_t idx) {
+                                            size_t idx, const int2* __restrict__ tab2 = nullptr) {
     Entry e;
-    if (DYN) {
+    if (DYN && tab2) {
+        // bf16 weights: one 8-byte record (the branch is uniform: tab2 is a
+        // kernel argument)
+        const int2 v = STREAM ? __ldcs(tab2 + idx) : __ldg(tab2 + idx);
+        e.t = v.x;
+        e.c = __uint_as_float((unsigned)v.y << 16);
+        e.s = __uint_as_float((unsigned)v.y & 0xffff0000u);
+    } else if (DYN) {
         const int4 v = STREAM ? __ldcs(tab + idx) : __ldg(tab + idx);
         e.t = v.x;
         e.c = __int_as_float(v.y);
@@ -166,7 +174,7 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
 #pragma unroll
         for (int r = 0; r < kGatherRC; ++r) {
             re[r] = zero_entry();
-            if (r < nrc) re[r] = load_entry<DYN, true>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
+            if (r < nrc) re[r] = load_entry<DYN, true>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
         }
         float chunk = 0.f;
 #pragma unroll 2
@@ -175,7 +183,7 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
                 const int k = is - s_begin;
                 if (k < 64 ? !((smask >> k) & 1ull) : !in_range(K.srng, (size_t)is * ncol + col, iz)) continue;
             }
-            const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
+            const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
             if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
             const size_t pair0 = (size_t)is * K.nr + r0;
             const float2* __restrict__ drow = d2 + pair0 * nt;
@@ -303,12 +311,12 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
         const float v = __ldg(K.mv + ii) * S;
         if (v == 0.f) continue;  // zero model point: no contribution
         if (DYN && !in_range(K.srng, (size_t)is * ncol + colp, izp)) continue;  // source weight zero here
-        const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
+        const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
         if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
         // all R receiver records in flight before any is used
         Entry re[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) re[r] = r < nrr ? load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii) : zero_entry();
+        for (int r = 0; r < R; ++r) re[r] = r < nrr ? load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2) : zero_entry();
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (r < nrr) {
@@ -475,7 +483,7 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
                 v = __ldg(K.mv + ii);
                 if (DYN && !in_range(K.srng, (size_t)is * ncol + col, iz)) v = 0.f;
                 if (v != 0.f) {
-                    se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii);
+                    se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
                     if (DYN && se.c == 0.f && se.s == 0.f) v = 0.f;
                 }
             }
@@ -487,7 +495,7 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
                 float val = 0.f;  // stays 0 for a receiver outside its active range
                 if (inb && v != 0.f && (!DYN || in_range(K.rrng, (size_t)(r0 + r) * ncol + col, iz))) {
                     val = v;
-                    const Entry re = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii);
+                    const Entry re = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
                     s = se.t + re.t;
                     if (DYN) {
                         float wt = fmaf(se.c, re.c, se.s * re.s);
@@ -576,6 +584,14 @@ __global__ void pack_tables_kernel(const int32_t* __restrict__ tq, const float* 
                                    const float* __restrict__ ws, int4* __restrict__ tab, int64_t n) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
         tab[k] = make_int4(tq[k], __float_as_int(wc[k]), __float_as_int(ws[k]), 0);
+}
+
+__global__ void pack_tables_bf16_kernel(const int32_t* __restrict__ tq, const float* __restrict__ wc,
+                                        const float* __restrict__ ws, int2* __restrict__ tab, int64_t n) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(wc[k], ws[k]);  // .x = wc (low half), .y = ws
+        tab[k] = make_int2(tq[k], *reinterpret_cast<const int*>(&h));
+    }
 }
 
 // Per (row, depth column): smallest and one-past-largest depth with a
@@ -1274,6 +1290,15 @@ int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, co
     const int64_t ncol = K.ni / K.nz;
     range_kernel<<<nb, 256, 0, stream>>>(wsc, wss, srng, K.ns, ncol, K.nz);
     range_kernel<<<nb, 256, 0, stream>>>(wrc, wrs, rrng, K.nr, ncol, K.nz);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_pack_tables_bf16(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
+                            const float* wrs, int2* stab2, int2* rtab2, cudaStream_t stream) {
+    const int nb = 4 * num_sms();
+    pack_tables_bf16_kernel<<<nb, 256, 0, stream>>>(K.tsq, wsc, wss, stab2, (int64_t)K.ns * K.ni);
+    pack_tables_bf16_kernel<<<nb, 256, 0, stream>>>(K.trq, wrc, wrs, rtab2, (int64_t)K.nr * K.ni);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

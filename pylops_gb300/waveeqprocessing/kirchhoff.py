@@ -319,6 +319,16 @@ class Kirchhoff(LinearOperator):
         (one trace per warp), 2 warp-binned (two traces per warp)."""
         _native.check(_native.lib().kgb_kirchhoff_set_variant(self._h, int(variant)))
 
+    def set_weight_precision(self, precision: str = "float32") -> None:
+        """Store the dynamic weights as ``'bfloat16'`` (8-byte table records,
+        about 1e-3 relative change of the results) or ``'float32'``
+        (default; 16-byte records, the mode that matches the reference to
+        1e-5).  Traveltimes are exact in both."""
+        if precision not in ("float32", "bfloat16"):
+            raise ValueError("precision must be 'float32' or 'bfloat16'")
+        self._sync_tables()
+        _native.check(_native.lib().kgb_kirchhoff_set_weight_precision(self._h, int(precision == "bfloat16")))
+
     def autotune(self, variants=(0, 1, 2), reps: int = 3) -> dict:
         """Time the forward for each spread variant on this operator's
         tables (random model, CUDA events on the current stream), keep the
