@@ -94,13 +94,13 @@ struct Entry {
 
 // STREAM: the record is read once per application (evict-first in L1 and
 // L2, so the caches keep what is reused: data traces, model, re-read rows).
-template <bool DYN, bool STREAM = false>
+// HALF: bf16-weight records (8 bytes) from tab2 instead of tab.
+template <bool DYN, bool STREAM = false, bool HALF = false>
 __device__ __forceinline__ Entry load_entry(const int32_t* __restrict__ tq, const int4* __restrict__ tab,
                                             size_t idx, const int2* __restrict__ tab2 = nullptr) {
     Entry e;
-    if (DYN && tab2) {
-        // bf16 weights: one 8-byte record (the branch is uniform: tab2 is a
-        // kernel argument)
+    if (DYN && HALF) {
+        // bf16 weights: one 8-byte record
         const int2 v = STREAM ? __ldcs(tab2 + idx) : __ldg(tab2 + idx);
         e.t = v.x;
         e.c = __uint_as_float((unsigned)v.y << 16);
@@ -139,7 +139,7 @@ __device__ __forceinline__ bool in_range(const uint32_t* __restrict__ rng, size_
 // data is stored as interleaved pairs (d[it], d[it+1]) so one 8-byte load
 // feeds the interpolation.  The sum over traces has a fixed order.
 // ---------------------------------------------------------------------------
-template <bool DYN, bool GATE, bool NONNEG>
+template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
 __global__ void __launch_bounds__(kGatherThreads, 4)
 gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __restrict__ d2,
               float* __restrict__ out, int r_per_split) {
@@ -174,7 +174,7 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
 #pragma unroll
         for (int r = 0; r < kGatherRC; ++r) {
             re[r] = zero_entry();
-            if (r < nrc) re[r] = load_entry<DYN, true>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
+            if (r < nrc) re[r] = load_entry<DYN, true, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
         }
         float chunk = 0.f;
 #pragma unroll 2
@@ -183,7 +183,7 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
                 const int k = is - s_begin;
                 if (k < 64 ? !((smask >> k) & 1ull) : !in_range(K.srng, (size_t)is * ncol + col, iz)) continue;
             }
-            const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
+            const Entry se = load_entry<DYN, false, HALF>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
             if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
             const size_t pair0 = (size_t)is * K.nr + r0;
             const float2* __restrict__ drow = d2 + pair0 * nt;
@@ -265,7 +265,7 @@ __device__ __forceinline__ int spread_scale_exponent(float amax, int64_t ni) {
 // ~2^-42 of the bound) and added exactly, so the trace is independent of the
 // order in which threads arrive.  The finished traces are converted back to
 // float, convolved with the wavelet in shared memory and written once.
-template <bool DYN, bool GATE, bool NONNEG, int R>
+template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false>
 __global__ void __launch_bounds__(kSpreadThreads, 2)
 spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
               const float* __restrict__ h, int L, int Lpad, int nt_pad, int fuse) {
@@ -311,12 +311,12 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
         const float v = __ldg(K.mv + ii) * S;
         if (v == 0.f) continue;  // zero model point: no contribution
         if (DYN && !in_range(K.srng, (size_t)is * ncol + colp, izp)) continue;  // source weight zero here
-        const Entry se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
+        const Entry se = load_entry<DYN, false, HALF>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
         if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
         // all R receiver records in flight before any is used
         Entry re[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) re[r] = r < nrr ? load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2) : zero_entry();
+        for (int r = 0; r < R; ++r) re[r] = r < nrr ? load_entry<DYN, false, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2) : zero_entry();
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             if (r < nrr) {
@@ -441,7 +441,7 @@ __device__ __forceinline__ void warp_bin_add(float* trc, bool contrib, int it, f
 // in the next.  Otherwise lanes that share a bin are found with
 // __match_any_sync and summed by the lowest lane of the bin in lane order.
 // No atomics and a fixed summation order: deterministic.
-template <bool DYN, bool GATE, bool NONNEG, int RT>
+template <bool DYN, bool GATE, bool NONNEG, int RT, bool HALF = false>
 __global__ void __launch_bounds__(256)
 spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
                      const float* __restrict__ h, int L, int Lpad, int nt_pad, int fuse) {
@@ -483,7 +483,7 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
                 v = __ldg(K.mv + ii);
                 if (DYN && !in_range(K.srng, (size_t)is * ncol + col, iz)) v = 0.f;
                 if (v != 0.f) {
-                    se = load_entry<DYN>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
+                    se = load_entry<DYN, false, HALF>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
                     if (DYN && se.c == 0.f && se.s == 0.f) v = 0.f;
                 }
             }
@@ -495,7 +495,7 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
                 float val = 0.f;  // stays 0 for a receiver outside its active range
                 if (inb && v != 0.f && (!DYN || in_range(K.rrng, (size_t)(r0 + r) * ncol + col, iz))) {
                     val = v;
-                    const Entry re = load_entry<DYN>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
+                    const Entry re = load_entry<DYN, false, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
                     s = se.t + re.t;
                     if (DYN) {
                         float wt = fmaf(se.c, re.c, se.s * re.s);
@@ -617,12 +617,12 @@ __global__ void range_kernel(const float* __restrict__ wc, const float* __restri
 // ---------------------------------------------------------------------------
 // launch configuration
 // ---------------------------------------------------------------------------
-template <bool DYN, bool GATE, bool NONNEG>
+template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
 int gather_blocks_per_sm() {
     static int cached = 0;
     if (!cached) {
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gather_kernel<DYN, GATE, NONNEG>, kGatherThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gather_kernel<DYN, GATE, NONNEG, HALF>, kGatherThreads, 0);
         cached = nb > 0 ? nb : 1;
     }
     return cached;
@@ -648,12 +648,12 @@ int choose_split(int64_t blocks, int capacity, int nr) {
     return best;
 }
 
-template <bool DYN, bool GATE, bool NONNEG>
+template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
 int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* partial, int64_t cap,
                     cudaStream_t stream) {
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
-    const int capacity = num_sms() * gather_blocks_per_sm<DYN, GATE, NONNEG>();
+    const int capacity = num_sms() * gather_blocks_per_sm<DYN, GATE, NONNEG, HALF>();
     int split = choose_split(blocks, capacity, K.nr);
     if (partial == nullptr || cap < (int64_t)split * K.ni) split = 1;
     const int nchunks = (K.nr + kGatherRC - 1) / kGatherRC;
@@ -661,7 +661,7 @@ int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* part
     split = (nchunks + c_per - 1) / c_per;
     float* out = split > 1 ? partial : img;
     dim3 grid((unsigned)blocks, (unsigned)split);
-    gather_kernel<DYN, GATE, NONNEG><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
+    gather_kernel<DYN, GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
     KGB_CUDA_TRY(cudaGetLastError());
     if (split > 1) {
         const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
@@ -705,10 +705,10 @@ int launch_prepass(const KirchDev& K, const float* m, cudaStream_t stream) {
     return KGB_OK;
 }
 
-template <bool DYN, bool GATE, bool NONNEG, int R>
+template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false>
 int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                     const SpreadShape& sh, cudaStream_t stream, bool prepare_only) {
-    auto kern = spread_kernel<DYN, GATE, NONNEG, R>;
+    auto kern = spread_kernel<DYN, GATE, NONNEG, R, HALF>;
     if (prepare_only) {
         KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
         return KGB_OK;
@@ -723,10 +723,10 @@ int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h,
 }
 
 // Warp-binned variant: RT traces per warp, 8 warps per CTA.
-template <bool DYN, bool GATE, bool NONNEG, int RT>
+template <bool DYN, bool GATE, bool NONNEG, int RT, bool HALF = false>
 int spread_binned_launch_r(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                            cudaStream_t stream, bool prepare_only) {
-    auto kern = spread_binned_kernel<DYN, GATE, NONNEG, RT>;
+    auto kern = spread_binned_kernel<DYN, GATE, NONNEG, RT, HALF>;
     const int Lpad = (L + 3) & ~3;
     const int nt_pad = (K.nt + 3) & ~3;
     const int warps = 8;
@@ -747,7 +747,7 @@ int spread_binned_launch_r(const KirchDev& K, const float* m, float* y, const fl
     return KGB_OK;
 }
 
-template <bool DYN, bool GATE, bool NONNEG>
+template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
 int spread_launch_t(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                     cudaStream_t stream, bool prepare_only) {
     const int Lpad = (L + 3) & ~3;
@@ -756,34 +756,38 @@ int spread_launch_t(const KirchDev& K, const float* m, float* y, const float* h,
     const bool fits2 = (size_t)(Lpad + 16 * (size_t)nt_pad) * 4 <= 227 * 1024;
     int rc = KGB_OK;
     if (prepare_only) {
-        if (fits1) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, true);
-        if (!rc && fits2) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, true);
+        if (fits1) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 1, HALF>(K, m, y, h, L, fuse, stream, true);
+        if (!rc && fits2) rc = spread_binned_launch_r<DYN, GATE, NONNEG, 2, HALF>(K, m, y, h, L, fuse, stream, true);
         if (rc) return rc;
     } else if (K.spread_variant == 2 && fits2) {
-        return spread_binned_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, stream, false);
+        return spread_binned_launch_r<DYN, GATE, NONNEG, 2, HALF>(K, m, y, h, L, fuse, stream, false);
     } else if (K.spread_variant == 1 && fits1) {
-        return spread_binned_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, stream, false);
+        return spread_binned_launch_r<DYN, GATE, NONNEG, 1, HALF>(K, m, y, h, L, fuse, stream, false);
     }
     const SpreadShape sh = spread_shape(K, L);
     switch (sh.R) {
-        case 8: return spread_launch_r<DYN, GATE, NONNEG, 8>(K, m, y, h, L, fuse, sh, stream, prepare_only);
-        case 4: return spread_launch_r<DYN, GATE, NONNEG, 4>(K, m, y, h, L, fuse, sh, stream, prepare_only);
-        case 2: return spread_launch_r<DYN, GATE, NONNEG, 2>(K, m, y, h, L, fuse, sh, stream, prepare_only);
-        case 1: return spread_launch_r<DYN, GATE, NONNEG, 1>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        case 8: return spread_launch_r<DYN, GATE, NONNEG, 8, HALF>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        case 4: return spread_launch_r<DYN, GATE, NONNEG, 4, HALF>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        case 2: return spread_launch_r<DYN, GATE, NONNEG, 2, HALF>(K, m, y, h, L, fuse, sh, stream, prepare_only);
+        case 1: return spread_launch_r<DYN, GATE, NONNEG, 1, HALF>(K, m, y, h, L, fuse, sh, stream, prepare_only);
         default:
             return set_error(KGB_ERR_NOT_IMPLEMENTED, "spread: nt=%d too long for one trace in shared memory", K.nt);
     }
 }
 
-template <bool DYN, bool GATE>
+template <bool DYN, bool GATE, bool HALF = false>
 int spread_dispatch_nn(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                        cudaStream_t stream, bool prep) {
-    if (K.nonneg) return spread_launch_t<DYN, GATE, true>(K, m, y, h, L, fuse, stream, prep);
-    return spread_launch_t<DYN, GATE, false>(K, m, y, h, L, fuse, stream, prep);
+    if (K.nonneg) return spread_launch_t<DYN, GATE, true, HALF>(K, m, y, h, L, fuse, stream, prep);
+    return spread_launch_t<DYN, GATE, false, HALF>(K, m, y, h, L, fuse, stream, prep);
 }
 
 int spread_dispatch(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y, const float* h,
                     int L, bool fuse, cudaStream_t stream, bool prep) {
+    if (dynamic && K.stab2) {
+        if (gate) return spread_dispatch_nn<true, true, true>(K, m, y, h, L, fuse, stream, prep);
+        return spread_dispatch_nn<true, false, true>(K, m, y, h, L, fuse, stream, prep);
+    }
     if (dynamic) {
         if (gate) return spread_dispatch_nn<true, true>(K, m, y, h, L, fuse, stream, prep);
         return spread_dispatch_nn<true, false>(K, m, y, h, L, fuse, stream, prep);
@@ -1208,7 +1212,10 @@ size_t wavelet_smem(int L, int nt) {
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
     int bps;
-    if (dynamic) bps = gate ? (K.nonneg ? gather_blocks_per_sm<true, true, true>() : gather_blocks_per_sm<true, true, false>())
+    if (dynamic && K.stab2)
+        bps = gate ? (K.nonneg ? gather_blocks_per_sm<true, true, true, true>() : gather_blocks_per_sm<true, true, false, true>())
+                   : (K.nonneg ? gather_blocks_per_sm<true, false, true, true>() : gather_blocks_per_sm<true, false, false, true>());
+    else if (dynamic) bps = gate ? (K.nonneg ? gather_blocks_per_sm<true, true, true>() : gather_blocks_per_sm<true, true, false>())
                             : (K.nonneg ? gather_blocks_per_sm<true, false, true>() : gather_blocks_per_sm<true, false, false>());
     else bps = K.nonneg ? gather_blocks_per_sm<false, false, true>() : gather_blocks_per_sm<false, false, false>();
     int split = choose_split(blocks, num_sms() * bps, K.nr);
@@ -1228,6 +1235,14 @@ int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, fl
     if (K.tq1) {
         if (K.tw1) return gather1_launch_t<false>(K, d2, img, partial, cap, stream);
         return gather1_launch_t<true>(K, d2, img, partial, cap, stream);
+    }
+    if (dynamic && K.stab2) {
+        if (gate) {
+            if (K.nonneg) return gather_launch_t<true, true, true, true>(K, d2, img, partial, cap, stream);
+            return gather_launch_t<true, true, false, true>(K, d2, img, partial, cap, stream);
+        }
+        if (K.nonneg) return gather_launch_t<true, false, true, true>(K, d2, img, partial, cap, stream);
+        return gather_launch_t<true, false, false, true>(K, d2, img, partial, cap, stream);
     }
     if (dynamic) {
         if (gate) {
@@ -1259,6 +1274,11 @@ int prepare_kernels(const KirchDev& K0, int L) {
         for (int dyn = 0; dyn < 2; ++dyn)
             for (int gate = 0; gate < 2; ++gate)
                 if ((rc = spread_dispatch(K, dyn, gate, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
+        // bf16-weight instantiations (dispatched on a non-null stab2; nothing is launched here)
+        KirchDev Kh = K;
+        Kh.stab2 = reinterpret_cast<const int2*>(&K);  // a non-null marker only
+        for (int gate = 0; gate < 2; ++gate)
+            if ((rc = spread_dispatch(Kh, 1, gate, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     }
     if ((rc = spread1_dispatch_t<true>(K, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     if ((rc = spread1_dispatch_t<false>(K, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
