@@ -631,7 +631,7 @@ def run_single(args):
         "hbm_fraction": round(B / step / 1e9 / peaks["hbm_gbs"], 4),
         "roofline": {"bound": "hbm", "kernel": "gather1 (adjoint)", "achieved": round(ach, 1),
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(ach / peaks["hbm_gbs"], 4),
-                     "traffic": None},
+                     "traffic": _traffic("gather1_adjoint", "single_table_2d_300x800_64x%d_nt1501" % nr)},
         "e2e": {"value": round(B / e2e / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * (K.ni + K.shape[0]),
                 "d2h_bytes_per_step": 4 * (K.ni + K.shape[0])},
         "gpu_launches": args.steps * (K.info()["kernels_forward"] + K.info()["kernels_adjoint"]),
