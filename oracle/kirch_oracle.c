@@ -1,7 +1,7 @@
 /*
  * C restatement of the reference's Numba CPU engine for the Kirchhoff path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA kernels at sizes the
+ * TEST INFRASTRUCTURE ONLY: the oracle for the CUDA kernels at sizes the
  * NumPy oracle cannot reach, and the timed CPU baseline of bench.py.  The
  * product never links or calls this file.
  *

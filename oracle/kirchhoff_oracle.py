@@ -1,6 +1,6 @@
 """FP64 NumPy oracle for the Kirchhoff demigration/migration path.
 
-TEST INFRASTRUCTURE ONLY.  This module is the checker: only ``tests/``,
+TEST INFRASTRUCTURE ONLY.  This module is the oracle: only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may import it.
 The product (``pylops_gb300``) never imports or calls anything in ``oracle/``.
 

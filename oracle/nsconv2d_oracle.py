@@ -1,6 +1,6 @@
 """Float64 restatement of the 2-D non-stationary convolution
 (``pylops/signalprocessing/nonstatconvolve2d.py:177-272``) -- test
-infrastructure: the checker for ``kgb_nsconv2d_apply``, never the thing
+infrastructure: the oracle for ``kgb_nsconv2d_apply``, never the thing
 measured or shipped.  Pinned to golden vectors the reference produced
 (``tests/golden/nsconv2d.npz``)."""
 

@@ -12,7 +12,7 @@ inverse square root of the diagonal of ``K^H K``), and LSQR
 (``pylops/optimization/cls_basic.py:711-1351``) runs on ``K P`` from
 ``z0 = x0 / p`` until the data residual reaches ``tol ||d||``.  Plain LSQR
 from zero is both the fallback (used when the warm start does not lower the
-residual) and the judge of the result (data residual and model error).
+residual) and the measure of the result (data residual and model error).
 
 PyLops has no counterpart of the network; the surrounding solve is the
 reference's ``lsqr(Kop * Diagonal(p), d, x0=z0)``.

@@ -1,6 +1,6 @@
 """Source-sharded operator and CGLS with two gloo ranks on the CPU; each
 rank's local operator is the float64 oracle of its sources (the GPU operator
-takes its place on a GPU machine).  The sharded forward must reproduce the
+takes its place on a GPU).  The sharded forward must reproduce the
 unsharded rows, the adjoint the unsharded image, and CGLS the unsharded
 iterates, to float64 rounding."""
 

@@ -2,7 +2,7 @@
 workload (2-D dynamic eikonal, v(z) = 1500 + 0.6 z), a U-Net trained on
 operator-generated pairs must bring LSQR to the same 1e-2 data residual in
 fewer operator applications than plain LSQR from zero, with a model error
-no worse; plain LSQR stays the judge of the residual."""
+no worse; the residual is recomputed for both, as plain LSQR measures it."""
 
 import numpy as np
 import pytest
