@@ -145,10 +145,13 @@ def cpu_baseline(K, m, d, target_s=10.0):
     build()
     C = COracle(K, _padded_wavelet(K))
     _cpu_step(C, m, d, 0, 1)  # first call: thread start-up, page faults
+    # the oracle runs sources in parallel: size the sample from a call with
+    # one source per host core
+    k = max(1, min(K.ns, os.cpu_count() or 1))
     t0 = time.perf_counter()
-    _cpu_step(C, m, d, 0, 1)
-    t1 = time.perf_counter() - t0
-    nsamp = int(max(1, min(K.ns, target_s / max(t1, 1e-3))))
+    _cpu_step(C, m, d, 0, k)
+    tk = time.perf_counter() - t0
+    nsamp = int(max(1, min(K.ns, k * max(1, int(target_s / max(tk, 1e-3))))))
     t0 = time.perf_counter()
     yc, xc = _cpu_step(C, m, d, 0, nsamp)
     dt_s = time.perf_counter() - t0
@@ -932,6 +935,8 @@ def run_lsm(args):
     clocks.start()
     out, ctx = experiment.run(n_train=args.lsm_train, n_test=args.steps, steps=args.lsm_steps, batch=8,
                               niter=600, variants=("plain", "warm", "learned", "psf"),
+                              stage2_pairs=args.lsm_stage2_pairs, stage2_steps=args.lsm_stage2_steps,
+                              steps_net=args.lsm_net_steps,
                               log=lambda *a: print(*a, file=sys.stderr, flush=True), return_objects=True)
     clk = clocks.stop()
     op, tests = ctx["op"], ctx["tests"]
@@ -955,12 +960,15 @@ def run_lsm(args):
         "warmup": 1, "ms_per_step": round(v["learned"]["seconds_median"] * 1e3, 2), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 operator, bf16 network", "data": "synthetic",
         "config": {"workload": "learned_lsm_2d_eikonal_dyn_256x512_48x256_nt1201", "train_pairs": args.lsm_train,
-                   "train_steps": args.lsm_steps, "batch": 8, "held_out_models": args.steps, "tol": 1e-2,
+                   "train_steps": args.lsm_steps, "stage2_residual_pairs": args.lsm_stage2_pairs,
+                   "stage2_steps": args.lsm_stage2_steps, "max_network_directions": 1 + args.lsm_net_steps,
+                   "batch": 8, "held_out_models": args.steps, "tol": 1e-2,
                    "l2": "operator tables (478 MB) larger than L2"},
         "plain_lsqr": v["plain"], "warm_start_only": v["warm"], "learned": v["learned"],
         "psf_image_domain_warm_start": v["psf"],
         "speedup_vs_plain_median": round(v["learned"]["speedup_vs_plain_median"], 3),
         "train": {k: out.get(k) for k in ("pairs_seconds", "train_seconds", "train_loss_first", "train_loss_last",
+                                          "stage2_pairs_seconds", "stage2_train_seconds", "stage2_loss_last",
                                           "inference_ms")},
         "e2e": {"value": round(e2e, 4), "unit": "s", "h2d_bytes_per_step": int(op.shape[0] * 4),
                 "d2h_bytes_per_step": int(op.shape[1] * 4)},
@@ -1004,6 +1012,9 @@ def main():
     ap.add_argument("--lsqr-iters", type=int, default=30, help="LSQR iterations after the timed steps (0: none)")
     ap.add_argument("--lsm-train", type=int, default=4096)
     ap.add_argument("--lsm-steps", type=int, default=3000)
+    ap.add_argument("--lsm-stage2-pairs", type=int, default=2048)
+    ap.add_argument("--lsm-stage2-steps", type=int, default=1500)
+    ap.add_argument("--lsm-net-steps", type=int, default=6, help="at most this many network directions after the warm start")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--cgls-iters", type=int, default=20)
     args = ap.parse_args()

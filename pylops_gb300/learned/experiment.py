@@ -21,7 +21,8 @@ import time
 
 import numpy as np
 
-from .lsm import LearnedLSM, illumination_diagonal, make_pairs, point_spread_functions, random_reflectivity, train
+from .lsm import (LearnedLSM, illumination_diagonal, make_pairs, make_residual_pairs, point_spread_functions,
+                  random_reflectivity, train)
 from .unet import UNet
 
 __all__ = ["lsm_operator", "run"]
@@ -62,7 +63,8 @@ def _summary(infos, errs):
 def run(n_train: int = 4096, n_test: int = 64, steps: int = 2000, batch: int = 8, lr: float = 1e-3,
         tol: float = 1e-2, niter: int = 600, seed: int = 0, levels: int = 4, base: int = 32,
         variants=("plain", "warm", "learned"), steps_net: int = 4, step_ratio: float = 0.7, log=print,
-        op=None, net_state: dict = None, save_net: str = None, return_objects: bool = False):
+        op=None, net_state: dict = None, save_net: str = None, return_objects: bool = False,
+        stage2_pairs: int = 0, stage2_steps: int = 0):
     import torch
 
     out = {"config": {"n_train": n_train, "n_test": n_test, "steps": steps, "batch": batch, "lr": lr,
@@ -93,6 +95,24 @@ def run(n_train: int = 4096, n_test: int = 64, steps: int = 2000, batch: int = 8
         out["train_loss_last"] = float(np.mean(losses[-20:]))
         log(f"trained {steps} steps in {out['train_seconds']:.1f} s, loss {out['train_loss_first']:.3f} -> "
             f"{out['train_loss_last']:.3f}")
+        if stage2_pairs and stage2_steps:
+            # second stage: residual pairs after the network's warm start, mixed
+            # with the first-stage pairs, training continued at a lower rate
+            t0 = time.perf_counter()
+            X2, E2 = make_residual_pairs(op, net, stage2_pairs, seed=seed + 1)
+            X = torch.cat([X[:stage2_pairs], X2])
+            M = torch.cat([M[:stage2_pairs], E2])
+            del X2, E2
+            torch.cuda.synchronize()
+            out["stage2_pairs_seconds"] = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            losses2 = train(net, X, M, steps=stage2_steps, batch=batch, lr=lr / 3, seed=seed + 1,
+                            log_every=max(stage2_steps // 5, 1))
+            torch.cuda.synchronize()
+            out["stage2_train_seconds"] = time.perf_counter() - t0
+            out["stage2_loss_last"] = float(np.mean(losses2[-20:]))
+            log(f"stage 2: {stage2_pairs} residual pairs in {out['stage2_pairs_seconds']:.1f} s, "
+                f"{stage2_steps} steps in {out['stage2_train_seconds']:.1f} s, loss {out['stage2_loss_last']:.3f}")
         del X, M
         if save_net:
             np.savez(save_net, **net.state_dict())
@@ -172,13 +192,16 @@ def main(argv=None):
     ap.add_argument("--variants", default="plain,warm,learned")
     ap.add_argument("--net-steps", type=int, default=4)
     ap.add_argument("--step-ratio", type=float, default=0.7)
+    ap.add_argument("--stage2-pairs", type=int, default=0)
+    ap.add_argument("--stage2-steps", type=int, default=0)
     ap.add_argument("--out", default=None)
     ap.add_argument("--save-net", default=None, help="write the trained network (.npz)")
     ap.add_argument("--load-net", default=None, help="skip training, load this network (.npz)")
     a = ap.parse_args(argv)
     r = run(n_train=a.train, n_test=a.test, steps=a.steps, batch=a.batch, lr=a.lr, niter=a.niter, seed=a.seed,
             variants=tuple(a.variants.split(",")), steps_net=a.net_steps, step_ratio=a.step_ratio,
-            net_state=dict(np.load(a.load_net)) if a.load_net else None, save_net=a.save_net)
+            net_state=dict(np.load(a.load_net)) if a.load_net else None, save_net=a.save_net,
+            stage2_pairs=a.stage2_pairs, stage2_steps=a.stage2_steps)
     s = json.dumps(r, indent=1)
     print(s)
     if a.out:

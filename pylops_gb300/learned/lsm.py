@@ -30,8 +30,8 @@ import numpy as np
 from .. import _native
 from .unet import UNet
 
-__all__ = ["random_reflectivity", "make_pairs", "train", "illumination_diagonal", "point_spread_functions",
-           "LearnedLSM", "SolveInfo"]
+__all__ = ["random_reflectivity", "make_pairs", "make_residual_pairs", "train", "illumination_diagonal",
+           "point_spread_functions", "LearnedLSM", "SolveInfo"]
 
 
 def random_reflectivity(nx: int, nz: int, rng: np.random.Generator, dx: float = 5.0, dz: float = 5.0,
@@ -94,6 +94,38 @@ def make_pairs(op, n: int, seed: int = 0, generator=random_reflectivity, **kw):
         op.apply_into(M[i].reshape(-1), d)
         op.apply_into(d, X[i].reshape(-1), adjoint=True)
     return X, M
+
+
+def make_residual_pairs(op, net: UNet, n: int, seed: int = 1, generator=random_reflectivity, **kw):
+    """Second-stage pairs for the network steps of the solve: for a fresh
+    model m with data d = K m, the network's warm start x1 = alpha UNet(K^H d)
+    (alpha the least-squares fit of K x1 to d) leaves the error e = m - x1;
+    the pair is (K^H K e, e / rms(e)) -- the gradient the solve feeds the
+    network after its warm start, and what the network should return.
+    Float32 CUDA tensors (n, nx, nz)."""
+    import torch
+
+    nx, nz = op.dims
+    rng = np.random.default_rng(seed)
+    X = torch.empty((n, nx, nz), dtype=torch.float32, device="cuda")
+    E = torch.empty((n, nx, nz), dtype=torch.float32, device="cuda")
+    d = torch.empty(op.shape[0], dtype=torch.float32, device="cuda")
+    ku = torch.empty_like(d)
+    img = torch.empty(op.ni, dtype=torch.float32, device="cuda")
+    for i in range(n):
+        m = torch.from_numpy(_normalised(generator(nx, nz, rng, **kw))).to("cuda").reshape(-1)
+        op.apply_into(m, d)
+        op.apply_into(d, img, adjoint=True)
+        u = net.forward(img.view(nx, nz)).reshape(-1).contiguous()
+        op.apply_into(u, ku)
+        kk = float(torch.dot(ku.double(), ku.double()))
+        alpha = float(torch.dot(ku.double(), d.double())) / kk if kk > 0 else 0.0
+        e = m - alpha * u
+        rms = float(torch.sqrt(torch.mean(e.double() ** 2)))
+        E[i] = (e / rms if rms > 0 else e).view(nx, nz)
+        op.apply_into(e.contiguous(), d)
+        op.apply_into(d, X[i].reshape(-1), adjoint=True)
+    return X, E
 
 
 def train(net: UNet, X, M, steps: int, batch: int = 8, lr: float = 1e-3, lr_final: float = 1e-4, seed: int = 0,
