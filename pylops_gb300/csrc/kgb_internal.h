@@ -56,6 +56,9 @@ struct KirchDev {
     // which the row's weight is exactly zero, packed lo | hi << 16
     const uint32_t* srng;  // [ns][ncol]
     const uint32_t* rrng;  // [nr][ncol]
+    // union of the ranges of each group of 8 consecutive receivers, packed
+    // the same way: a point outside it has zero weight for all 8
+    const uint32_t* grng;  // [ceil(nr/8)][ncol]
     // single traveltime table (one entry per image point and trace, mode
     // 'byot' with trav of shape (ni, ns*nr)): tq1[tr][ii] is the fixed-point
     // sample count (tw1 == nullptr) or, for tables with negative times, the
@@ -85,6 +88,8 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
 int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
                        const float* wrs, int4* stab, int4* rtab, uint32_t* srng, uint32_t* rrng,
                        cudaStream_t stream);
+// Union ranges of groups of 8 receivers from the per-receiver ranges.
+int launch_group_ranges(const uint32_t* rrng, uint32_t* grng, int nr, int64_t ncol, cudaStream_t stream);
 // The same records with the weights rounded to bf16 (8 bytes each).
 int launch_pack_tables_bf16(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
                             const float* wrs, int2* stab2, int2* rtab2, cudaStream_t stream);
@@ -130,6 +135,7 @@ struct kgb_kirchhoff {
     int4* rtab = nullptr;
     uint32_t* srng = nullptr;
     uint32_t* rrng = nullptr;
+    uint32_t* grng = nullptr;
     int2* stab2 = nullptr;     // bf16-weight records (when bf16_weights), see KirchDev
     int2* rtab2 = nullptr;
     bool bf16_weights = false;
@@ -150,7 +156,7 @@ struct kgb_kirchhoff {
         K.vscale = vscale; K.izmin = izmin;
         K.nonneg = nonneg ? 1 : 0; K.wmax = wmax; K.mv = mv; K.absmax = absmax;
         K.spread_variant = spread_variant;
-        K.stab = stab; K.rtab = rtab; K.srng = srng; K.rrng = rrng;
+        K.stab = stab; K.rtab = rtab; K.srng = srng; K.rrng = rrng; K.grng = grng;
         K.tq1 = tq1; K.tw1 = tw1;
         K.stab2 = bf16_weights ? stab2 : nullptr; K.rtab2 = bf16_weights ? rtab2 : nullptr;
         return K;

@@ -92,6 +92,9 @@ static int repack(kgb_kirchhoff* op) {
     if ((rc = launch_pack_tables(op->view(), op->wsc, op->wss, op->wrc, op->wrs, op->stab, op->rtab, op->srng,
                                  op->rrng, nullptr)))
         return rc;
+    if (!op->grng && (rc = dev_alloc(&op->grng, (size_t)((op->nr + 7) / 8) * ncol, "alloc receiver group ranges")))
+        return rc;
+    if ((rc = launch_group_ranges(op->rrng, op->grng, op->nr, ncol, nullptr))) return rc;
     if (op->bf16_weights) {
         if (!op->stab2 && (rc = dev_alloc(&op->stab2, (size_t)op->ns * op->ni, "alloc bf16 source records"))) return rc;
         if (!op->rtab2 && (rc = dev_alloc(&op->rtab2, (size_t)op->nr * op->ni, "alloc bf16 receiver records")))
@@ -175,7 +178,7 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
                     op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
                     op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng, op->tq1, op->tw1,
-                    op->stab2, op->rtab2};
+                    op->stab2, op->rtab2, op->grng};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);

@@ -294,25 +294,10 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     for (int r = 0; r < R; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
     __syncthreads();
     const int64_t ncol = K.ni / K.nz;
-    // depth column and depth of this thread's point, advanced incrementally
-    int64_t col = tid / K.nz;
-    int iz = tid - (int)(col * K.nz);
-    const int64_t stride_col = (int64_t)blockDim.x / K.nz;
-    const int stride_iz = blockDim.x - (int)(stride_col * K.nz);
-    for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
-        const int64_t colp = col;
-        const int izp = iz;
-        col += stride_col;
-        iz += stride_iz;
-        if (iz >= K.nz) {
-            iz -= K.nz;
-            ++col;
-        }
-        const float v = __ldg(K.mv + ii) * S;
-        if (v == 0.f) continue;  // zero model point: no contribution
-        if (DYN && !in_range(K.srng, (size_t)is * ncol + colp, izp)) continue;  // source weight zero here
+    // one image point (index ii, depth izp in column colp, scaled value v)
+    auto point = [&](int64_t ii, int64_t colp, int izp, float v) {
         const Entry se = load_entry<DYN, false, HALF>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
-        if (DYN && se.c == 0.f && se.s == 0.f) continue;  // source outside the angle aperture
+        if (DYN && se.c == 0.f && se.s == 0.f) return;  // source outside the angle aperture
         // all R receiver records in flight before any is used
         Entry re[R];
 #pragma unroll
@@ -337,6 +322,43 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
                     atomicAdd(a + 1, (unsigned long long)__float2ll_rn(v1));
                 }
             }
+        }
+    };
+    if (DYN && R == 8 && K.grng) {
+        // a warp per depth column, over the depths where both the source
+        // and at least one receiver of this group of 8 have a nonzero weight
+        const int lane = tid & 31;
+        const int nw = blockDim.x >> 5;
+        for (int64_t c = tid >> 5; c < ncol; c += nw) {
+            const uint32_t a = __ldg(K.srng + (size_t)is * ncol + c);
+            const uint32_t b = __ldg(K.grng + (size_t)g * ncol + c);
+            const int lo = max((int)(a & 0xffffu), (int)(b & 0xffffu));
+            const int hi = min((int)(a >> 16), (int)(b >> 16));
+            for (int iz = lo + lane; iz < hi; iz += 32) {
+                const int64_t ii = c * K.nz + iz;
+                const float v = __ldg(K.mv + ii) * S;
+                if (v != 0.f) point(ii, c, iz, v);
+            }
+        }
+    } else {
+        // depth column and depth of this thread's point, advanced incrementally
+        int64_t col = tid / K.nz;
+        int iz = tid - (int)(col * K.nz);
+        const int64_t stride_col = (int64_t)blockDim.x / K.nz;
+        const int stride_iz = blockDim.x - (int)(stride_col * K.nz);
+        for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
+            const int64_t colp = col;
+            const int izp = iz;
+            col += stride_col;
+            iz += stride_iz;
+            if (iz >= K.nz) {
+                iz -= K.nz;
+                ++col;
+            }
+            const float v = __ldg(K.mv + ii) * S;
+            if (v == 0.f) continue;  // zero model point: no contribution
+            if (DYN && !in_range(K.srng, (size_t)is * ncol + colp, izp)) continue;  // source weight zero here
+            point(ii, colp, izp, v);
         }
     }
     __syncthreads();
@@ -591,6 +613,29 @@ __global__ void pack_tables_bf16_kernel(const int32_t* __restrict__ tq, const fl
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         const __nv_bfloat162 h = __floats2bfloat162_rn(wc[k], ws[k]);  // .x = wc (low half), .y = ws
         tab[k] = make_int2(tq[k], *reinterpret_cast<const int*>(&h));
+    }
+}
+
+// Union of the depth ranges of the receivers 8g .. 8g+7 for each column
+// (empty ranges, lo = hi, do not widen it).
+__global__ void group_range_kernel(const uint32_t* __restrict__ rrng, uint32_t* __restrict__ grng, int nr,
+                                   int64_t ncol) {
+    const int ng = (nr + 7) / 8;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < (int64_t)ng * ncol;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int g = (int)(k / ncol);
+        const int64_t col = k - (int64_t)g * ncol;
+        int lo = 1 << 30, hi = 0;
+        for (int r = 8 * g; r < min(nr, 8 * g + 8); ++r) {
+            const uint32_t v = rrng[(size_t)r * ncol + col];
+            const int l = (int)(v & 0xffffu), h = (int)(v >> 16);
+            if (h > l) {
+                lo = min(lo, l);
+                hi = max(hi, h);
+            }
+        }
+        if (hi == 0) lo = 0;
+        grng[k] = (uint32_t)lo | ((uint32_t)hi << 16);
     }
 }
 
@@ -1319,6 +1364,12 @@ int launch_pack_tables_bf16(const KirchDev& K, const float* wsc, const float* ws
     const int nb = 4 * num_sms();
     pack_tables_bf16_kernel<<<nb, 256, 0, stream>>>(K.tsq, wsc, wss, stab2, (int64_t)K.ns * K.ni);
     pack_tables_bf16_kernel<<<nb, 256, 0, stream>>>(K.trq, wrc, wrs, rtab2, (int64_t)K.nr * K.ni);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_group_ranges(const uint32_t* rrng, uint32_t* grng, int nr, int64_t ncol, cudaStream_t stream) {
+    group_range_kernel<<<4 * num_sms(), 256, 0, stream>>>(rrng, grng, nr, ncol);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
