@@ -144,6 +144,8 @@ __global__ void __launch_bounds__(kGatherThreads, 4)
 gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __restrict__ d2,
               float* __restrict__ out, int r_per_split) {
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // lanes of this warp that stay (blockDim is a multiple of 32)
+    const unsigned live = __ballot_sync(0xffffffffu, ii < K.ni);
     if (ii >= K.ni) return;
     // blockIdx.y selects a range of receivers: every split sweeps all sources,
     // which are re-streamed per receiver chunk anyway, so splitting adds no
@@ -169,6 +171,12 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
     }
     float total = 0.f;
     for (int r0 = r_begin; r0 < r_end; r0 += kGatherRC) {
+        // r0 is a multiple of 8: the warp skips the chunk when none of its
+        // receivers has a nonzero weight at any of the warp's points (a
+        // warp-uniform branch; a per-thread one costs register spills)
+        if (DYN && kGatherRC == 8 && K.grng &&
+            !__any_sync(live, in_range(K.grng, (size_t)(r0 >> 3) * ncol + col, iz)))
+            continue;
         Entry re[kGatherRC];
         const int nrc = min(kGatherRC, r_end - r0);
 #pragma unroll
