@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "fir.cuh"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -85,19 +86,22 @@ absmax_kernel(const float* __restrict__ m, int64_t n, unsigned* __restrict__ out
 template <int R>
 __global__ void __launch_bounds__(256)
 batch_spread_kernel(const Prob* __restrict__ probs, const SpreadItem* __restrict__ items, const float* __restrict__ m,
-                    float* __restrict__ y, const unsigned* __restrict__ absmax, int64_t max_ni, int nt_pad_max) {
+                    float* __restrict__ y, const unsigned* __restrict__ absmax, int64_t max_ni, int nt_pad_max,
+                    int span_max) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const SpreadItem it_ = items[blockIdx.x];
     const Prob P = probs[it_.p];
     const int nt_pad = (P.nt + 3) & ~3;
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    // the finished trace, zero-padded for fir_same, then the padded taps
     float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad_max);
-    float* hs = ftr + nt_pad_max;
+    float* hs = ftr + span_max;
     const int tid = threadIdx.x;
     const int r0 = it_.g * R;
     const int nrr = min(R, P.nr - r0);
     for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
-    for (int k = tid; k < P.L; k += blockDim.x) hs[k] = P.h[k];
+    for (int k = tid; k < fir_lpad(P.L); k += blockDim.x) hs[k] = k < P.L ? P.h[k] : 0.f;
+    for (int k = tid; k < fir_span(P.L, P.nt); k += blockDim.x) ftr[k] = 0.f;
     const float amax = __uint_as_float(*absmax);
     int e = 0;
     if (amax > 0.f) {
@@ -136,18 +140,16 @@ batch_spread_kernel(const Prob* __restrict__ probs, const SpreadItem* __restrict
     }
     __syncthreads();
     const float invS = ldexpf(1.f, -e);
-    const int c = (P.L - 1) / 2;
+    float* xt = ftr + fir_q(P.L);
     for (int r = 0; r < nrr; ++r) {
-        for (int n = tid; n < P.nt; n += blockDim.x) ftr[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        for (int n = tid; n < P.nt; n += blockDim.x) xt[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        __syncthreads();
+        // convolved trace into this receiver's spent accumulator row
+        float* os = reinterpret_cast<float*>(acc + (size_t)r * nt_pad);
+        fir_same(hs, ftr, os, P.L, P.nt, tid, blockDim.x);
         __syncthreads();
         float* __restrict__ yrow = y + P.d_off + ((size_t)it_.is * P.nr + r0 + r) * P.nt;
-        for (int n = tid; n < P.nt; n += blockDim.x) {
-            const int kmin = max(0, n + c - (P.nt - 1));
-            const int kmax = min(P.L - 1, n + c);
-            float o = 0.f;
-            for (int k = kmin; k <= kmax; ++k) o = fmaf(hs[k], ftr[n + c - k], o);
-            yrow[n] = o;
-        }
+        for (int n = tid; n < P.nt; n += blockDim.x) yrow[n] = os[n];
         __syncthreads();
     }
 }
@@ -157,11 +159,11 @@ batch_spread_kernel(const Prob* __restrict__ probs, const SpreadItem* __restrict
 // written as interleaved pairs (d[t], d[t+1]) for the gather.
 __global__ void __launch_bounds__(256)
 batch_correlate_kernel(const Prob* __restrict__ probs, int nprob, const float* __restrict__ d, float2* __restrict__ dc,
-                       int64_t ntraces, int nt_pad_max, int Lpad_max) {
-    extern __shared__ float smem[];
+                       int64_t ntraces, int span_max, int Lpad_max) {
+    extern __shared__ __align__(16) float smem[];
     float* gs = smem;
-    float* xs = smem + Lpad_max;
-    float* os = xs + nt_pad_max;
+    float* xp = smem + Lpad_max;  // zero-padded trace
+    float* os = xp + span_max;
     for (int64_t tr = blockIdx.x; tr < ntraces; tr += gridDim.x) {
         // problem of this trace: binary search over the trace offsets
         int lo = 0, hi = nprob - 1;
@@ -172,19 +174,14 @@ batch_correlate_kernel(const Prob* __restrict__ probs, int nprob, const float* _
         }
         const Prob& P = probs[lo];
         __syncthreads();
-        for (int k = threadIdx.x; k < P.L; k += blockDim.x) gs[k] = P.hflip[k];
+        for (int k = threadIdx.x; k < fir_lpad(P.L); k += blockDim.x) gs[k] = k < P.L ? P.hflip[k] : 0.f;
         const int64_t local = tr - P.tr_off;
         const float* xrow = d + P.d_off + local * P.nt;
-        for (int n = threadIdx.x; n < P.nt; n += blockDim.x) xs[n] = xrow[n];
+        const int q = fir_q(P.L);
+        for (int i = threadIdx.x; i < fir_span(P.L, P.nt); i += blockDim.x)
+            xp[i] = (i >= q && i < q + P.nt) ? xrow[i - q] : 0.f;
         __syncthreads();
-        const int c = (P.L - 1) / 2;
-        for (int n = threadIdx.x; n < P.nt; n += blockDim.x) {
-            const int kmin = max(0, n + c - (P.nt - 1));
-            const int kmax = min(P.L - 1, n + c);
-            float acc = 0.f;
-            for (int k = kmin; k <= kmax; ++k) acc = fmaf(gs[k], xs[n + c - k], acc);
-            os[n] = acc;
-        }
+        fir_same(gs, xp, os, P.L, P.nt, threadIdx.x, blockDim.x);
         __syncthreads();
         float2* yrow = dc + P.d_off + local * P.nt;
         for (int n = threadIdx.x; n < P.nt; n += blockDim.x)
@@ -390,7 +387,8 @@ struct kgb_batch {
     std::vector<kgb_kirchhoff*> ops;
     int nprob = 0;
     int64_t nm = 0, nd = 0, ntraces = 0, max_ni = 0;
-    int nt_pad_max = 0, Lpad_max = 0;
+    int nt_pad_max = 0, Lpad_max = 0;  // Lpad_max: padded taps (fir_lpad)
+    int span_max = 0, out_max = 0;     // padded trace and FIR output floats
     int R = 8;  // receivers per forward item (autotuned)
     Prob* d_probs = nullptr;
     SpreadItem* d_spread[4] = {nullptr, nullptr, nullptr, nullptr};  // R = 1, 2, 4, 8
@@ -420,8 +418,10 @@ namespace {
 int r_index(int R) { return R == 1 ? 0 : R == 2 ? 1 : R == 4 ? 2 : 3; }
 
 size_t spread_smem(const kgb_batch* b, int R) {
-    return (size_t)R * b->nt_pad_max * 8 + (size_t)(b->nt_pad_max + b->Lpad_max) * 4;
+    return (size_t)R * b->nt_pad_max * 8 + (size_t)(b->span_max + b->Lpad_max) * 4;
 }
+
+size_t correlate_smem(const kgb_batch* b) { return (size_t)(b->Lpad_max + b->span_max + b->out_max) * 4; }
 
 int batch_forward(kgb_batch* b, const float* m, float* y, cudaStream_t s) {
     KGB_CUDA_TRY(cudaMemsetAsync(b->absmax, 0, sizeof(unsigned), s));
@@ -429,19 +429,19 @@ int batch_forward(kgb_batch* b, const float* m, float* y, cudaStream_t s) {
     const int ri = r_index(b->R);
     const size_t smem = spread_smem(b, b->R);
     switch (b->R) {
-        case 1: batch_spread_kernel<1><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max); break;
-        case 2: batch_spread_kernel<2><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max); break;
-        case 4: batch_spread_kernel<4><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max); break;
-        default: batch_spread_kernel<8><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max); break;
+        case 1: batch_spread_kernel<1><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
+        case 2: batch_spread_kernel<2><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
+        case 4: batch_spread_kernel<4><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
+        default: batch_spread_kernel<8><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
     }
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
 
 int batch_adjoint(kgb_batch* b, const float* d, float* img, cudaStream_t s) {
-    const size_t smem = (size_t)(b->Lpad_max + 2 * b->nt_pad_max) * 4;
+    const size_t smem = correlate_smem(b);
     const int64_t nb = std::min<int64_t>(b->ntraces, 8 * 152);
-    batch_correlate_kernel<<<(unsigned)nb, 256, smem, s>>>(b->d_probs, b->nprob, d, b->dc, b->ntraces, b->nt_pad_max,
+    batch_correlate_kernel<<<(unsigned)nb, 256, smem, s>>>(b->d_probs, b->nprob, d, b->dc, b->ntraces, b->span_max,
                                                           b->Lpad_max);
     batch_gather_kernel<<<b->n_gather, kTile, 0, s>>>(b->d_probs, b->d_gather, b->dc, img);
     KGB_CUDA_TRY(cudaGetLastError());
@@ -556,7 +556,9 @@ int kgb_batch_create(kgb_batch** out, kgb_kirchhoff* const* ops, int nops) {
         b->ntraces += op->npair();
         b->max_ni = std::max(b->max_ni, op->ni);
         b->nt_pad_max = std::max(b->nt_pad_max, (op->nt + 3) & ~3);
-        b->Lpad_max = std::max(b->Lpad_max, (op->L + 3) & ~3);
+        b->Lpad_max = std::max(b->Lpad_max, fir_lpad(op->L));
+        b->span_max = std::max(b->span_max, fir_span(op->L, op->nt));
+        b->out_max = std::max(b->out_max, fir_out(op->nt));
     }
     int rc = KGB_OK;
     do {
@@ -597,7 +599,7 @@ int kgb_batch_create(kgb_batch** out, kgb_kirchhoff* const* ops, int nops) {
         KGB_CUDA_TRY(cudaFuncSetAttribute(batch_spread_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)spread_smem(b, 4)));
         KGB_CUDA_TRY(cudaFuncSetAttribute(batch_spread_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem8));
         KGB_CUDA_TRY(cudaFuncSetAttribute(batch_correlate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)((b->Lpad_max + 2 * b->nt_pad_max) * 4)));
+                                          (int)correlate_smem(b)));
     } while (0);
     if (rc) {
         kgb_batch_destroy(b);

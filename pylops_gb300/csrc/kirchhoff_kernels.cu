@@ -26,6 +26,7 @@
 
 #include <algorithm>
 
+#include "fir.cuh"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -276,11 +277,12 @@ __device__ __forceinline__ int spread_scale_exponent(float amax, int64_t ni) {
 template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false>
 __global__ void __launch_bounds__(kSpreadThreads, 2)
 spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
-              const float* __restrict__ h, int L, int Lpad, int nt_pad, int fuse) {
+              const float* __restrict__ h, int L, int nt_pad, int fuse) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    // the finished trace, zero-padded for fir_same, then the padded taps
     float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad);
-    float* hs = ftr + nt_pad;
+    float* hs = ftr + fir_span(L, K.nt);
     const int tid = threadIdx.x;
     const int nt = K.nt;
     const int ngroups = (K.nr + R - 1) / R;
@@ -293,13 +295,16 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     const int r0 = g * R;
     const int nrr = min(R, K.nr - r0);
     for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
-    if (fuse)
-        for (int k = tid; k < L; k += blockDim.x) hs[k] = h[k];
+    if (fuse) {
+        for (int k = tid; k < fir_lpad(L); k += blockDim.x) hs[k] = k < L ? h[k] : 0.f;
+        for (int k = tid; k < fir_span(L, K.nt); k += blockDim.x) ftr[k] = 0.f;
+    }
     const int e = spread_scale_exponent(__uint_as_float(*K.absmax) * K.wmax, K.ni);
     const float S = ldexpf(1.f, e);
-    int izmin[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) izmin[r] = (GATE && r < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + r) : 0;
+    // first depth of each receiver's gate, in shared memory (read as a warp
+    // broadcast; held in registers it costs spills)
+    __shared__ int izmin[R];
+    if (tid < R) izmin[tid] = (GATE && tid < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + tid) : 0;
     __syncthreads();
     const int64_t ncol = K.ni / K.nz;
     // one image point (index ii, depth izp in column colp, scaled value v)
@@ -371,23 +376,21 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     }
     __syncthreads();
     const float invS = ldexpf(1.f, -e);
-    const int c = (L - 1) / 2;
+    float* xt = fuse ? ftr + fir_q(L) : ftr;
     for (int r = 0; r < nrr; ++r) {
-        for (int n = tid; n < nt; n += blockDim.x) ftr[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        for (int n = tid; n < nt; n += blockDim.x) xt[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
         __syncthreads();
-        float* __restrict__ yrow = y + ((size_t)is * K.nr + r0 + r) * nt;
-        for (int n = tid; n < nt; n += blockDim.x) {
-            float o;
-            if (fuse) {
-                const int kmin = max(0, n + c - (nt - 1));
-                const int kmax = min(L - 1, n + c);
-                o = 0.f;
-                for (int k = kmin; k <= kmax; ++k) o = fmaf(hs[k], ftr[n + c - k], o);
-            } else {
-                o = ftr[n];
-            }
-            __stcs(yrow + n, o);
+        // the convolved trace goes to this receiver's accumulator row, which
+        // is no longer needed (2 * nt_pad >= fir_out(nt) floats)
+        const float* o = xt;
+        if (fuse) {
+            float* os = reinterpret_cast<float*>(acc + (size_t)r * nt_pad);
+            fir_same(hs, ftr, os, L, nt, tid, blockDim.x);
+            __syncthreads();
+            o = os;
         }
+        float* __restrict__ yrow = y + ((size_t)is * K.nr + r0 + r) * nt;
+        for (int n = tid; n < nt; n += blockDim.x) __stcs(yrow + n, o[n]);
         __syncthreads();
     }
 }
@@ -565,39 +568,35 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
 }
 
 // ---------------------------------------------------------------------------
-// 'same'-mode FIR along time: o[n] = sum_k g[k] x[n + c - k], c = (L-1)/2.
-// One block per trace (grid-stride), trace and taps staged in shared memory.
-// interleave = 1 writes (o[n], o[n+1]) pairs for the gather; g == nullptr
-// copies the trace (o = x).
+// 'same'-mode FIR along time: o[n] = sum_k g[k] x[n + c - k], c = (L-1)/2
+// (fir_same).  One block per trace (grid-stride); taps and the zero-padded
+// trace staged in shared memory.  interleave = 1 writes (o[n], o[n+1])
+// pairs for the gather; g == nullptr copies the trace (o = x).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, int nt,
-               const float* __restrict__ g, int L, int Lpad, int interleave) {
-    extern __shared__ float smem[];
+               const float* __restrict__ g, int L, int interleave) {
+    extern __shared__ __align__(16) float smem[];
+    const int Lp = fir_lpad(L);
+    const int span = fir_span(L, nt);
+    const int q = fir_q(L);
     float* gs = smem;
-    float* xs = smem + Lpad;
-    float* os = xs + ((nt + 3) & ~3);
-    if (g)
-        for (int k = threadIdx.x; k < L; k += blockDim.x) gs[k] = g[k];
-    const int c = (L - 1) / 2;
+    float* xp = gs + Lp;
+    float* os = xp + span;
+    if (g) {
+        for (int k = threadIdx.x; k < Lp; k += blockDim.x) gs[k] = k < L ? g[k] : 0.f;
+        for (int i = threadIdx.x; i < span; i += blockDim.x) xp[i] = 0.f;
+    }
     for (int64_t tr = blockIdx.x; tr < ntr; tr += gridDim.x) {
         __syncthreads();
         const float* xrow = x + tr * nt;
-        for (int n = threadIdx.x; n < nt; n += blockDim.x) xs[n] = xrow[n];
+        float* dst = g ? xp + q : os;
+        for (int n = threadIdx.x; n < nt; n += blockDim.x) dst[n] = __ldcs(xrow + n);
         __syncthreads();
-        for (int n = threadIdx.x; n < nt; n += blockDim.x) {
-            float acc;
-            if (g) {
-                const int kmin = max(0, n + c - (nt - 1));
-                const int kmax = min(L - 1, n + c);
-                acc = 0.f;
-                for (int k = kmin; k <= kmax; ++k) acc = fmaf(gs[k], xs[n + c - k], acc);
-            } else {
-                acc = xs[n];
-            }
-            os[n] = acc;
+        if (g) {
+            fir_same(gs, xp, os, L, nt, threadIdx.x, blockDim.x);
+            __syncthreads();
         }
-        __syncthreads();
         if (interleave) {
             float2* yrow = reinterpret_cast<float2*>(y) + tr * nt;
             for (int n = threadIdx.x; n < nt; n += blockDim.x)
@@ -727,16 +726,15 @@ int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* part
 struct SpreadShape {
     int R;
     size_t smem;
-    int Lpad, nt_pad;
+    int nt_pad;
 };
 
 // Receivers per CTA: as many as keep two CTAs per SM, fewer when the grid
 // would not fill the GPU.
 SpreadShape spread_shape(const KirchDev& K, int L) {
     SpreadShape sh;
-    sh.Lpad = (L + 3) & ~3;
     sh.nt_pad = (K.nt + 3) & ~3;
-    const size_t fixed = (size_t)(sh.nt_pad + sh.Lpad) * sizeof(float);
+    const size_t fixed = (size_t)(fir_span(L, K.nt) + fir_lpad(L)) * sizeof(float);
     const size_t budget2 = 110 * 1024, budget1 = 220 * 1024;
     int R = 8;
     auto need = [&](int r) { return fixed + (size_t)r * sh.nt_pad * 8; };
@@ -770,7 +768,7 @@ int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h,
     if (rc) return rc;
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (int64_t)K.ns * ((K.nr + R - 1) / R);
-    kern<<<(unsigned)blocks, kSpreadThreads, sh.smem, stream>>>(K, fp, y, h, L, sh.Lpad, sh.nt_pad, fuse ? 1 : 0);
+    kern<<<(unsigned)blocks, kSpreadThreads, sh.smem, stream>>>(K, fp, y, h, L, sh.nt_pad, fuse ? 1 : 0);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -1075,8 +1073,9 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
                int nt_pad, int fuse) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    // the finished trace, zero-padded for fir_same, then the padded taps
     float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad);
-    float* hs = ftr + nt_pad;
+    float* hs = ftr + fir_span(L, K.nt);
     const int tid = threadIdx.x;
     const int nt = K.nt;
     const int nsnr = K.ns * K.nr;
@@ -1084,8 +1083,10 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
     if (tr0 >= nsnr) return;
     const int ntr = min(R, nsnr - tr0);
     for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
-    if (fuse)
-        for (int k = tid; k < L; k += blockDim.x) hs[k] = h[k];
+    if (fuse) {
+        for (int k = tid; k < fir_lpad(L); k += blockDim.x) hs[k] = k < L ? h[k] : 0.f;
+        for (int k = tid; k < fir_span(L, K.nt); k += blockDim.x) ftr[k] = 0.f;
+    }
     // |v (1 - w)| <= 2 |v| on the negative-time path: one bit of headroom
     const int e = spread_scale_exponent(__uint_as_float(*K.absmax) * (FIXED ? 1.f : 2.f), K.ni);
     const float S = ldexpf(1.f, e);
@@ -1115,23 +1116,20 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
     }
     __syncthreads();
     const float invS = ldexpf(1.f, -e);
-    const int c = (L - 1) / 2;
+    float* xt = fuse ? ftr + fir_q(L) : ftr;
     for (int r = 0; r < ntr; ++r) {
-        for (int n = tid; n < nt; n += blockDim.x) ftr[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        for (int n = tid; n < nt; n += blockDim.x) xt[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
         __syncthreads();
-        float* __restrict__ yrow = y + (size_t)(tr0 + r) * nt;
-        for (int n = tid; n < nt; n += blockDim.x) {
-            float o;
-            if (fuse) {
-                const int kmin = max(0, n + c - (nt - 1));
-                const int kmax = min(L - 1, n + c);
-                o = 0.f;
-                for (int k = kmin; k <= kmax; ++k) o = fmaf(hs[k], ftr[n + c - k], o);
-            } else {
-                o = ftr[n];
-            }
-            __stcs(yrow + n, o);
+        // convolved trace into this trace's spent accumulator row
+        const float* o = xt;
+        if (fuse) {
+            float* os = reinterpret_cast<float*>(acc + (size_t)r * nt_pad);
+            fir_same(hs, ftr, os, L, nt, tid, blockDim.x);
+            __syncthreads();
+            o = os;
         }
+        float* __restrict__ yrow = y + (size_t)(tr0 + r) * nt;
+        for (int n = tid; n < nt; n += blockDim.x) __stcs(yrow + n, o[n]);
         __syncthreads();
     }
 }
@@ -1186,7 +1184,7 @@ int spread1_dispatch_t(const KirchDev& K, const float* m, float* y, const float*
     } else if (!prep && K.spread_variant != 0 && binned_fits) {
         return spread1_binned_launch<FIXED>(K, m, y, h, L, fuse, stream, false);
     }
-    const size_t fixed = (size_t)(nt_pad + Lpad) * sizeof(float);
+    const size_t fixed = (size_t)(fir_span(L, K.nt) + fir_lpad(L)) * sizeof(float);
     auto need = [&](int r) { return fixed + (size_t)r * nt_pad * 8; };
     int R = 8;
     while (R > 1 && need(R) > 110 * 1024) R >>= 1;
@@ -1256,8 +1254,7 @@ int gather1_launch_t(const KirchDev& K, const float2* d2, float* img, float* par
 }
 
 size_t wavelet_smem(int L, int nt) {
-    const int Lpad = (L + 3) & ~3;
-    return (size_t)(Lpad + 2 * ((nt + 3) & ~3)) * sizeof(float);
+    return (size_t)(fir_lpad(L) + fir_span(L, nt) + fir_out(nt)) * sizeof(float);
 }
 
 }  // namespace
@@ -1344,12 +1341,14 @@ int prepare_kernels(const KirchDev& K0, int L) {
 int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L, int interleave,
                    cudaStream_t stream) {
     if (ntr <= 0 || nt <= 0) return KGB_OK;
-    const int Lpad = (L + 3) & ~3;
     const size_t smem = wavelet_smem(L, nt);
     if (smem > 227 * 1024)
         return set_error(KGB_ERR_NOT_IMPLEMENTED, "wavelet: nt=%d too long for shared memory", nt);
-    const int64_t blocks = std::min<int64_t>(ntr, 8 * num_sms());
-    wavelet_kernel<<<(unsigned)blocks, 256, smem, stream>>>(x, y, ntr, nt, g, L, Lpad, interleave);
+    // threads: enough for the output blocks of one trace, whole warps
+    const int nblk = fir_out(nt) / kFirJ;
+    const int threads = g ? std::min(256, (nblk + 31) / 32 * 32) : 256;
+    const int64_t blocks = std::min<int64_t>(ntr, 16 * num_sms());
+    wavelet_kernel<<<(unsigned)blocks, threads, smem, stream>>>(x, y, ntr, nt, g, L, interleave);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
