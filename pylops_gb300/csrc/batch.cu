@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "fir.cuh"
+#include "fixed_acc.cuh"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -86,31 +87,25 @@ absmax_kernel(const float* __restrict__ m, int64_t n, unsigned* __restrict__ out
 template <int R>
 __global__ void __launch_bounds__(256)
 batch_spread_kernel(const Prob* __restrict__ probs, const SpreadItem* __restrict__ items, const float* __restrict__ m,
-                    float* __restrict__ y, const unsigned* __restrict__ absmax, int64_t max_ni, int nt_pad_max,
+                    float* __restrict__ y, const unsigned* __restrict__ absmax, int nt_pad_max,
                     int span_max) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const SpreadItem it_ = items[blockIdx.x];
     const Prob P = probs[it_.p];
     const int nt_pad = (P.nt + 3) & ~3;
+    // R trace rows of 64-bit fixed-point bins (fixed_add layout)
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    uint32_t* acc32 = reinterpret_cast<uint32_t*>(smem_raw);
     // the finished trace, zero-padded for fir_same, then the padded taps
     float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad_max);
     float* hs = ftr + span_max;
     const int tid = threadIdx.x;
     const int r0 = it_.g * R;
     const int nrr = min(R, P.nr - r0);
-    for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
+    fixed_clear(acc32, R, nt_pad, tid, blockDim.x);
     for (int k = tid; k < fir_lpad(P.L); k += blockDim.x) hs[k] = k < P.L ? P.h[k] : 0.f;
     for (int k = tid; k < fir_span(P.L, P.nt); k += blockDim.x) ftr[k] = 0.f;
-    const float amax = __uint_as_float(*absmax);
-    int e = 0;
-    if (amax > 0.f) {
-        int ex;
-        frexpf(amax, &ex);
-        int nb = 0;
-        while (nb < 40 && ((int64_t)1 << nb) <= max_ni) ++nb;
-        e = max(-126, min(61 - nb - ex, 126));
-    }
+    const int e = fixed_scale_exponent(__uint_as_float(*absmax));
     const float S = ldexpf(1.f, e);
     __syncthreads();
     const float* __restrict__ mp = m + P.m_off;
@@ -131,9 +126,9 @@ batch_spread_kernel(const Prob* __restrict__ probs, const SpreadItem* __restrict
                     const float w = fp_frac(s, t, P.F);
                     const float v1 = v * w;
                     const float v0 = v - v1;
-                    unsigned long long* a = acc + (size_t)r * nt_pad + t;
-                    atomicAdd(a, (unsigned long long)__float2ll_rn(v0));
-                    atomicAdd(a + 1, (unsigned long long)__float2ll_rn(v1));
+                    uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
+                    fixed_add(row, nt_pad, t, __float2int_rn(v0));
+                    fixed_add(row, nt_pad, t + 1, __float2int_rn(v1));
                 }
             }
         }
@@ -142,10 +137,10 @@ batch_spread_kernel(const Prob* __restrict__ probs, const SpreadItem* __restrict
     const float invS = ldexpf(1.f, -e);
     float* xt = ftr + fir_q(P.L);
     for (int r = 0; r < nrr; ++r) {
-        for (int n = tid; n < P.nt; n += blockDim.x) xt[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        for (int n = tid; n < P.nt; n += blockDim.x) xt[n] = (float)fixed_get(acc32 + (size_t)r * 2 * nt_pad, nt_pad, n) * invS;
         __syncthreads();
         // convolved trace into this receiver's spent accumulator row
-        float* os = reinterpret_cast<float*>(acc + (size_t)r * nt_pad);
+        float* os = reinterpret_cast<float*>(acc32 + (size_t)r * 2 * nt_pad);
         fir_same(hs, ftr, os, P.L, P.nt, tid, blockDim.x);
         __syncthreads();
         float* __restrict__ yrow = y + P.d_off + ((size_t)it_.is * P.nr + r0 + r) * P.nt;
@@ -386,7 +381,7 @@ using namespace kgb::bt;
 struct kgb_batch {
     std::vector<kgb_kirchhoff*> ops;
     int nprob = 0;
-    int64_t nm = 0, nd = 0, ntraces = 0, max_ni = 0;
+    int64_t nm = 0, nd = 0, ntraces = 0;
     int nt_pad_max = 0, Lpad_max = 0;  // Lpad_max: padded taps (fir_lpad)
     int span_max = 0, out_max = 0;     // padded trace and FIR output floats
     int R = 8;  // receivers per forward item (autotuned)
@@ -429,10 +424,10 @@ int batch_forward(kgb_batch* b, const float* m, float* y, cudaStream_t s) {
     const int ri = r_index(b->R);
     const size_t smem = spread_smem(b, b->R);
     switch (b->R) {
-        case 1: batch_spread_kernel<1><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
-        case 2: batch_spread_kernel<2><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
-        case 4: batch_spread_kernel<4><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
-        default: batch_spread_kernel<8><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->max_ni, b->nt_pad_max, b->span_max); break;
+        case 1: batch_spread_kernel<1><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->nt_pad_max, b->span_max); break;
+        case 2: batch_spread_kernel<2><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->nt_pad_max, b->span_max); break;
+        case 4: batch_spread_kernel<4><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->nt_pad_max, b->span_max); break;
+        default: batch_spread_kernel<8><<<b->n_spread[ri], 256, smem, s>>>(b->d_probs, b->d_spread[ri], m, y, b->absmax, b->nt_pad_max, b->span_max); break;
     }
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
@@ -554,7 +549,6 @@ int kgb_batch_create(kgb_batch** out, kgb_kirchhoff* const* ops, int nops) {
         b->nm += op->ni;
         b->nd += op->ndata();
         b->ntraces += op->npair();
-        b->max_ni = std::max(b->max_ni, op->ni);
         b->nt_pad_max = std::max(b->nt_pad_max, (op->nt + 3) & ~3);
         b->Lpad_max = std::max(b->Lpad_max, fir_lpad(op->L));
         b->span_max = std::max(b->span_max, fir_span(op->L, op->nt));

@@ -69,6 +69,11 @@ struct KirchDev {
     // used instead of stab/rtab when non-null
     const int2* stab2;  // [ns][ni]
     const int2* rtab2;  // [nr][ni]
+    // fixed-point spread (variant 0) only: receiver groups [g0, g1) of this
+    // launch, and whether it first computes mv and absmax (prepass = 0 when
+    // an earlier launch on an ordered stream already did)
+    int g0, g1;
+    int prepass;
 };
 
 // Launchers (kirchhoff_kernels.cu).  All asynchronous on `stream`.
@@ -88,6 +93,12 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
 int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, const float* wrc,
                        const float* wrs, int4* stab, int4* rtab, uint32_t* srng, uint32_t* rrng,
                        cudaStream_t stream);
+// Receivers per group of the fixed-point spread (variant 0) for this
+// operator, 0 when the forward does not run that kernel (binned variants,
+// single traveltime table, traces too long for shared memory).
+int spread_group_size(const KirchDev& K, int L);
+// The forward's prepass alone (mv = m * 2/v or m, and absmax).
+int launch_spread_prepass(const KirchDev& K, bool dynamic, const float* m, cudaStream_t stream);
 // Union ranges of groups of 8 receivers from the per-receiver ranges.
 int launch_group_ranges(const uint32_t* rrng, uint32_t* grng, int nr, int64_t ncol, cudaStream_t stream);
 // The same records with the weights rounded to bf16 (8 bytes each).
@@ -147,6 +158,12 @@ struct kgb_kirchhoff {
     float* m_stage = nullptr;  // device staging for the host-buffer entry points
     float* d_stage = nullptr;
     cudaStream_t stream = nullptr;  // used by the host-buffer entry points
+    // host-buffer entry points: a second compute stream and a copy stream
+    // (created on first use) and the events that order the chunks
+    static constexpr int kHostChunks = 4;
+    cudaStream_t stream2 = nullptr;
+    cudaStream_t cstream = nullptr;
+    cudaEvent_t ev[kHostChunks + 1] = {};
     int device = 0;
 
     kgb::KirchDev view() const {
@@ -159,6 +176,7 @@ struct kgb_kirchhoff {
         K.stab = stab; K.rtab = rtab; K.srng = srng; K.rrng = rrng; K.grng = grng;
         K.tq1 = tq1; K.tw1 = tw1;
         K.stab2 = bf16_weights ? stab2 : nullptr; K.rtab2 = bf16_weights ? rtab2 : nullptr;
+        K.g0 = 0; K.g1 = 1 << 30; K.prepass = 1;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

@@ -182,6 +182,10 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);
+    if (op->stream2) cudaStreamDestroy(op->stream2);
+    if (op->cstream) cudaStreamDestroy(op->cstream);
+    for (cudaEvent_t e : op->ev)
+        if (e) cudaEventDestroy(e);
     cudaSetDevice(dev);
     delete op;
     return KGB_OK;
@@ -480,29 +484,91 @@ static int ensure_stage(kgb_kirchhoff* op) {
     return KGB_OK;
 }
 
+static int ensure_streams(kgb_kirchhoff* op) {
+    if (!op->stream2) KGB_CUDA_TRY(cudaStreamCreateWithFlags(&op->stream2, cudaStreamNonBlocking));
+    if (!op->cstream) KGB_CUDA_TRY(cudaStreamCreateWithFlags(&op->cstream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : op->ev)
+        if (!e) KGB_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return KGB_OK;
+}
+
+// Forward with host buffers.  With the fixed-point spread the receiver
+// groups run as kHostChunks launches alternating between two streams (a
+// launch fills the tail of the previous one) and each chunk's traces go to
+// the host on a copy stream while the next chunks compute.  Every trace is
+// computed exactly as in one launch.
 int kgb_kirchhoff_forward_host(kgb_kirchhoff* op, const float* m_host, float* d_host) {
     int rc = check_ready(op);
     if (rc) return rc;
     if (!m_host || !d_host) return set_error(KGB_ERR_VALUE, "forward_host: null pointer");
     KGB_CUDA_TRY(cudaSetDevice(op->device));
     if ((rc = ensure_stage(op))) return rc;
-    KGB_CUDA_TRY(cudaMemcpyAsync(op->m_stage, m_host, (size_t)op->ni * 4, cudaMemcpyHostToDevice, op->stream));
-    if ((rc = kgb_kirchhoff_forward(op, op->m_stage, op->d_stage, op->stream))) return rc;
-    KGB_CUDA_TRY(cudaMemcpyAsync(d_host, op->d_stage, (size_t)op->ndata() * 4, cudaMemcpyDeviceToHost, op->stream));
-    KGB_CUDA_TRY(cudaStreamSynchronize(op->stream));
+    cudaStream_t s = op->stream;
+    KGB_CUDA_TRY(cudaMemcpyAsync(op->m_stage, m_host, (size_t)op->ni * 4, cudaMemcpyHostToDevice, s));
+    kgb::KirchDev K = op->view();
+    const int R = spread_group_size(K, op->L);
+    const size_t pitch = (size_t)op->nr * op->nt * 4;
+    if (R == 0 || pitch > ((size_t)1 << 30)) {
+        if ((rc = kgb_kirchhoff_forward(op, op->m_stage, op->d_stage, s))) return rc;
+        KGB_CUDA_TRY(cudaMemcpyAsync(d_host, op->d_stage, (size_t)op->ndata() * 4, cudaMemcpyDeviceToHost, s));
+        KGB_CUDA_TRY(cudaStreamSynchronize(s));
+        return KGB_OK;
+    }
+    if ((rc = ensure_streams(op))) return rc;
+    if ((rc = launch_spread_prepass(K, op->dynamic, op->m_stage, s))) return rc;
+    KGB_CUDA_TRY(cudaEventRecord(op->ev[0], s));
+    KGB_CUDA_TRY(cudaStreamWaitEvent(op->stream2, op->ev[0], 0));
+    const int ngroups = (op->nr + R - 1) / R;
+    const int nch = std::min(kgb_kirchhoff::kHostChunks, ngroups);
+    K.prepass = 0;
+    for (int c = 0; c < nch; ++c) {
+        K.g0 = (int)((int64_t)c * ngroups / nch);
+        K.g1 = (int)((int64_t)(c + 1) * ngroups / nch);
+        cudaStream_t sc = (c & 1) ? op->stream2 : s;
+        if ((rc = launch_spread(K, op->dynamic, op->has_gate, op->m_stage, op->d_stage, op->h_dev, op->L, true, sc)))
+            return rc;
+        KGB_CUDA_TRY(cudaEventRecord(op->ev[1 + c], sc));
+        KGB_CUDA_TRY(cudaStreamWaitEvent(op->cstream, op->ev[1 + c], 0));
+        const int r_lo = K.g0 * R, r_hi = std::min(op->nr, K.g1 * R);
+        const size_t off = (size_t)r_lo * op->nt;
+        KGB_CUDA_TRY(cudaMemcpy2DAsync(d_host + off, pitch, op->d_stage + off, pitch, (size_t)(r_hi - r_lo) * op->nt * 4,
+                                       (size_t)op->ns, cudaMemcpyDeviceToHost, op->cstream));
+    }
+    KGB_CUDA_TRY(cudaStreamSynchronize(op->cstream));
     return KGB_OK;
 }
 
+// Adjoint with host buffers: the data go to the device in kHostChunks
+// source blocks on a copy stream and each block is correlated with the
+// wavelet as soon as it lands; the gather runs once all are in.
 int kgb_kirchhoff_adjoint_host(kgb_kirchhoff* op, const float* d_host, float* m_host) {
     int rc = check_ready(op);
     if (rc) return rc;
     if (!m_host || !d_host) return set_error(KGB_ERR_VALUE, "adjoint_host: null pointer");
     KGB_CUDA_TRY(cudaSetDevice(op->device));
-    if ((rc = ensure_stage(op))) return rc;
-    KGB_CUDA_TRY(cudaMemcpyAsync(op->d_stage, d_host, (size_t)op->ndata() * 4, cudaMemcpyHostToDevice, op->stream));
-    if ((rc = kgb_kirchhoff_adjoint(op, op->d_stage, op->m_stage, op->stream))) return rc;
-    KGB_CUDA_TRY(cudaMemcpyAsync(m_host, op->m_stage, (size_t)op->ni * 4, cudaMemcpyDeviceToHost, op->stream));
-    KGB_CUDA_TRY(cudaStreamSynchronize(op->stream));
+    if ((rc = ensure_stage(op)) || (rc = ensure_streams(op))) return rc;
+    cudaStream_t s = op->stream;
+    // the copy stream may only overwrite the staging buffer after the
+    // previous work on it is done
+    KGB_CUDA_TRY(cudaEventRecord(op->ev[0], s));
+    KGB_CUDA_TRY(cudaStreamWaitEvent(op->cstream, op->ev[0], 0));
+    const int nch = std::min(kgb_kirchhoff::kHostChunks, op->ns);
+    for (int c = 0; c < nch; ++c) {
+        const int s0 = (int)((int64_t)c * op->ns / nch), s1 = (int)((int64_t)(c + 1) * op->ns / nch);
+        const size_t off = (size_t)s0 * op->nr * op->nt;
+        const int64_t ntr = (int64_t)(s1 - s0) * op->nr;
+        KGB_CUDA_TRY(cudaMemcpyAsync(op->d_stage + off, d_host + off, (size_t)ntr * op->nt * 4, cudaMemcpyHostToDevice,
+                                     op->cstream));
+        KGB_CUDA_TRY(cudaEventRecord(op->ev[1 + c], op->cstream));
+        KGB_CUDA_TRY(cudaStreamWaitEvent(s, op->ev[1 + c], 0));
+        if ((rc = launch_wavelet(op->d_stage + off, op->dcorr + 2 * off, ntr, op->nt, op->hflip_dev, op->L, 1, s)))
+            return rc;
+    }
+    if ((rc = launch_gather(op->view(), op->dynamic, op->has_gate, op->dcorr, op->m_stage, op->partial,
+                            op->partial_elems, s)))
+        return rc;
+    KGB_CUDA_TRY(cudaMemcpyAsync(m_host, op->m_stage, (size_t)op->ni * 4, cudaMemcpyDeviceToHost, s));
+    KGB_CUDA_TRY(cudaStreamSynchronize(s));
     return KGB_OK;
 }
 

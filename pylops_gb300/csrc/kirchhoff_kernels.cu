@@ -27,6 +27,7 @@
 #include <algorithm>
 
 #include "fir.cuh"
+#include "fixed_acc.cuh"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -253,25 +254,14 @@ spread_prepass_kernel(const KirchDev K, const float* __restrict__ m) {
     if ((threadIdx.x & 31) == 0 && amax > 0.f) atomicMax(K.absmax, __float_as_uint(amax));
 }
 
-// Exponent e of the fixed-point scale 2^e: |v| 2^e < 2^(61 - ceil(log2(ni+1)))
-// for every contribution bound |v| <= amax, so ni of them sum inside int64.
-__device__ __forceinline__ int spread_scale_exponent(float amax, int64_t ni) {
-    if (!(amax > 0.f)) return 0;
-    int ex;
-    frexpf(amax, &ex);  // amax < 2^ex
-    int nb = 0;
-    while (nb < 40 && ((int64_t)1 << nb) <= ni) ++nb;
-    const int e = 61 - nb - ex;
-    return max(-126, min(e, 126));
-}
-
 // Spreading, fixed-point variant: one CTA per (source, group of R receivers).
-// The CTA sweeps all image points (one per thread per step), loads the
-// source-side entry once per point and, for each of its R traces,
+// A warp takes a depth column at a time and sweeps the depths where the
+// source and at least one receiver of the group have a nonzero weight,
+// loads the source-side entry once per point and, for each of its R traces,
 // accumulates the two contributions v*(1-w), v*w into that trace's shared-
-// memory time bins as 64-bit fixed point: each contribution is scaled by a
-// power of two chosen from a bound on |v|, rounded to an integer (resolution
-// ~2^-42 of the bound) and added exactly, so the trace is independent of the
+// memory time bins as 64-bit fixed point (fixed_add: each contribution
+// scaled by a power of two chosen from a bound on |v|, rounded to an integer
+// of at most 27 bits and added exactly), so the trace is independent of the
 // order in which threads arrive.  The finished traces are converted back to
 // float, convolved with the wavelet in shared memory and written once.
 template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false>
@@ -279,7 +269,9 @@ __global__ void __launch_bounds__(kSpreadThreads, 2)
 spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
               const float* __restrict__ h, int L, int nt_pad, int fuse) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    // R trace rows of 64-bit fixed-point bins (fixed_add layout)
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    uint32_t* acc32 = reinterpret_cast<uint32_t*>(smem_raw);
     // the finished trace, zero-padded for fir_same, then the padded taps
     float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad);
     float* hs = ftr + fir_span(L, K.nt);
@@ -290,16 +282,16 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     // one time share a few receiver groups (whose rows stay in L2) and sweep
     // the sources.
     const int is = blockIdx.x % K.ns;
-    const int g = blockIdx.x / K.ns;
-    if (g >= ngroups) return;
+    const int g = K.g0 + (int)(blockIdx.x / K.ns);
+    if (g >= ngroups || g >= K.g1) return;
     const int r0 = g * R;
     const int nrr = min(R, K.nr - r0);
-    for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
+    fixed_clear(acc32, R, nt_pad, tid, blockDim.x);
     if (fuse) {
         for (int k = tid; k < fir_lpad(L); k += blockDim.x) hs[k] = k < L ? h[k] : 0.f;
         for (int k = tid; k < fir_span(L, K.nt); k += blockDim.x) ftr[k] = 0.f;
     }
-    const int e = spread_scale_exponent(__uint_as_float(*K.absmax) * K.wmax, K.ni);
+    const int e = fixed_scale_exponent(__uint_as_float(*K.absmax) * K.wmax);
     const float S = ldexpf(1.f, e);
     // first depth of each receiver's gate, in shared memory (read as a warp
     // broadcast; held in registers it costs spills)
@@ -330,9 +322,9 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
                     const float w = fp.frac(s, it);
                     const float v1 = val * w;
                     const float v0 = val - v1;
-                    unsigned long long* a = acc + (size_t)r * nt_pad + it;
-                    atomicAdd(a, (unsigned long long)__float2ll_rn(v0));
-                    atomicAdd(a + 1, (unsigned long long)__float2ll_rn(v1));
+                    uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
+                    fixed_add(row, nt_pad, it, __float2int_rn(v0));
+                    fixed_add(row, nt_pad, it + 1, __float2int_rn(v1));
                 }
             }
         }
@@ -378,13 +370,13 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     const float invS = ldexpf(1.f, -e);
     float* xt = fuse ? ftr + fir_q(L) : ftr;
     for (int r = 0; r < nrr; ++r) {
-        for (int n = tid; n < nt; n += blockDim.x) xt[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        for (int n = tid; n < nt; n += blockDim.x) xt[n] = (float)fixed_get(acc32 + (size_t)r * 2 * nt_pad, nt_pad, n) * invS;
         __syncthreads();
         // the convolved trace goes to this receiver's accumulator row, which
         // is no longer needed (2 * nt_pad >= fir_out(nt) floats)
         const float* o = xt;
         if (fuse) {
-            float* os = reinterpret_cast<float*>(acc + (size_t)r * nt_pad);
+            float* os = reinterpret_cast<float*>(acc32 + (size_t)r * 2 * nt_pad);
             fir_same(hs, ftr, os, L, nt, tid, blockDim.x);
             __syncthreads();
             o = os;
@@ -764,10 +756,15 @@ int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h,
         KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
         return KGB_OK;
     }
-    int rc = launch_prepass<DYN>(K, m, stream);
-    if (rc) return rc;
+    if (K.prepass) {
+        int rc = launch_prepass<DYN>(K, m, stream);
+        if (rc) return rc;
+    }
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
-    const int64_t blocks = (int64_t)K.ns * ((K.nr + R - 1) / R);
+    const int ngroups = (K.nr + R - 1) / R;
+    const int gn = std::min(ngroups, K.g1) - std::max(0, K.g0);
+    if (gn <= 0) return KGB_OK;
+    const int64_t blocks = (int64_t)K.ns * gn;
     kern<<<(unsigned)blocks, kSpreadThreads, sh.smem, stream>>>(K, fp, y, h, L, sh.nt_pad, fuse ? 1 : 0);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
@@ -1072,7 +1069,9 @@ __global__ void __launch_bounds__(kSpreadThreads, 2)
 spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ y, const float* __restrict__ h, int L,
                int nt_pad, int fuse) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    // R trace rows of 64-bit fixed-point bins (fixed_add layout)
     unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem_raw);
+    uint32_t* acc32 = reinterpret_cast<uint32_t*>(smem_raw);
     // the finished trace, zero-padded for fir_same, then the padded taps
     float* ftr = reinterpret_cast<float*>(acc + (size_t)R * nt_pad);
     float* hs = ftr + fir_span(L, K.nt);
@@ -1082,13 +1081,13 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
     const int tr0 = blockIdx.x * R;
     if (tr0 >= nsnr) return;
     const int ntr = min(R, nsnr - tr0);
-    for (int k = tid; k < R * nt_pad; k += blockDim.x) acc[k] = 0ull;
+    fixed_clear(acc32, R, nt_pad, tid, blockDim.x);
     if (fuse) {
         for (int k = tid; k < fir_lpad(L); k += blockDim.x) hs[k] = k < L ? h[k] : 0.f;
         for (int k = tid; k < fir_span(L, K.nt); k += blockDim.x) ftr[k] = 0.f;
     }
     // |v (1 - w)| <= 2 |v| on the negative-time path: one bit of headroom
-    const int e = spread_scale_exponent(__uint_as_float(*K.absmax) * (FIXED ? 1.f : 2.f), K.ni);
+    const int e = fixed_scale_exponent(__uint_as_float(*K.absmax) * (FIXED ? 1.f : 2.f));
     const float S = ldexpf(1.f, e);
     __syncthreads();
     for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
@@ -1108,9 +1107,9 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
             if (r < ntr && single_entry<FIXED>(K, fp, q[r], wf[r], it, w)) {
                 const float v1 = v * w;
                 const float v0 = v - v1;
-                unsigned long long* a = acc + (size_t)r * nt_pad + it;
-                atomicAdd(a, (unsigned long long)__float2ll_rn(v0));
-                atomicAdd(a + 1, (unsigned long long)__float2ll_rn(v1));
+                uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
+                fixed_add(row, nt_pad, it, __float2int_rn(v0));
+                fixed_add(row, nt_pad, it + 1, __float2int_rn(v1));
             }
         }
     }
@@ -1118,12 +1117,12 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
     const float invS = ldexpf(1.f, -e);
     float* xt = fuse ? ftr + fir_q(L) : ftr;
     for (int r = 0; r < ntr; ++r) {
-        for (int n = tid; n < nt; n += blockDim.x) xt[n] = (float)(long long)acc[(size_t)r * nt_pad + n] * invS;
+        for (int n = tid; n < nt; n += blockDim.x) xt[n] = (float)fixed_get(acc32 + (size_t)r * 2 * nt_pad, nt_pad, n) * invS;
         __syncthreads();
         // convolved trace into this trace's spent accumulator row
         const float* o = xt;
         if (fuse) {
-            float* os = reinterpret_cast<float*>(acc + (size_t)r * nt_pad);
+            float* os = reinterpret_cast<float*>(acc32 + (size_t)r * 2 * nt_pad);
             fir_same(hs, ftr, os, L, nt, tid, blockDim.x);
             __syncthreads();
             o = os;
@@ -1304,6 +1303,15 @@ int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, fl
     }
     if (K.nonneg) return gather_launch_t<false, false, true>(K, d2, img, partial, cap, stream);
     return gather_launch_t<false, false, false>(K, d2, img, partial, cap, stream);
+}
+
+int spread_group_size(const KirchDev& K, int L) {
+    if (K.tq1 || K.spread_variant != 0 || K.ns <= 0 || K.nr <= 0 || K.nt <= 0) return 0;
+    return spread_shape(K, L).R;
+}
+
+int launch_spread_prepass(const KirchDev& K, bool dynamic, const float* m, cudaStream_t stream) {
+    return dynamic ? launch_prepass<true>(K, m, stream) : launch_prepass<false>(K, m, stream);
 }
 
 int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,

@@ -82,6 +82,16 @@ class _WaveletOperator(LinearOperator):
         return self._apply(x, True)
 
 
+def _pinned_empty(n: int) -> np.ndarray:
+    """A float32 host array in page-locked memory from torch's caching host
+    allocator: the device-to-host copy of a result runs at full speed and,
+    once the caller drops the array, the block is reused by the next call
+    instead of faulting in fresh pages."""
+    import torch
+
+    return torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+
+
 class Kirchhoff(LinearOperator):
     r"""Kirchhoff demigration operator (``kirchhoff.py:40-256``).
 
@@ -379,7 +389,7 @@ class Kirchhoff(LinearOperator):
             tdt = getattr(torch, str(self.dtype)) if str(self.dtype) in ("float32", "float64") else torch.float32
             return y if tdt == torch.float32 else y.to(tdt)
         xx = np.ascontiguousarray(np.asarray(x), dtype=np.float32)
-        y = np.empty(out_n, dtype=np.float32)
+        y = _pinned_empty(out_n)
         if which in ("forward", "adjoint"):
             fn = getattr(L, "kgb_kirchhoff_" + which + "_host")
             _native.check(fn(self._h, xx.ctypes.data, y.ctypes.data))

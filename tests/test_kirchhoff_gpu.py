@@ -142,6 +142,38 @@ def test_torch_device_path_matches_host_path():
     assert np.array_equal(xd.cpu().numpy(), xh)
 
 
+@pytest.mark.parametrize("dynamic,variant", [(True, 0), (False, 0), (True, 1)])
+def test_chunked_host_path_matches_device_path(dynamic, variant):
+    """The host-buffer calls run the forward in receiver-group chunks on two
+    streams and the adjoint's correlation in source chunks, overlapped with
+    the copies; 37 receivers make a ragged last group and more groups than
+    chunks.  Variant 1 takes the unchunked host path.  Bitwise equal to the
+    device calls."""
+    import torch
+
+    from pylops_gb300.utils.wavelets import ricker
+    from pylops_gb300.waveeqprocessing import Kirchhoff
+
+    z, x = np.arange(60) * 5.0, np.arange(90) * 5.0
+    t = np.arange(400) * 0.002
+    wav, _, wc = ricker(t[:31], f0=20)
+    srcs = np.vstack((np.linspace(0, x[-1], 5), np.zeros(5)))
+    recs = np.vstack((np.linspace(0, x[-1], 37), np.zeros(37)))
+    vel = 1500.0 + 2.0 * np.broadcast_to(z[None, :], (90, 60))
+    K = Kirchhoff(z, x, t, srcs, recs, np.ascontiguousarray(vel), wav, wc, mode="eikonal", dynamic=dynamic,
+                  engine="cuda", dtype="float32")
+    K.set_spread_variant(variant)
+    rng = np.random.default_rng(4)
+    m = rng.standard_normal(K.ni).astype(np.float32)
+    d = rng.standard_normal(K.shape[0]).astype(np.float32)
+    for _ in range(2):  # the second call reuses streams, events and pinned blocks
+        yh, xh = K @ m, K.H @ d
+        yd = (K @ torch.as_tensor(m, device="cuda")).cpu().numpy()
+        xd = (K.H @ torch.as_tensor(d, device="cuda")).cpu().numpy()
+        assert np.array_equal(yh, yd)
+        assert np.array_equal(xh, xd)
+
+
 def test_table_reassignment_refreshes_device_copy():
     """The reference's tests reassign trav_srcs/trav_recs after construction."""
     g = load("k2d_kin")
