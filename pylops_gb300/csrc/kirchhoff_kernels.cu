@@ -36,7 +36,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int kGatherThreads = 256;
-constexpr int kGatherRC = 8;        // receivers held in registers per thread
+constexpr int kGatherRC = 4;        // receivers held in registers per thread
 constexpr int kSpreadThreads = 512;
 constexpr int kMaxSplit = 16;       // source splits of the gather (partial images)
 
@@ -139,10 +139,13 @@ __device__ __forceinline__ bool in_range(const uint32_t* __restrict__ rng, size_
 // entries in registers and sweeps every source against them, so table reads
 // are ~1/kGatherRC per pair-point and coalesced.  The correlated
 // data is stored as interleaved pairs (d[it], d[it+1]) so one 8-byte load
-// feeds the interpolation.  The sum over traces has a fixed order.
+// feeds the interpolation.  The sum over traces has a fixed order.  The
+// loop is a chain of dependent loads (source record, then its data), so the
+// kernel is sized for occupancy: four receivers per thread fit 32 registers
+// and eight blocks (the SM's 64 warps) stay resident.
 // ---------------------------------------------------------------------------
 template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
-__global__ void __launch_bounds__(kGatherThreads, 4)
+__global__ void __launch_bounds__(kGatherThreads, 8)
 gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __restrict__ d2,
               float* __restrict__ out, int r_per_split) {
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -155,13 +158,12 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
     const int s_begin = 0, s_end = K.ns;
     const int r_begin = blockIdx.y * r_per_split;
     const int r_end = min(K.nr, r_begin + r_per_split);
-    int64_t col = 0;
-    int iz = 0;
+    int col = 0, iz = 0;  // depth column and depth (column counts fit in int)
     if (DYN || GATE) {
-        col = ii / K.nz;
-        iz = (int)(ii - col * K.nz);
+        col = (int)(ii / K.nz);
+        iz = (int)(ii - (int64_t)col * K.nz);
     }
-    const int64_t ncol = K.ni / K.nz;
+    const int ncol = (int)(K.ni / K.nz);
     const int nt = K.nt;
     // dynamic: which sources of this split are active at this image point
     // (sources beyond the first 64 of the split are always tested)
@@ -173,10 +175,10 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
     }
     float total = 0.f;
     for (int r0 = r_begin; r0 < r_end; r0 += kGatherRC) {
-        // r0 is a multiple of 8: the warp skips the chunk when none of its
-        // receivers has a nonzero weight at any of the warp's points (a
+        // the warp skips the chunk when no receiver of the group of 8 that
+        // holds it has a nonzero weight at any of the warp's points (a
         // warp-uniform branch; a per-thread one costs register spills)
-        if (DYN && kGatherRC == 8 && K.grng &&
+        if (DYN && 8 % kGatherRC == 0 && K.grng &&
             !__any_sync(live, in_range(K.grng, (size_t)(r0 >> 3) * ncol + col, iz)))
             continue;
         Entry re[kGatherRC];
@@ -187,7 +189,6 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
             if (r < nrc) re[r] = load_entry<DYN, true, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
         }
         float chunk = 0.f;
-#pragma unroll 2
         for (int is = s_begin; is < s_end; ++is) {
             if (DYN) {
                 const int k = is - s_begin;
