@@ -39,13 +39,15 @@ __device__ __forceinline__ void fixed_clear(uint32_t* __restrict__ acc, int nrow
     }
 }
 
+// x == 0 touches nothing (bin may then be out of range).
 __device__ __forceinline__ void fixed_add(uint32_t* __restrict__ row, int nt_pad, int bin, int x) {
-    if (x == 0) return;
-    const uint32_t old = atomicAdd(row + bin, (uint32_t)x);
-    const uint32_t now = old + (uint32_t)x;
-    // carry out of the low word, minus one for the sign extension of x
-    const int hi = (now < old ? 1 : 0) - (x < 0 ? 1 : 0);
-    if (hi) atomicAdd(row + nt_pad + bin, (uint32_t)hi);
+    if (x != 0) {
+        const uint32_t old = atomicAdd(row + bin, (uint32_t)x);
+        const uint32_t now = old + (uint32_t)x;
+        // carry out of the low word, minus one for the sign extension of x
+        const int hi = (now < old ? 1 : 0) - (x < 0 ? 1 : 0);
+        if (hi) atomicAdd(row + nt_pad + bin, (uint32_t)hi);
+    }
 }
 
 __device__ __forceinline__ long long fixed_get(const uint32_t* __restrict__ row, int nt_pad, int bin) {

@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "fir.cuh"
 #include "fixed_acc.cuh"
@@ -300,35 +301,42 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     if (tid < R) izmin[tid] = (GATE && tid < nrr) ? __ldg(K.izmin + (size_t)is * K.nr + r0 + tid) : 0;
     __syncthreads();
     const int64_t ncol = K.ni / K.nz;
-    // one image point (index ii, depth izp in column colp, scaled value v)
-    auto point = [&](int64_t ii, int64_t colp, int izp, float v) {
+    // one image point (index ii, depth izp in column colp, scaled value v);
+    // FULL: all R receivers of the group exist (no per-receiver bounds)
+    auto point_t = [&](auto full, int64_t ii, int64_t colp, int izp, float v) {
+        constexpr bool FULL = decltype(full)::value;
         const Entry se = load_entry<DYN, false, HALF>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
         if (DYN && se.c == 0.f && se.s == 0.f) return;  // source outside the angle aperture
         // all R receiver records in flight before any is used
         Entry re[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) re[r] = r < nrr ? load_entry<DYN, false, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2) : zero_entry();
+        for (int r = 0; r < R; ++r)
+            re[r] = (FULL || r < nrr) ? load_entry<DYN, false, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2)
+                                      : zero_entry();
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            if (r < nrr) {
-                const int s = se.t + re[r].t;
-                float val = v;
-                if (DYN) {
-                    float wt = fmaf(se.c, re[r].c, se.s * re[r].s);
-                    if (GATE && izp < izmin[r]) wt = 0.f;
-                    val *= wt;
-                }
-                if (fp.valid(s) && val != 0.f) {
-                    const int it = fp.index(s);
-                    const float w = fp.frac(s, it);
-                    const float v1 = val * w;
-                    const float v0 = val - v1;
-                    uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
-                    fixed_add(row, nt_pad, it, __float2int_rn(v0));
-                    fixed_add(row, nt_pad, it + 1, __float2int_rn(v1));
-                }
+            const int s = se.t + re[r].t;
+            float val = v;
+            if (DYN) {
+                float wt = fmaf(se.c, re[r].c, se.s * re[r].s);
+                if (GATE && izp < izmin[r]) wt = 0.f;
+                val *= wt;
             }
+            // straight-line code: an invalid time or a missing receiver
+            // gives zero contributions, which fixed_add skips
+            const bool ok = (FULL || r < nrr) && fp.valid(s);
+            const int it = fp.index(s);
+            const float w = fp.frac(s, it);
+            const float v1 = val * w;
+            const float v0 = val - v1;
+            uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
+            fixed_add(row, nt_pad, it, ok ? __float2int_rn(v0) : 0);
+            fixed_add(row, nt_pad, it + 1, ok ? __float2int_rn(v1) : 0);
         }
+    };
+    auto point = [&](int64_t ii, int64_t colp, int izp, float v) {
+        if (nrr == R) point_t(std::true_type{}, ii, colp, izp, v);
+        else point_t(std::false_type{}, ii, colp, izp, v);
     };
     if (DYN && R == 8 && K.grng) {
         // a warp per depth column, over the depths where both the source
