@@ -18,7 +18,7 @@
 
 namespace kgb {
 
-constexpr int kFixedBits = 28;
+constexpr int kFixedBits = 30;
 constexpr uint32_t kFixedBias = 0x80000000u;
 
 // e with |v| 2^e < 2^kFixedBits for |v| <= amax
