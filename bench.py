@@ -582,6 +582,7 @@ def run_single(args):
     K = Kirchhoff(z, x, t, srcs, recs, 1500.0, wav, wc, mode="byot", trav=table, engine="cuda", dtype="float32")
     K.native_handle
     t_setup = time.perf_counter() - t0
+    variant_ms = K.autotune()
     g = torch.Generator(device="cuda").manual_seed(0)
     m = torch.randn(K.ni, device="cuda", generator=g)
     d = torch.randn(K.shape[0], device="cuda", generator=g)
@@ -631,6 +632,8 @@ def run_single(args):
         "config": {"workload": "single_table_2d_300x800_64x%d_nt1501" % nr, "table_gb": round(table_bytes / 1e9, 3),
                    "l2": "table larger than L2", "setup_s": round(t_setup, 1)},
         "kernel_ms": {"forward": round(fwd_ms, 3), "adjoint": round(adj_ms, 3)},
+        "spread_variant_ms": {str(k): round(v, 3) for k, v in variant_ms.items()},
+        "spread_variant": K.info()["spread_variant"],
         "hbm_fraction": round(B / step / 1e9 / peaks["hbm_gbs"], 4),
         "roofline": {"bound": "hbm", "kernel": "gather1 (adjoint)", "achieved": round(ach, 1),
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": round(ach / peaks["hbm_gbs"], 4),

@@ -126,7 +126,11 @@ int kgb_kirchhoff_adjoint(kgb_kirchhoff* op, const float* d_dev, float* m_dev, v
 
 /* Same as forward/adjoint with host buffers: the copies to and from the
  * device happen inside the call, which returns after the result is on the
- * host.  Replaces: _KirchhoffCudaHelper._matvec_cuda / _rmatvec_cuda
+ * host.  The copies overlap the kernels (the forward's traces leave in
+ * receiver-group chunks as they finish, the adjoint's data arrive in
+ * source chunks and are correlated as they land); results equal the
+ * device calls bit for bit.  Page-locked host buffers copy at full speed.
+ * Replaces: _KirchhoffCudaHelper._matvec_cuda / _rmatvec_cuda
  * (_kirchhoff_cuda.py:443-489) called with numpy arrays. */
 int kgb_kirchhoff_forward_host(kgb_kirchhoff* op, const float* m_host, float* d_host);
 int kgb_kirchhoff_adjoint_host(kgb_kirchhoff* op, const float* d_host, float* m_host);
@@ -144,10 +148,12 @@ int kgb_kirchhoff_gather(kgb_kirchhoff* op, const float* d_dev, float* m_dev, vo
 int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x_dev, float* y_dev, int adjoint,
                           void* stream);
 
-/* Choose the forward (spreading) kernel: 0 = 64-bit fixed-point shared-
- * memory accumulation, 1 = warp-binned (one trace per warp, the default),
- * 2 = warp-binned with two traces per warp.  All three are deterministic and
- * give the same result up to float32 rounding.  No reference counterpart
+/* Choose the forward (spreading) kernel: 0 = fixed-point shared-memory
+ * accumulation (the default, fastest on every workload measured),
+ * 1 = warp-binned (one trace per warp), 2 = warp-binned with two traces per
+ * warp.  All three are deterministic and give the same result up to float32
+ * rounding.  The host-buffer forward overlaps its copies with variant 0 only.
+ * No reference counterpart
  * (the reference has one CUDA kernel per mode, _kirchhoff_cuda.py:55-298);
  * used by the tile autotuner. */
 int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant);

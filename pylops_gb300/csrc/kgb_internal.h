@@ -37,7 +37,7 @@ struct KirchDev {
     int frac_bits;
     int nonneg;        // every ts + tr >= 0: index math without the negative-time case
     float wmax;        // bound on |dynamic weight| (1 for kinematic), for the fixed-point scale
-    int spread_variant; // 0: 64-bit fixed-point atomics; 1/2: warp-binned, 1/2 traces per warp
+    int spread_variant; // 0: fixed-point shared-memory atomics (the default); 1/2: warp-binned, 1/2 traces per warp
     float* mv;         // scratch: m * 2/v per application (ni)
     unsigned* absmax;  // scratch: bits of max |mv| per application
     const int32_t* tsq;
@@ -137,7 +137,7 @@ struct kgb_kirchhoff {
     bool has_gate = false;
     bool nonneg = true;
     float wmax = 1.f;
-    int spread_variant = 1;
+    int spread_variant = 0;
     float* mv = nullptr;
     unsigned* absmax = nullptr;
     bool trav_ready = false;
