@@ -186,7 +186,7 @@ batch_correlate_kernel(const Prob* __restrict__ probs, int nprob, const float* _
 
 // One CTA per item (problem, tile of kTile image points); each thread sums
 // its image point over all traces of its problem in a fixed order.
-__global__ void __launch_bounds__(kTile, 4)
+__global__ void __launch_bounds__(kTile, 8)  // 30 registers: the SM's 64 warps hide the load chain
 batch_gather_kernel(const Prob* __restrict__ probs, const GatherItem* __restrict__ items,
                     const float2* __restrict__ dc, float* __restrict__ img) {
     const GatherItem it_ = items[blockIdx.x];
