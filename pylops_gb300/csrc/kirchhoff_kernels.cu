@@ -263,9 +263,10 @@ spread_prepass_kernel(const KirchDev K, const float* __restrict__ m) {
 // accumulates the two contributions v*(1-w), v*w into that trace's shared-
 // memory time bins as 64-bit fixed point (fixed_add: each contribution
 // scaled by a power of two chosen from a bound on |v|, rounded to an integer
-// of at most 27 bits and added exactly), so the trace is independent of the
-// order in which threads arrive.  The finished traces are converted back to
-// float, convolved with the wavelet in shared memory and written once.
+// of at most kFixedBits bits plus sign and added exactly), so the trace is
+// independent of the order in which threads arrive.  The finished traces
+// are converted back to float, convolved with the wavelet in shared memory
+// and written once.
 template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false>
 __global__ void __launch_bounds__(kSpreadThreads, 2)
 spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
