@@ -160,7 +160,7 @@ struct kgb_kirchhoff {
     cudaStream_t stream = nullptr;  // used by the host-buffer entry points
     // host-buffer entry points: a second compute stream and a copy stream
     // (created on first use) and the events that order the chunks
-    static constexpr int kHostChunks = 4;
+    static constexpr int kHostChunks = 8;
     cudaStream_t stream2 = nullptr;
     cudaStream_t cstream = nullptr;
     cudaEvent_t ev[kHostChunks + 1] = {};
