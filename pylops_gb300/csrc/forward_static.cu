@@ -1,8 +1,9 @@
 // Forward application that allocates nothing: kgb_kirchhoff_forward_static.
 //
 // The regular forward (kgb_kirchhoff_forward) keeps its scratch -- the model
-// scaled by 2/v and the maximum of its magnitude, which set the forward's
-// fixed-point scale -- in buffers the operator allocated.  This entry point
+// scaled by 2/v and the statistics of its magnitude (maximum, exponent
+// histogram) that set the forward's fixed-point scale -- in buffers the
+// operator allocated.  This entry point
 // keeps the same scratch in the file-scope device array below instead, so the
 // call itself never allocates device memory.  It is meant for callers that
 // must not call cudaMalloc while they run: code working inside a fixed
@@ -19,7 +20,7 @@
 //    loaded and stays allocated until the process exits;
 //  * every call on a GPU uses the same array: calls whose kernels overlap on
 //    that GPU (for example on two streams) race and must be serialised by the
-//    caller.  The maximum word is cleared at the start of every call; the
+//    caller.  The scale block is cleared at the start of every call; the
 //    scaled model is rewritten in full by every call;
 //  * the first call on a GPU looks the array's device address up with
 //    cudaGetSymbolAddress (once per device, that device current); make that
@@ -33,9 +34,11 @@
 namespace {
 
 constexpr int64_t kStaticMaxImagePoints = (int64_t)1 << 22;
-// scaled model (kStaticMaxImagePoints floats) followed by the maximum word,
-// which therefore starts on a 256-byte boundary too
-__device__ __align__(256) float g_forward_scratch[kStaticMaxImagePoints + 64];
+// scaled model (kStaticMaxImagePoints floats) followed by the forward's
+// scale block (kgb::kScaleWords words), which therefore starts on a 256-byte
+// boundary too
+__device__ __align__(256) float g_forward_scratch[kStaticMaxImagePoints + 512];
+static_assert(kgb::kScaleWords <= 512, "scale block does not fit the static scratch");
 
 constexpr int kMaxDevices = 64;
 float* g_scratch_ptr[kMaxDevices] = {nullptr};

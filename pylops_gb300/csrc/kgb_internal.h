@@ -39,7 +39,7 @@ struct KirchDev {
     float wmax;        // bound on |dynamic weight| (1 for kinematic), for the fixed-point scale
     int spread_variant; // 0: fixed-point shared-memory atomics (the default); 1/2: warp-binned, 1/2 traces per warp
     float* mv;         // scratch: m * 2/v per application (ni)
-    unsigned* absmax;  // scratch: bits of max |mv| per application
+    unsigned* absmax;  // scratch: the forward's scale block (kScaleWords, see fixed_acc.cuh) per application
     const int32_t* tsq;
     const int32_t* trq;
     const float* wsc;
@@ -76,6 +76,11 @@ struct KirchDev {
     int prepass;
 };
 
+// u32 words of the forward's fixed-point scale block: [0] bits of max |mv|,
+// [1] the chosen scale exponent, [2, 2 + 256) histogram of the exponents of
+// the nonzero |mv|
+constexpr int kScaleWords = 2 + 256;
+
 // Launchers (kirchhoff_kernels.cu).  All asynchronous on `stream`.
 int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,
                   const float* h, int L, bool fuse_wavelet, cudaStream_t stream);
@@ -97,7 +102,7 @@ int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, co
 // operator, 0 when the forward does not run that kernel (binned variants,
 // single traveltime table, traces too long for shared memory).
 int spread_group_size(const KirchDev& K, int L);
-// The forward's prepass alone (mv = m * 2/v or m, and absmax).
+// The forward's prepass alone (mv = m * 2/v or m, and its scale block).
 int launch_spread_prepass(const KirchDev& K, bool dynamic, const float* m, cudaStream_t stream);
 // Union ranges of groups of 8 receivers from the per-receiver ranges.
 int launch_group_ranges(const uint32_t* rrng, uint32_t* grng, int nr, int64_t ncol, cudaStream_t stream);

@@ -157,7 +157,7 @@ int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni
         op->partial_elems = gather_partial_elems(op->view());
         if ((rc = dev_alloc(&op->partial, (size_t)op->partial_elems, "alloc partial images"))) break;
         if ((rc = dev_alloc(&op->mv, (size_t)ni, "alloc scaled model"))) break;
-        if ((rc = dev_alloc(&op->absmax, 1, "alloc model maximum"))) break;
+        if ((rc = dev_alloc(&op->absmax, kScaleWords, "alloc forward scale block"))) break;
         if ((rc = prepare_kernels(op->view(), op->L))) break;
         e = cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) { rc = cuda_error(e, "create stream"); break; }

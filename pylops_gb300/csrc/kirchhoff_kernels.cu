@@ -243,6 +243,9 @@ __global__ void sum_partials_kernel(const float* __restrict__ partial, float* __
 template <bool DYN>
 __global__ void __launch_bounds__(256)
 spread_prepass_kernel(const KirchDev K, const float* __restrict__ m) {
+    __shared__ unsigned hist[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) hist[k] = 0u;
+    __syncthreads();
     float amax = 0.f;
     for (int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ii < K.ni;
          ii += (int64_t)gridDim.x * blockDim.x) {
@@ -250,10 +253,19 @@ spread_prepass_kernel(const KirchDev K, const float* __restrict__ m) {
         if (DYN) v *= __ldg(K.vscale + ii);
         K.mv[ii] = v;
         amax = fmaxf(amax, fabsf(v));
+        if (v != 0.f) atomicAdd(&hist[scale_bucket(v)], 1u);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(FULL, amax, o));
     if ((threadIdx.x & 31) == 0 && amax > 0.f) atomicMax(K.absmax, __float_as_uint(amax));
+    __syncthreads();
+    for (int k = threadIdx.x; k < 256; k += blockDim.x)
+        if (hist[k]) atomicAdd(K.absmax + 2 + k, hist[k]);
+}
+
+// One block: the scale exponent from the scale block (fixed_choose_exponent).
+__global__ void __launch_bounds__(256) spread_scale_kernel(const KirchDev K, float wfactor) {
+    fixed_choose_exponent(K.absmax, K.ni, wfactor);
 }
 
 // Spreading, fixed-point variant: one CTA per (source, group of R receivers).
@@ -294,7 +306,7 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
         for (int k = tid; k < fir_lpad(L); k += blockDim.x) hs[k] = k < L ? h[k] : 0.f;
         for (int k = tid; k < fir_span(L, K.nt); k += blockDim.x) ftr[k] = 0.f;
     }
-    const int e = fixed_scale_exponent(__uint_as_float(*K.absmax) * K.wmax);
+    const int e = (int)K.absmax[1];  // spread_scale_kernel
     const float S = ldexpf(1.f, e);
     // first depth of each receiver's gate, in shared memory (read as a warp
     // broadcast; held in registers it costs spills)
@@ -304,8 +316,10 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     const int64_t ncol = K.ni / K.nz;
     // one image point (index ii, depth izp in column colp, scaled value v);
     // FULL: all R receivers of the group exist (no per-receiver bounds)
-    auto point_t = [&](auto full, int64_t ii, int64_t colp, int izp, float v) {
+    // WIDE: the point may give contributions of 2^31 or more (fixed_wide)
+    auto point_t = [&](auto full, auto wide, int64_t ii, int64_t colp, int izp, float v) {
         constexpr bool FULL = decltype(full)::value;
+        constexpr bool WIDE = decltype(wide)::value;
         const Entry se = load_entry<DYN, false, HALF>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
         if (DYN && se.c == 0.f && se.s == 0.f) return;  // source outside the angle aperture
         // all R receiver records in flight before any is used
@@ -331,13 +345,24 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
             const float v1 = val * w;
             const float v0 = val - v1;
             uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
-            fixed_add(row, nt_pad, it, ok ? __float2int_rn(v0) : 0);
-            fixed_add(row, nt_pad, it + 1, ok ? __float2int_rn(v1) : 0);
+            if (WIDE) {
+                fixed_add_wide(row, nt_pad, it, ok ? v0 : 0.f);
+                fixed_add_wide(row, nt_pad, it + 1, ok ? v1 : 0.f);
+            } else {
+                fixed_add(row, nt_pad, it, ok ? __float2int_rn(v0) : 0);
+                fixed_add(row, nt_pad, it + 1, ok ? __float2int_rn(v1) : 0);
+            }
         }
     };
     auto point = [&](int64_t ii, int64_t colp, int izp, float v) {
-        if (nrr == R) point_t(std::true_type{}, ii, colp, izp, v);
-        else point_t(std::false_type{}, ii, colp, izp, v);
+        if (fixed_wide(v, K.wmax)) {
+            if (nrr == R) point_t(std::true_type{}, std::true_type{}, ii, colp, izp, v);
+            else point_t(std::false_type{}, std::true_type{}, ii, colp, izp, v);
+        } else if (nrr == R) {
+            point_t(std::true_type{}, std::false_type{}, ii, colp, izp, v);
+        } else {
+            point_t(std::false_type{}, std::false_type{}, ii, colp, izp, v);
+        }
     };
     if (DYN && R == 8 && K.grng) {
         // a warp per depth column, over the depths where both the source
@@ -749,11 +774,14 @@ SpreadShape spread_shape(const KirchDev& K, int L) {
     return sh;
 }
 
+// wfactor: bound on |contribution| / |mv| (the largest weight; 2 for the
+// single table's negative-time path)
 template <bool DYN>
-int launch_prepass(const KirchDev& K, const float* m, cudaStream_t stream) {
-    KGB_CUDA_TRY(cudaMemsetAsync(K.absmax, 0, sizeof(unsigned), stream));
+int launch_prepass(const KirchDev& K, const float* m, cudaStream_t stream, float wfactor) {
+    KGB_CUDA_TRY(cudaMemsetAsync(K.absmax, 0, kScaleWords * sizeof(unsigned), stream));
     const int pb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
     spread_prepass_kernel<DYN><<<pb, 256, 0, stream>>>(K, m);
+    spread_scale_kernel<<<1, 256, 0, stream>>>(K, wfactor);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -767,7 +795,7 @@ int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h,
         return KGB_OK;
     }
     if (K.prepass) {
-        int rc = launch_prepass<DYN>(K, m, stream);
+        int rc = launch_prepass<DYN>(K, m, stream, K.wmax);
         if (rc) return rc;
     }
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
@@ -795,7 +823,7 @@ int spread_binned_launch_r(const KirchDev& K, const float* m, float* y, const fl
         KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         return KGB_OK;
     }
-    int rc = launch_prepass<DYN>(K, m, stream);
+    int rc = launch_prepass<DYN>(K, m, stream, K.wmax);
     if (rc) return rc;
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int per_cta = warps * RT;
@@ -1097,12 +1125,13 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
         for (int k = tid; k < fir_span(L, K.nt); k += blockDim.x) ftr[k] = 0.f;
     }
     // |v (1 - w)| <= 2 |v| on the negative-time path: one bit of headroom
-    const int e = fixed_scale_exponent(__uint_as_float(*K.absmax) * (FIXED ? 1.f : 2.f));
+    const int e = (int)K.absmax[1];  // spread_scale_kernel
     const float S = ldexpf(1.f, e);
     __syncthreads();
     for (int64_t ii = tid; ii < K.ni; ii += blockDim.x) {
         const float v = __ldg(K.mv + ii) * S;
         if (v == 0.f) continue;
+        const bool wide = fixed_wide(v, FIXED ? 1.f : 2.f);
         int q[R];
         float wf[R];
 #pragma unroll
@@ -1118,8 +1147,13 @@ spread1_kernel(const KirchDev K, const FixedPoint<true> fp, float* __restrict__ 
                 const float v1 = v * w;
                 const float v0 = v - v1;
                 uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
-                fixed_add(row, nt_pad, it, __float2int_rn(v0));
-                fixed_add(row, nt_pad, it + 1, __float2int_rn(v1));
+                if (wide) {
+                    fixed_add_wide(row, nt_pad, it, v0);
+                    fixed_add_wide(row, nt_pad, it + 1, v1);
+                } else {
+                    fixed_add(row, nt_pad, it, __float2int_rn(v0));
+                    fixed_add(row, nt_pad, it + 1, __float2int_rn(v1));
+                }
             }
         }
     }
@@ -1151,7 +1185,7 @@ int spread1_launch_r(const KirchDev& K, const float* m, float* y, const float* h
         KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         return KGB_OK;
     }
-    int rc = launch_prepass<false>(K, m, stream);
+    int rc = launch_prepass<false>(K, m, stream, FIXED ? 1.f : 2.f);
     if (rc) return rc;
     const FixedPoint<true> fp = make_fp<true>(K.frac_bits, K.nt);
     const int64_t blocks = ((int64_t)K.ns * K.nr + R - 1) / R;
@@ -1321,7 +1355,7 @@ int spread_group_size(const KirchDev& K, int L) {
 }
 
 int launch_spread_prepass(const KirchDev& K, bool dynamic, const float* m, cudaStream_t stream) {
-    return dynamic ? launch_prepass<true>(K, m, stream) : launch_prepass<false>(K, m, stream);
+    return dynamic ? launch_prepass<true>(K, m, stream, K.wmax) : launch_prepass<false>(K, m, stream, K.wmax);
 }
 
 int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,

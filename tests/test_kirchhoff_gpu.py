@@ -108,6 +108,36 @@ def test_config1_scale_against_oracle(dynamic, angleaperture, aperture):
         assert rel(y, yr) < TOL, (variant, rel(y, yr))
 
 
+@pytest.mark.parametrize("sign", [1.0, -1.0, 0.0])
+def test_fixed_point_carries_against_oracle(sign):
+    """The forward accumulates 30-bit contributions into 64-bit bins whose
+    low 32-bit words start at 2^31; a constant-sign model makes every bin
+    collect many same-sign contributions close to the scale bound, so the
+    low words wrap and the carry/borrow into the high words runs (sign 0: a
+    mixed-sign model with one dominant point, mostly small contributions).
+    Against the float64 oracle, both forward variants."""
+    from pylops_gb300.waveeqprocessing import Kirchhoff
+
+    for dynamic in (False, True):
+        c = _config1_like(dynamic=dynamic, angleaperture=None if not dynamic else 60.0)
+        args = (c["z"], c["x"], c["t"], c["srcs"], c["recs"], c["vel"], c["wav"], c["wc"])
+        kw = dict(mode="analytic", dynamic=dynamic, angleaperture=90.0 if not dynamic else 60.0)
+        K = Kirchhoff(*args, engine="cuda", dtype="float32", **kw)
+        O = ko.KirchhoffOracle(*args, **kw)
+        if sign:
+            m = np.full(K.ni, sign)
+        else:
+            m = np.random.default_rng(8).standard_normal(K.ni) * 1e-3
+            m[K.ni // 2] = 50.0
+        # the spreading alone: the zero-mean wavelet would cancel most of a
+        # constant-sign trace and measure float32 conditioning, not the sums
+        yo = O.spread(m)
+        for variant in (0, 1):
+            K.set_spread_variant(variant)
+            y = K.spread(m.astype(np.float32))
+            assert rel(y, yo) < TOL, (dynamic, variant, rel(y, yo))
+
+
 def test_bitwise_determinism():
     c = _config1_like(dynamic=True, angleaperture=40.0)
     from pylops_gb300.waveeqprocessing import Kirchhoff
