@@ -25,7 +25,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
+#include <vector>
 
 #include "fir.cuh"
 #include "fixed_acc.cuh"
@@ -1300,6 +1302,35 @@ size_t wavelet_smem(int L, int nt) {
     return (size_t)(fir_lpad(L) + fir_span(L, nt) + fir_out(nt)) * sizeof(float);
 }
 
+int wavelet_threads(const float* g, int nt) {
+    const int nblk = fir_out(nt) / kFirJ;
+    return g ? std::min(256, (nblk + 31) / 32 * 32) : 256;
+}
+
+// Resident wavelet_kernel blocks per SM for a launch shape, cached: the
+// operator's shapes are queried when its kernels are prepared, outside any
+// stream capture.
+int wavelet_blocks_per_sm(int threads, size_t smem) {
+    struct Entry {
+        int threads;
+        size_t smem;
+        int per_sm;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Entry& e : cache)
+        if (e.threads == threads && e.smem == smem) return e.per_sm;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wavelet_kernel, threads, smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    cache.push_back({threads, smem, per_sm});
+    return per_sm;
+}
+
 }  // namespace
 
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
@@ -1385,8 +1416,12 @@ int prepare_kernels(const KirchDev& K0, int L) {
     if ((rc = spread1_dispatch_t<true>(K, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     if ((rc = spread1_dispatch_t<false>(K, nullptr, nullptr, nullptr, L, true, nullptr, true))) return rc;
     const size_t smem = wavelet_smem(L, K.nt);
-    if (smem <= 227 * 1024)
+    if (smem <= 227 * 1024) {
         KGB_CUDA_TRY(cudaFuncSetAttribute(wavelet_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        // the launch shapes of the correlation (with the wavelet) and of the copy (without)
+        wavelet_blocks_per_sm(wavelet_threads(&K.wmax, K.nt), smem);
+        wavelet_blocks_per_sm(wavelet_threads(nullptr, K.nt), wavelet_smem(1, K.nt));
+    }
     return KGB_OK;
 }
 
@@ -1396,10 +1431,10 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
     const size_t smem = wavelet_smem(L, nt);
     if (smem > 227 * 1024)
         return set_error(KGB_ERR_NOT_IMPLEMENTED, "wavelet: nt=%d too long for shared memory", nt);
-    // threads: enough for the output blocks of one trace, whole warps
-    const int nblk = fir_out(nt) / kFirJ;
-    const int threads = g ? std::min(256, (nblk + 31) / 32 * 32) : 256;
-    const int64_t blocks = std::min<int64_t>(ntr, 16 * num_sms());
+    // threads: enough for the output blocks of one trace, whole warps;
+    // blocks: as many as stay resident (one wave of the grid-stride loop)
+    const int threads = wavelet_threads(g, nt);
+    const int64_t blocks = std::min<int64_t>(ntr, (int64_t)wavelet_blocks_per_sm(threads, smem) * num_sms());
     wavelet_kernel<<<(unsigned)blocks, threads, smem, stream>>>(x, y, ntr, nt, g, L, interleave);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
