@@ -586,9 +586,9 @@ int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
     s[4] = op->frac_bits; s[5] = op->L; s[6] = op->has_gate ? 1 : 0; s[7] = op->dynamic;
     s[8] = op->nonneg ? 1 : 0;
     s[9] = gather_nsplit(op->view(), op->dynamic, op->has_gate);
-    // kernels per application: forward = prepass + spread; adjoint =
-    // correlation + gather (+ partial-image sum when split)
-    s[10] = 2;
+    // kernels per application: forward = prepass + scale choice + spread;
+    // adjoint = correlation + gather (+ partial-image sum when split)
+    s[10] = 3;
     s[11] = 2 + (s[9] > 1 ? 1 : 0);
     s[12] = op->spread_variant;
     return KGB_OK;
