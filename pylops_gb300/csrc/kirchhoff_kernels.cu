@@ -270,6 +270,11 @@ __global__ void __launch_bounds__(256) spread_scale_kernel(const KirchDev K, flo
     fixed_choose_exponent(K.absmax, K.ni, wfactor);
 }
 
+// Bound on |contribution| / |scaled model value| of the fixed-point spread:
+// the largest weight, twice that on the general path, whose interpolation
+// weight can be negative (|v (1 - w)| <= 2 |v| for -1 < w < 0).
+__host__ __device__ __forceinline__ float spread_wfactor(float wmax, bool nonneg) { return nonneg ? wmax : 2.f * wmax; }
+
 // Spreading, fixed-point variant: one CTA per (source, group of R receivers).
 // A warp takes a depth column at a time and sweeps the depths where the
 // source and at least one receiver of the group have a nonzero weight,
@@ -357,7 +362,7 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
         }
     };
     auto point = [&](int64_t ii, int64_t colp, int izp, float v) {
-        if (fixed_wide(v, K.wmax)) {
+        if (fixed_wide(v, spread_wfactor(K.wmax, NONNEG))) {
             if (nrr == R) point_t(std::true_type{}, std::true_type{}, ii, colp, izp, v);
             else point_t(std::false_type{}, std::true_type{}, ii, colp, izp, v);
         } else if (nrr == R) {
@@ -797,7 +802,7 @@ int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h,
         return KGB_OK;
     }
     if (K.prepass) {
-        int rc = launch_prepass<DYN>(K, m, stream, K.wmax);
+        int rc = launch_prepass<DYN>(K, m, stream, spread_wfactor(K.wmax, NONNEG));
         if (rc) return rc;
     }
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
@@ -1386,7 +1391,8 @@ int spread_group_size(const KirchDev& K, int L) {
 }
 
 int launch_spread_prepass(const KirchDev& K, bool dynamic, const float* m, cudaStream_t stream) {
-    return dynamic ? launch_prepass<true>(K, m, stream, K.wmax) : launch_prepass<false>(K, m, stream, K.wmax);
+    const float wf = spread_wfactor(K.wmax, K.nonneg != 0);
+    return dynamic ? launch_prepass<true>(K, m, stream, wf) : launch_prepass<false>(K, m, stream, wf);
 }
 
 int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, float* y,
