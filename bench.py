@@ -798,7 +798,7 @@ def run_nsconv(args):
     print(json.dumps(line))
 
 
-def run_config4(args):
+def run_kirchhoff3d(args):
     """The 3-D workload: analytic constant velocity 2500 m/s, dynamic, 100 x 100
     x 120 grid at 10 m, 16 sources on a 4 x 4 and 400 receivers on a 20 x 20
     surface grid, nt = 1001 at 4 ms, 20 Hz Ricker, traveltimes exact and
@@ -1004,11 +1004,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "lsm", "single", "unet", "nsconv", "config4"],
-                    help="config2: the headline fwd+adj workload; batch: 256 batched LSM problems; "
+    ap.add_argument("--workload", default="kirchhoff2d",
+                    choices=["kirchhoff2d", "batch", "lsm", "single", "unet", "nsconv", "kirchhoff3d"],
+                    help="kirchhoff2d: the headline fwd+adj workload; batch: 256 batched LSM problems; "
                          "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models); "
                          "single: the single-traveltime-table (HBM-streaming) mode; unet: U-Net training; "
-                         "nsconv: the non-stationary convolution (image-domain Hessian); config4: the 3-D workload")
+                         "nsconv: the non-stationary convolution (image-domain Hessian); kirchhoff3d: the 3-D workload")
     ap.add_argument("--weights", default="bfloat16", choices=["bfloat16", "float32"],
                     help="dynamic weight tables of the 3-D workload")
     ap.add_argument("--single-receivers", type=int, default=100)
@@ -1035,8 +1036,8 @@ def main():
         run_unet(args)
     elif args.workload == "nsconv":
         run_nsconv(args)
-    elif args.workload == "config4":
-        run_config4(args)
+    elif args.workload == "kirchhoff3d":
+        run_kirchhoff3d(args)
     else:
         run_gpu(args)
 

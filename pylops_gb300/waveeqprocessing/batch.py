@@ -144,7 +144,7 @@ class KirchhoffBatch(LinearOperator):
 
 
 def random_problems(n: int, seed: int = 0, nt: int = 501, dt: float = 0.004, f0: float = 25.0):
-    """Seeded batch of the batched-LSM configuration: per problem a constant
+    """Seeded batch of the batched-LSM workload: per problem a constant
     velocity U[1500, 3500] m/s, nz in U[64, 200], nx in U[64, 256] at 4 m,
     8-32 sources and 32-128 receivers at the surface, a 25 Hz Ricker, and a
     reflectivity of 2-6 random-dip layers.  Returns a list of dicts with the

@@ -64,7 +64,7 @@ def test_dottest(name):
     assert dottest(K, rtol=1e-5, seed=4, backend="torch")
 
 
-def _config1_like(nz=100, nx=200, ns=10, nr=50, nt=651, dynamic=False, angleaperture=90.0, aperture=None):
+def _grid_100x200(nz=100, nx=200, ns=10, nr=50, nt=651, dynamic=False, angleaperture=90.0, aperture=None):
     z = np.arange(nz) * 4.0
     x = np.arange(nx) * 4.0
     t = np.arange(nt) * 0.004
@@ -86,11 +86,11 @@ def _config1_like(nz=100, nx=200, ns=10, nr=50, nt=651, dynamic=False, angleaper
 
 @pytest.mark.parametrize("dynamic,angleaperture,aperture", [(False, 90.0, None), (True, 30.0, None),
                                                             (True, None, 1.5)])
-def test_config1_scale_against_oracle(dynamic, angleaperture, aperture):
-    """Full config-1 geometry (100x200 grid, 10x50 traces, nt=651) vs the oracle."""
+def test_100x200_grid_against_oracle(dynamic, angleaperture, aperture):
+    """100x200 grid at 4 m, 10x50 traces, nt=651, against the oracle."""
     from pylops_gb300.waveeqprocessing import Kirchhoff
 
-    c = _config1_like(dynamic=dynamic, angleaperture=angleaperture, aperture=aperture)
+    c = _grid_100x200(dynamic=dynamic, angleaperture=angleaperture, aperture=aperture)
     args = (c["z"], c["x"], c["t"], c["srcs"], c["recs"], c["vel"], c["wav"], c["wc"])
     kw = dict(mode="analytic", dynamic=dynamic, angleaperture=angleaperture, aperture=aperture)
     K = Kirchhoff(*args, engine="cuda", dtype="float32", **kw)
@@ -119,7 +119,7 @@ def test_fixed_point_carries_against_oracle(sign):
     from pylops_gb300.waveeqprocessing import Kirchhoff
 
     for dynamic in (False, True):
-        c = _config1_like(dynamic=dynamic, angleaperture=None if not dynamic else 60.0)
+        c = _grid_100x200(dynamic=dynamic, angleaperture=None if not dynamic else 60.0)
         args = (c["z"], c["x"], c["t"], c["srcs"], c["recs"], c["vel"], c["wav"], c["wc"])
         kw = dict(mode="analytic", dynamic=dynamic, angleaperture=90.0 if not dynamic else 60.0)
         K = Kirchhoff(*args, engine="cuda", dtype="float32", **kw)
@@ -170,7 +170,7 @@ def test_negative_two_table_times_against_oracle():
 
 
 def test_bitwise_determinism():
-    c = _config1_like(dynamic=True, angleaperture=40.0)
+    c = _grid_100x200(dynamic=True, angleaperture=40.0)
     from pylops_gb300.waveeqprocessing import Kirchhoff
 
     K = Kirchhoff(c["z"], c["x"], c["t"], c["srcs"], c["recs"], c["vel"], c["wav"], c["wc"], mode="analytic",
