@@ -82,11 +82,18 @@ class _WaveletOperator(LinearOperator):
         return self._apply(x, True)
 
 
+_PINNED_MAX_BYTES = 1 << 31
+
+
 def _pinned_empty(n: int) -> np.ndarray:
     """A float32 host array in page-locked memory from torch's caching host
     allocator: the device-to-host copy of a result runs at full speed and,
     once the caller drops the array, the block is reused by the next call
-    instead of faulting in fresh pages."""
+    instead of faulting in fresh pages.  Page-locked memory is a limited
+    host resource that the allocator keeps once used, so results above 2 GiB
+    are ordinary (pageable) arrays."""
+    if 4 * n > _PINNED_MAX_BYTES:
+        return np.empty(n, dtype=np.float32)
     import torch
 
     return torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
