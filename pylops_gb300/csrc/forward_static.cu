@@ -22,9 +22,15 @@
 //    that GPU (for example on two streams) race and must be serialised by the
 //    caller.  The scale block is cleared at the start of every call; the
 //    scaled model is rewritten in full by every call;
-//  * the first call on a GPU looks the array's device address up with
-//    cudaGetSymbolAddress (once per device, that device current); make that
-//    first call before any stream capture.
+//  * the array's device address is looked up (cudaGetSymbolAddress, with
+//    the operator's device current) when an operator is created
+//    (kgb_kirchhoff_create calls static_scratch_prepare), which is also when
+//    a lazily loaded module places the array in device memory; the call
+//    itself only reads the cached address.  Create the operator before any
+//    stream capture.  A device reset (cudaDeviceReset, or the primary
+//    context released and created again) invalidates the cached address
+//    together with every operator of that device; operators created after
+//    it look the address up again.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -44,21 +50,38 @@ constexpr int kMaxDevices = 64;
 float* g_scratch_ptr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mu;
 
-// Device address of g_forward_scratch on the current device (host code may
-// not use the symbol itself as a device pointer).
-int scratch_for_current_device(float** out) {
+}  // namespace
+
+namespace kgb {
+
+// Look up the device address of g_forward_scratch on the current device and
+// cache it for that device (host code may not use the symbol itself as a
+// device pointer).  Called by kgb_kirchhoff_create with the operator's
+// device current; every creation looks it up again, so a cache left stale by
+// a device reset is replaced by the next operator created on that device.
+int static_scratch_prepare() {
     int dev = 0;
     KGB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return KGB_OK;  // forward_static then refuses this device
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_forward_scratch);
+    if (e != cudaSuccess) return cuda_error(e, "forward_static scratch: cudaGetSymbolAddress");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    g_scratch_ptr[dev] = static_cast<float*>(p);
+    return KGB_OK;
+}
+
+}  // namespace kgb
+
+namespace {
+
+// The cached address for device `dev` (set when an operator was created there).
+int scratch_for_device(int dev, float** out) {
     if (dev < 0 || dev >= kMaxDevices)
         return kgb::set_error(KGB_ERR_VALUE, "forward_static: device %d beyond the supported %d", dev, kMaxDevices);
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_forward_scratch);
-        if (e != cudaSuccess) return kgb::cuda_error(e, "forward_static: cudaGetSymbolAddress");
-        g_scratch_ptr[dev] = static_cast<float*>(p);
-    }
     *out = g_scratch_ptr[dev];
+    if (!*out) return kgb::set_error(KGB_ERR_STATE, "forward_static: no operator was created on device %d", dev);
     return KGB_OK;
 }
 
@@ -81,7 +104,7 @@ extern "C" int kgb_kirchhoff_forward_static(kgb_kirchhoff* op, const float* m_de
         return set_error(KGB_ERR_STATE, "forward_static: current device %d is not the operator's device %d", dev,
                          op->device);
     float* scratch = nullptr;
-    int rc = scratch_for_current_device(&scratch);
+    int rc = scratch_for_device(dev, &scratch);
     if (rc) return rc;
     kgb::KirchDev K = op->view();
     K.mv = scratch;

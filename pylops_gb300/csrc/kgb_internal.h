@@ -114,6 +114,10 @@ int launch_pack_tables_bf16(const KirchDev& K, const float* wsc, const float* ws
 int64_t gather_partial_elems(const KirchDev& K);
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate);
 
+// Look up and cache, for the current device, the address of the static
+// scratch array of kgb_kirchhoff_forward_static (forward_static.cu).
+int static_scratch_prepare();
+
 // Deterministic float64 reductions (solver.cu).
 int launch_dot_f64(const float* a, const float* b, int64_t n, double* out, double* block_scratch,
                    cudaStream_t stream);

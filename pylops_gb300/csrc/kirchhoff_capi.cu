@@ -159,6 +159,7 @@ int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni
         if ((rc = dev_alloc(&op->mv, (size_t)ni, "alloc scaled model"))) break;
         if ((rc = dev_alloc(&op->absmax, kScaleWords, "alloc forward scale block"))) break;
         if ((rc = prepare_kernels(op->view(), op->L))) break;
+        if ((rc = static_scratch_prepare())) break;
         e = cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) { rc = cuda_error(e, "create stream"); break; }
     } while (0);

@@ -1,8 +1,9 @@
 """Generate golden input/output vectors from the PyLops reference itself.
 
-Run in a container where the reference source tree is importable:
+Run where the reference (PyLops) source tree is available, with its
+location in the environment variable PYLOPS_REFERENCE:
 
-    PYTHONPATH=/root/reference python tests/golden/make_golden.py
+    PYLOPS_REFERENCE=<path to the PyLops source tree> python tests/golden/make_golden.py
 
 It writes ``tests/golden/*.npz``.  Every case is built with the reference's
 own public API (``pylops.waveeqprocessing.Kirchhoff`` with ``engine='numpy'``,
@@ -17,6 +18,9 @@ import sys
 import warnings
 
 import numpy as np
+
+if os.environ.get("PYLOPS_REFERENCE"):
+    sys.path.insert(0, os.environ["PYLOPS_REFERENCE"])
 
 warnings.filterwarnings("ignore")
 
