@@ -1,7 +1,9 @@
-"""ctypes wrapper of the C restatement ``oracle/kirch_oracle.c``.
+"""ctypes wrapper of the C restatements ``oracle/kirch_oracle.c`` (the
+numba loop nests) and ``oracle/eikonal_oracle.c`` (the fast-marching tables).
 
-TEST INFRASTRUCTURE ONLY (tests, smoke check and the CPU-baseline leg of
-bench.py).  ``build()`` compiles it with gcc/OpenMP into ``oracle/_build/``.
+TEST INFRASTRUCTURE ONLY (tests, smoke check, the CPU-baseline leg and the
+reference arm of bench.py).  ``build()`` compiles both with gcc/OpenMP into
+one library under ``oracle/_build/``.
 """
 
 import ctypes
@@ -11,16 +13,16 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "kirch_oracle.c")
+SRCS = [os.path.join(HERE, "kirch_oracle.c"), os.path.join(HERE, "eikonal_oracle.c")]
 OUT = os.path.join(HERE, "_build", "libkirch_oracle.so")
 _lib = None
 
 
 def build(force=False):
-    if not force and os.path.exists(OUT) and os.path.getmtime(OUT) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(OUT) and all(os.path.getmtime(OUT) >= os.path.getmtime(s) for s in SRCS):
         return OUT
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
-    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c99", SRC, "-o", OUT + ".tmp", "-lm"]
+    cmd = ["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-std=c99", *SRCS, "-o", OUT + ".tmp", "-lm"]
     subprocess.run(cmd, check=True, capture_output=True)
     os.replace(OUT + ".tmp", OUT)
     return OUT
@@ -45,6 +47,8 @@ def lib():
         L.ko_spread.argtypes = [ctypes.POINTER(_Op), P, P, ctypes.c_int, ctypes.c_int]
         L.ko_gather.argtypes = [ctypes.POINTER(_Op), P, P, ctypes.c_int, ctypes.c_int]
         L.ko_conv.argtypes = [P, P, ctypes.c_int64, ctypes.c_int, P, ctypes.c_int]
+        L.eo_tables.argtypes = [ctypes.c_int, P, P, P, ctypes.c_int, P, P, P, ctypes.c_int]
+        L.eo_tables.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -100,3 +104,24 @@ class COracle:
 
     def rmatvec(self, d):
         return self.gather(self.conv(d, adjoint=True))
+
+
+def eikonal_tables(dims, dsamp, speed, points, order=2, with_trav=True, with_dist=True):
+    """Fast-marching tables of ``points`` (npts, nd) grid coordinates on a grid
+    of shape ``dims`` with spacings ``dsamp``: (trav, dist), each (N, npts)
+    or None, trav with the velocity ``speed`` (shape ``dims``), dist with
+    speed 1."""
+    dims = np.ascontiguousarray(dims, dtype=np.int32)
+    nd = dims.size
+    N = int(np.prod(dims))
+    h = np.ascontiguousarray(dsamp, dtype=np.float64)
+    pts = np.ascontiguousarray(points, dtype=np.int32).reshape(-1, nd)
+    sp = np.ascontiguousarray(np.broadcast_to(np.asarray(speed, np.float64), tuple(dims)))
+    trav = np.empty((N, pts.shape[0])) if with_trav else None
+    dist = np.empty((N, pts.shape[0])) if with_dist else None
+    rc = lib().eo_tables(nd, dims.ctypes.data, h.ctypes.data, sp.ctypes.data, pts.shape[0], pts.ctypes.data,
+                         trav.ctypes.data if trav is not None else None,
+                         dist.ctypes.data if dist is not None else None, order)
+    if rc != 0:
+        raise ValueError("eikonal oracle: bad arguments")
+    return trav, dist

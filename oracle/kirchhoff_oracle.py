@@ -33,6 +33,7 @@ __all__ = [
     "aperture_taper",
     "identify_geometry",
     "traveltime_table_analytic",
+    "traveltime_table_eikonal",
     "angles_from_gradients",
     "pad_wavelet",
     "conv_same",
@@ -120,6 +121,32 @@ def traveltime_table_analytic(z, x, srcs, recs, vel, y=None):
     axes = tuple(range(g["ndims"]))
     grad_s = np.gradient(trav_srcs.reshape(*dims, g["ns"]), *g["dsamp"], axis=axes)
     grad_r = np.gradient(trav_recs.reshape(*dims, g["nr"]), *g["dsamp"], axis=axes)
+    return trav_srcs, trav_recs, dist_srcs, dist_recs, grad_s, grad_r
+
+
+def traveltime_table_eikonal(z, x, srcs, recs, vel, y=None):
+    """Eikonal tables, ``kirchhoff.py:609-638`` (one fast-marching solve per
+    source and per receiver, for the traveltimes with ``vel`` and for the
+    distances with unit speed; the point at ``round((p - origin)/dsamp)``)
+    and the gradient step ``kirchhoff.py:642-648``.  The fast marching is
+    the C restatement ``oracle/eikonal_oracle.c`` of the method scikit-fmm
+    implements (scikit-fmm itself is not available).  Same returns as
+    :func:`traveltime_table_analytic`."""
+    from oracle.kirch_oracle_c import eikonal_tables
+
+    g = identify_geometry(z, x, srcs, recs, y=y)
+    dims = tuple(int(d) for d in g["dims"])
+    vel = np.asarray(vel, dtype=np.float64).reshape(dims)
+    origin, dsamp = g["origin"], g["dsamp"]
+
+    def _points(p):
+        return np.round((p.T - origin) / dsamp).astype(np.int32)
+
+    trav_srcs, dist_srcs = eikonal_tables(dims, dsamp, vel, _points(srcs))
+    trav_recs, dist_recs = eikonal_tables(dims, dsamp, vel, _points(recs))
+    axes = tuple(range(g["ndims"]))
+    grad_s = np.gradient(trav_srcs.reshape(*dims, g["ns"]), *dsamp, axis=axes)
+    grad_r = np.gradient(trav_recs.reshape(*dims, g["nr"]), *dsamp, axis=axes)
     return trav_srcs, trav_recs, dist_srcs, dist_recs, grad_s, grad_r
 
 
@@ -301,7 +328,7 @@ def trav_rmatvec(d, nsnr, nt, ni, itrav, travd):
 # operator wrapper (constructor semantics of kirchhoff.py:234-455)
 # ----------------------------------------------------------------------------
 class KirchhoffOracle:
-    """FP64 restatement of ``Kirchhoff(...)`` for ``mode in {'analytic','byot'}``.
+    """FP64 restatement of ``Kirchhoff(...)`` for ``mode in {'analytic','eikonal','byot'}``.
 
     ``trav``/``amp`` (byot) must be tuples of per-source and per-receiver
     tables, as for the reference's ``travsrcrec`` path.  ``vel`` is the scalar
@@ -328,8 +355,9 @@ class KirchhoffOracle:
             else:
                 self.six = np.zeros(nr * ns)
                 self.rix = np.zeros(nr * ns)
-        if mode == "analytic":
-            ts, tr, ds, dr, gs, gr = traveltime_table_analytic(z, x, srcs, recs, vel, y=y)
+        if mode in ("analytic", "eikonal"):
+            table = traveltime_table_analytic if mode == "analytic" else traveltime_table_eikonal
+            ts, tr, ds, dr, gs, gr = table(z, x, srcs, recs, vel, y=y)
             self.trav_srcs, self.trav_recs = ts, tr
             if dynamic:  # kirchhoff.py:316-330
                 maxdist = 1e-2 * (np.max(ds) + np.max(dr))
@@ -345,7 +373,7 @@ class KirchhoffOracle:
                 gs = np.gradient(self.trav_srcs.reshape(*dims, ns), axis=axes)
                 gr = np.gradient(self.trav_recs.reshape(*dims, nr), axis=axes)
         else:
-            raise NotImplementedError("oracle supports analytic and byot tables")
+            raise NotImplementedError("method must be analytic, eikonal or byot")
         if dynamic:
             self.angle_srcs, self.angle_recs = angles_from_gradients(gs, gr, self.ndims, ni, ns, nr)
         self.h = pad_wavelet(wav, wavcenter)

@@ -159,3 +159,48 @@ def test_nsconv2d_oracle_matches_reference():
     g = load("nsconv2d")
     assert rel(nsconv2d(g["x_in"], g["hs"], g["ihx"], g["ihz"]), g["fwd"]) < 1e-12
     assert rel(nsconv2d(g["y_in"], g["hs"], g["ihx"], g["ihz"], adjoint=True), g["adj"]) < 1e-12
+
+
+def test_eikonal_oracle_matches_analytic_and_the_package_solver():
+    """The oracle's fast-marching tables (oracle/eikonal_oracle.c): within
+    the reference's analytic-vs-eikonal bar (test_kirchhoff.py:163-212,
+    decimal=2) at constant velocity, and equal to the package's own
+    fast-marching solver on a variable-velocity 2-D and 3-D grid (two
+    independent restatements of the same method; tolerance 1e-12)."""
+    from oracle.kirchhoff_oracle import traveltime_table_analytic, traveltime_table_eikonal
+    from pylops_gb300.waveeqprocessing.kirchhoff import Kirchhoff
+
+    z = np.arange(20) * 2.0
+    x = np.arange(12) * 1.0
+    s = np.vstack((np.linspace(0, 11, 6), 2 * np.ones(6)))
+    r = np.vstack((np.linspace(0, 11, 2), 2 * np.ones(2)))
+    te = traveltime_table_eikonal(z, x, s, r, 500 * np.ones((12, 20)))
+    ta = traveltime_table_analytic(z, x, s, r, 500.0)
+    np.testing.assert_array_almost_equal(ta[0], te[0], decimal=2)
+    np.testing.assert_array_almost_equal(ta[1], te[1], decimal=2)
+
+    rng = np.random.default_rng(0)
+    z = np.arange(40) * 5.0
+    x = np.arange(50) * 5.0
+    X, Z = np.meshgrid(x, z, indexing="ij")
+    vel = 1500 + 0.5 * Z + 200 * np.exp(-((X - 120) ** 2 + (Z - 100) ** 2) / (2 * 30.0 ** 2))
+    s = np.vstack((np.linspace(x[0], x[-1], 5), np.zeros(5)))
+    r = np.vstack((np.linspace(x[0], x[-1], 7), np.full(7, 10.0)))
+    a = traveltime_table_eikonal(z, x, s, r, vel)
+    b = Kirchhoff._traveltime_table(z, x, s, r, vel, mode="eikonal")
+    for i in range(4):
+        np.testing.assert_allclose(a[i], b[i], rtol=1e-12, atol=0)
+    for i in (4, 5):
+        for k in range(2):
+            np.testing.assert_allclose(a[i][k], b[i][k], rtol=1e-9, atol=1e-15)
+
+    y = np.arange(8) * 10.0
+    z = np.arange(9) * 10.0
+    x = np.arange(10) * 10.0
+    v3 = 2000 + 300 * rng.random((8, 10, 9))
+    s3 = np.vstack(([20.0, 50.0], [30.0, 60.0], [0.0, 0.0]))
+    r3 = np.vstack(([0.0, 70.0], [10.0, 90.0], [0.0, 0.0]))
+    a = traveltime_table_eikonal(z, x, s3, r3, v3, y=y)
+    b = Kirchhoff._traveltime_table(z, x, s3, r3, v3, y=y, mode="eikonal")
+    for i in range(4):
+        np.testing.assert_allclose(a[i], b[i], rtol=1e-12, atol=0)
