@@ -382,6 +382,9 @@ def run_gpu(args):
         "traces_per_s": round(ngpu * K.nsnr / (ms_step * 1e-3), 1),
         "pair_points_per_s": float(f"{ngpu * 2 * pairs / (ms_step * 1e-3):.4e}"),
         "hbm_fraction": round(value / hbm, 5) if hbm else None,
+        "pair_rate_fraction": _pair_rate(2 * pairs / (ms_step * 1e-3),
+                                         {"spread_fwd_wavelet": pairs / (kern["spread_fwd_wavelet"] * 1e-3),
+                                          "gather_adj": pairs / (kern["gather_adj"] * 1e-3)}, clk),
         "kernels_ms": {k: round(v, 4) for k, v in kern.items()},
         "spread_variant_ms": {str(k): round(v, 3) for k, v in variant_ms.items()},
         "spread_variant": best,
@@ -412,12 +415,61 @@ def run_gpu(args):
                                     / np.linalg.norm(yc[:rows])),
             "adjoint_rel_l2": float(np.linalg.norm(x_mask - xc) / np.linalg.norm(xc)),
         }
+    if rank == 0 and ws == 1 and not args.sources and args.subrecords:
+        # the other configurations, each with its own roofline and clocks
+        del K, m, d, y, dcorr, img
+        torch.cuda.empty_cache()
+        out["subrecords"] = _subrecords(args)
     if rank == 0:
         print(json.dumps(out))
     if dist:
         dist.destroy_process_group()
 
 
+def _subrecords(args):
+    """Records of the 3-D workload (bf16 and float32 weights), the batched
+    LSM workload and the learned-vs-plain LSM comparison, measured in the
+    same run as the headline line.  A record that fails carries its error."""
+    import copy
+
+    import torch
+
+    sub = copy.copy(args)
+    sub.steps = max(1, min(args.steps, 10))
+    jobs = [("kirchhoff3d_bf16_weights", lambda: kirchhoff3d_record(sub, "bfloat16")),
+            ("kirchhoff3d_float32_weights", lambda: kirchhoff3d_record(sub, "float32")),
+            ("batched_lsm", lambda: batch_record(sub)),
+            ("learned_lsm", lambda: lsm_record(sub, args.lsm_models, ("plain", "warm", "learned"), False))]
+    recs = {}
+    for name, job in jobs:
+        t0 = time.perf_counter()
+        try:
+            recs[name] = job()
+        except Exception as e:  # keep the headline line; the record says what failed
+            recs[name] = {"error": f"{type(e).__name__}: {e}"}
+        recs[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return recs
+
+
+
+
+def _pair_rate(step_rate, kernel_rates, clk, instr_per_pair=15):
+    """The instruction roofline of the pair-point loop: achieved pair-points/s
+    over SMs x 128 FP32 lanes x SM clock / the minimum instructions per
+    dynamic pair-point (15: time add, index and fraction, two weight FMAs,
+    interpolation, accumulation)."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+    peak = sms * 128 * mhz * 1e6 / instr_per_pair
+    rec = {"value": round(step_rate / peak, 4), "peak_pair_points_per_s": float(f"{peak:.4e}"),
+           "instr_per_pair_min": instr_per_pair, "sms": sms, "sm_mhz": mhz}
+    for k, v in kernel_rates.items():
+        rec[k] = round(v / peak, 4)
+    return rec
 
 
 def _traffic(kernel: str, workload: str):
@@ -495,6 +547,10 @@ def run_reference(args):
 
 
 def run_batch(args):
+    print(json.dumps(batch_record(args)))
+
+
+def batch_record(args):
     """Batched LSM workload (256 independent 2-D kinematic problems of random
     size, 20 CGLS iterations each, one CUDA-graph launch).  A step is one
     batched CGLS solve; value = compulsory GB/s of its 2*20+2 operator
@@ -514,17 +570,22 @@ def run_batch(args):
         B.cgls(y, niter=args.cgls_iters, tol=0.0)
     torch.cuda.synchronize()
     ts = []
+    clocks = ClockSampler()
+    clocks.start()
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         x, iiter, kold, cost = B.cgls(y, niter=args.cgls_iters, tol=0.0)
         torch.cuda.synchronize()
         ts.append(time.perf_counter() - t0)
+    clk = clocks.stop()
     step = statistics.median(ts)
     napply = 2 * args.cgls_iters + 2
     Bytes = sum(compulsory_bytes(K.ni, K.ns, K.nr, K.nt, s_tab=4) for K in B.ops) / 2 * napply
     rels = [float(c[-1] / c[0]) for c in cost]
-    print(json.dumps({
+    hbm = _peaks().get("hbm_gbs")
+    gbs = Bytes / step / 1e9
+    return {
         "metric": "batched LSM (CGLS) GB/s and problems/s", "value": round(Bytes / step / 1e9, 3), "unit": "GB/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -534,7 +595,12 @@ def run_batch(args):
                    "setup_s": round(t_setup, 2)},
         "problems_per_s": round(len(B.ops) / step, 2),
         "residual_reduction_median": round(float(np.median(rels)), 5),
-    }))
+        "roofline": {"bound": "hbm", "kernel": "batched CGLS iteration (spread, correlation, gather, vector kernels)",
+                     "achieved": round(gbs, 2), "peak": hbm, "unit": "GB/s",
+                     "frac": round(gbs / hbm, 5) if hbm else None, "traffic": None,
+                     "note": "compulsory bytes of the 2 n + 2 operator applications / solve time"},
+        "clocks": clk,
+    }
 
 
 def run_single(args):
@@ -790,6 +856,10 @@ def run_nsconv(args):
 
 
 def run_kirchhoff3d(args):
+    print(json.dumps(kirchhoff3d_record(args, args.weights)))
+
+
+def kirchhoff3d_record(args, weights):
     """The 3-D workload: analytic constant velocity 2500 m/s, dynamic, 100 x 100
     x 120 grid at 10 m, 16 sources on a 4 x 4 and 400 receivers on a 20 x 20
     surface grid, nt = 1001 at 4 ms, 20 Hz Ricker, traveltimes exact and
@@ -817,7 +887,7 @@ def run_kirchhoff3d(args):
     t0 = time.perf_counter()
     K = Kirchhoff(z, x, t, srcs, recs, 2500.0, wav, wc, y=y, mode="analytic", dynamic=True, engine="cuda",
                   dtype="float32")
-    K.set_weight_precision(args.weights)
+    K.set_weight_precision(weights)
     t_setup = time.perf_counter() - t0
     variant_ms = K.autotune()
     # reflectivity: 4 planar dipping reflectors with N(0,1) amplitudes
@@ -852,7 +922,7 @@ def run_kirchhoff3d(args):
         ad.append(e1.elapsed_time(e2))
     clk = clocks.stop()
     step = (statistics.median(fw) + statistics.median(ad)) / 1e3
-    rec_bytes = 8 if args.weights == "bfloat16" else 12
+    rec_bytes = 8 if weights == "bfloat16" else 12
     B = 2 * (rec_bytes * K.ni * (K.ns + K.nr) + 8 * K.ni + 4 * K.nsnr * K.nt)
     # 15 LSQR iterations on the device (one graph launch)
     K.apply_into(m, d)
@@ -889,12 +959,12 @@ def run_kirchhoff3d(args):
         dd = K @ mh_
         K.H @ dd
     e2e = (time.perf_counter() - te) / 3
-    print(json.dumps({
+    return {
         "metric": "Kirchhoff 3-D fwd+adj GB/s vs HBM peak", "value": round(B / step / 1e9, 2), "unit": "GB/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 (weights %s)" % args.weights, "data": "synthetic",
-        "config": {"workload": "kirchhoff3d_analytic_dynamic_100x100x120_16x400_nt1001", "weights": args.weights,
+        "dtype": "f32 (weights %s)" % weights, "data": "synthetic",
+        "config": {"workload": "kirchhoff3d_analytic_dynamic_100x100x120_16x400_nt1001", "weights": weights,
                    "l2": "tables larger than L2", "setup_s": round(t_setup, 1)},
         "kernel_ms": {"forward": round(statistics.median(fw), 3), "adjoint": round(statistics.median(ad), 3)},
         "spread_variant_ms": {str(k_): round(v_, 3) for k_, v_ in variant_ms.items()},
@@ -911,10 +981,14 @@ def run_kirchhoff3d(args):
                 "d2h_bytes_per_step": 4 * (K.ni + K.shape[0])},
         "gpu_launches": args.steps * (K.info()["kernels_forward"] + K.info()["kernels_adjoint"]),
         "clocks": clk,
-    }))
+    }
 
 
 def run_lsm(args):
+    print(json.dumps(lsm_record(args, args.steps, ("plain", "warm", "learned", "psf"), not args.no_cpu_baseline)))
+
+
+def lsm_record(args, n_test, variants, with_cpu):
     """Learned-preconditioned LSM workload: 2-D dynamic eikonal Kirchhoff,
     v(z) = 1500 + 0.6 z on 256 x 512 at 5 m, 48 sources, 256 receivers,
     nt = 1201 at 2 ms, 15 Hz Ricker.  The BF16 U-Net is trained on
@@ -927,8 +1001,8 @@ def run_lsm(args):
 
     clocks = ClockSampler()
     clocks.start()
-    out, ctx = experiment.run(n_train=args.lsm_train, n_test=args.steps, steps=args.lsm_steps, batch=8,
-                              niter=600, variants=("plain", "warm", "learned", "psf"),
+    out, ctx = experiment.run(n_train=args.lsm_train, n_test=n_test, steps=args.lsm_steps, batch=8,
+                              niter=600, variants=variants,
                               stage2_pairs=args.lsm_stage2_pairs, stage2_steps=args.lsm_stage2_steps,
                               steps_net=args.lsm_net_steps,
                               log=lambda *a: print(*a, file=sys.stderr, flush=True), return_objects=True)
@@ -950,16 +1024,16 @@ def run_lsm(args):
     peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops") or 1700.0
     line = {
         "metric": "LSM seconds to 1e-2 relative data residual, learned vs plain GPU LSQR",
-        "value": round(v["learned"]["seconds_median"], 4), "unit": "s", "n_gpus": 1, "steps": args.steps,
+        "value": round(v["learned"]["seconds_median"], 4), "unit": "s", "n_gpus": 1, "steps": n_test,
         "warmup": 1, "ms_per_step": round(v["learned"]["seconds_median"] * 1e3, 2), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 operator, bf16 network", "data": "synthetic",
         "config": {"workload": "learned_lsm_2d_eikonal_dyn_256x512_48x256_nt1201", "train_pairs": args.lsm_train,
                    "train_steps": args.lsm_steps, "stage2_residual_pairs": args.lsm_stage2_pairs,
                    "stage2_steps": args.lsm_stage2_steps, "max_network_directions": 1 + args.lsm_net_steps,
-                   "batch": 8, "held_out_models": args.steps, "tol": 1e-2,
+                   "batch": 8, "held_out_models": n_test, "tol": 1e-2,
                    "l2": "operator tables (478 MB) larger than L2"},
         "plain_lsqr": v["plain"], "warm_start_only": v["warm"], "learned": v["learned"],
-        "psf_image_domain_warm_start": v["psf"],
+        "psf_image_domain_warm_start": v.get("psf"),
         "speedup_vs_plain_median": round(v["learned"]["speedup_vs_plain_median"], 3),
         "train": {k: out.get(k) for k in ("pairs_seconds", "train_seconds", "train_loss_first", "train_loss_last",
                                           "stage2_pairs_seconds", "stage2_train_seconds", "stage2_loss_last",
@@ -972,7 +1046,7 @@ def run_lsm(args):
         "gpu_launches": int(v["learned"]["gpu_launches_median"]),
         "clocks": clk,
     }
-    if not args.no_cpu_baseline:
+    if with_cpu:
         m = tests[0].reshape(-1).astype(np.float64)
         dd = np.random.default_rng(0).standard_normal(op.shape[0])
         rec, _, _, _ = cpu_baseline(op, m, dd, target_s=args.cpu_seconds)
@@ -980,7 +1054,7 @@ def run_lsm(args):
         per_it = compulsory_bytes(op.ni, op.ns, op.nr, op.nt) / (rec["value"] * 1e9)
         line["cpu_baseline"] = {"value": round(per_it * its, 2), "unit": "s", "cores": rec["cores"], "kind": "port",
                                 "sample": rec["sample"] + f"; x {its:.0f} plain LSQR iterations"}
-    print(json.dumps(line))
+    return line
 
 
 def main():
@@ -1009,6 +1083,10 @@ def main():
     ap.add_argument("--lsm-stage2-pairs", type=int, default=2048)
     ap.add_argument("--lsm-stage2-steps", type=int, default=1500)
     ap.add_argument("--lsm-net-steps", type=int, default=6, help="at most this many network directions after the warm start")
+    ap.add_argument("--lsm-models", type=int, default=32,
+                    help="held-out models of the learned-LSM record in the default run")
+    ap.add_argument("--no-subrecords", dest="subrecords", action="store_false",
+                    help="headline workload only (no 3-D, batched and learned-LSM records)")
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--cgls-iters", type=int, default=20)
     args = ap.parse_args()

@@ -167,6 +167,21 @@ def angles_from_gradients(grad_s, grad_r, ndims, ni, ns, nr):
     return a_s, a_r
 
 
+def wavelet_reshaping(wav, dt, dimsrc, dimrec, ndims):
+    """``wavfilter=True`` (``kirchhoff.py:659-681``): the wavelet's spectrum
+    times sqrt(j 2 pi f) in 2-D and -j 2 pi f in 3-D (rfft / irfft of the
+    wavelet's own length); a 2-D source or receiver in a 3-D model raises."""
+    f = np.fft.rfftfreq(len(wav), dt)
+    omega = 2 * np.pi * f
+    if dimsrc == 2 and ndims == 2:
+        mult = np.sqrt(1j * omega)
+    elif ndims == 3 and (dimsrc == 2 or dimrec == 2):
+        raise NotImplementedError("2.D wavelet currently not available")
+    else:
+        mult = -1j * omega
+    return np.fft.irfft(np.fft.rfft(wav, n=len(wav)) * mult, n=len(wav))
+
+
 def pad_wavelet(h, offset):
     """Zero-pad a filter the way ``_Convolve1Dshort`` does
     (``pylops/signalprocessing/convolve1d.py:76-88``) so that a plain
@@ -337,7 +352,7 @@ class KirchhoffOracle:
 
     def __init__(self, z, x, t, srcs, recs, vel, wav, wavcenter, y=None,
                  mode="analytic", dynamic=False, trav=None, amp=None,
-                 aperture=None, angleaperture=90.0):
+                 aperture=None, angleaperture=90.0, wavfilter=False):
         g = identify_geometry(z, x, srcs, recs, y=y)
         self.g = g
         self.ndims, self.nx, self.nz, self.ny = g["ndims"], g["nx"], g["nz"], g["ny"]
@@ -376,7 +391,9 @@ class KirchhoffOracle:
             raise NotImplementedError("method must be analytic, eikonal or byot")
         if dynamic:
             self.angle_srcs, self.angle_recs = angles_from_gradients(gs, gr, self.ndims, ni, ns, nr)
-        self.h = pad_wavelet(wav, wavcenter)
+        # kirchhoff.py:395-398
+        self.wav = wavelet_reshaping(wav, self.dt, srcs.shape[0], recs.shape[0], self.ndims) if wavfilter else wav
+        self.h = pad_wavelet(self.wav, wavcenter)
         self.aperturetap = aperture_taper()
         if aperture is not None and self.ndims == 3:
             aperture = None

@@ -519,13 +519,13 @@ class Kirchhoff(LinearOperator):
         return trav, dist
 
     def _wavelet_reshaping(self, wav, dt, dimsrc, dimrec, dimv):
-        """Wavelet filter (``kirchhoff.py:659-681``)."""
-        f = np.fft.rfftfreq(len(wav), dt)
-        W = np.fft.rfft(wav, n=len(wav))
-        if dimsrc == 2 and dimv == 2:
-            Wfilt = W * np.sqrt(1j * 2 * np.pi * f)
-        elif (dimsrc == 2 or dimrec == 2) and dimv == 3:
+        """``wavfilter=True`` (``kirchhoff.py:659-681``): the omega factor of
+        the wave equation applied to the wavelet's spectrum -- sqrt(j omega)
+        for a 2-D model, -j omega for a 3-D model with 3-D sources and
+        receivers; 2.5-D (2-D points in a 3-D model) is not available."""
+        n = len(wav)
+        jw = 2j * np.pi * np.fft.rfftfreq(n, dt)
+        if dimv == 3 and 2 in (dimsrc, dimrec):
             raise NotImplementedError("2.D wavelet currently not available")
-        elif dimsrc == 3 and dimrec == 3 and dimv == 3:
-            Wfilt = W * (-1j * 2 * np.pi * f)
-        return np.fft.irfft(Wfilt, n=len(wav))
+        factor = np.sqrt(jw) if (dimv == 2 and dimsrc == 2) else -jw
+        return np.fft.irfft(factor * np.fft.rfft(wav, n=n), n=n)

@@ -305,5 +305,25 @@ def main():
     print("wrote nsconv2d")
 
 
+def wavfilter_cases():
+    """15) wavfilter=True: the wavelet reshaped by sqrt(j omega) in 2-D and by
+    -j omega in 3-D (kirchhoff.py:395-398, 659-681)."""
+    rng = np.random.default_rng(2024)
+    K = Kirchhoff(z, x, t, s2d, r2d, v0, wav, wavc, mode="analytic", dynamic=False, wavfilter=True,
+                  engine="numpy")
+    _save("k2d_wavfilter", K, rng.standard_normal(K.ni), rng.standard_normal(K.shape[0]),
+          extra=dict(vel_scalar=v0, wavc=wavc, wavfilter_in=True, wav_in=wav), geometry=geom2d())
+    s3d6 = s3d[:, ::4].copy()
+    K = Kirchhoff(z, x, t, s3d6, r3d, v0, wav, wavc, y=y, mode="analytic", dynamic=True,
+                  angleaperture=45.0, wavfilter=True, engine="numpy")
+    _save("k3d_wavfilter", K, rng.standard_normal(K.ni), rng.standard_normal(K.shape[0]),
+          extra=dict(vel_scalar=v0, wavc=wavc, angleaperture_in=45.0, wavfilter_in=True, wav_in=wav),
+          geometry=dict(z=z, x=x, t=t, srcs=s3d6, recs=r3d, y=y))
+
+
+CASES = {"all": main, "wavfilter": wavfilter_cases}
+
 if __name__ == "__main__":
-    sys.exit(main())
+    # python make_golden.py [all|wavfilter ...]: the named groups (default all)
+    for name in (sys.argv[1:] or ["all", "wavfilter"]):
+        CASES[name]()

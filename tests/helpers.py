@@ -26,7 +26,11 @@ def kwargs_from_golden(g):
         kw["angleaperture"] = float(g["angleaperture_in"])
     elif bool(g["dynamic"]):
         kw["angleaperture"] = None if np.allclose(g["angleaperture"], np.deg2rad([0.0, 1000.0])) else 90.0
-    args = (g["z"], g["x"], g["t"], g["srcs"], g["recs"], vel, g["wav"], int(g["wavc"]))
+    wav = g["wav"]
+    if "wavfilter_in" in g:  # the golden's wav is the reshaped one; the constructor gets the original
+        kw["wavfilter"] = True
+        wav = g["wav_in"]
+    args = (g["z"], g["x"], g["t"], g["srcs"], g["recs"], vel, wav, int(g["wavc"]))
     return args, kw
 
 
@@ -36,4 +40,5 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-GOLDEN_CASES = ["k2d_kin", "k2d_dyn_ap", "k2d_dyn_noap", "k3d_kin", "k3d_dyn", "k2d_dyn_byot", "k2d_kin_f32"]
+GOLDEN_CASES = ["k2d_kin", "k2d_dyn_ap", "k2d_dyn_noap", "k3d_kin", "k3d_dyn", "k2d_dyn_byot", "k2d_kin_f32",
+                "k2d_wavfilter", "k3d_wavfilter"]

@@ -8,7 +8,8 @@ import pytest
 from oracle import kirchhoff_oracle as ko
 from tests.conftest import GOLDEN
 
-CASES = ["k2d_kin", "k2d_dyn_ap", "k2d_dyn_noap", "k3d_kin", "k3d_dyn", "k2d_dyn_byot", "k2d_kin_f32"]
+CASES = ["k2d_kin", "k2d_dyn_ap", "k2d_dyn_noap", "k3d_kin", "k3d_dyn", "k2d_dyn_byot", "k2d_kin_f32",
+         "k2d_wavfilter", "k3d_wavfilter"]
 
 
 def load(name):
@@ -31,7 +32,11 @@ def build(g):
         kw["angleaperture"] = float(g["angleaperture_in"])
     elif bool(g["dynamic"]):
         kw["angleaperture"] = None if np.allclose(g["angleaperture"], np.deg2rad([0.0, 1000.0])) else 90.0
-    return ko.KirchhoffOracle(g["z"], g["x"], g["t"], g["srcs"], g["recs"], vel, g["wav"],
+    wav = g["wav"]
+    if "wavfilter_in" in g:  # the golden's wav is the reshaped one
+        kw["wavfilter"] = True
+        wav = g["wav_in"]
+    return ko.KirchhoffOracle(g["z"], g["x"], g["t"], g["srcs"], g["recs"], vel, wav,
                               int(g["wavc"]), dynamic=bool(g["dynamic"]), **kw)
 
 
@@ -48,6 +53,7 @@ def test_tables_match_reference(name):
     np.testing.assert_allclose(K.aperture, g["aperture"])
     np.testing.assert_allclose(K.angleaperture, g["angleaperture"])
     np.testing.assert_allclose(K.aperturetap, g["aperturetap"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(K.wav, g["wav"], rtol=1e-12, atol=1e-14)
     if K.dynamic:
         for k in ("amp_srcs", "amp_recs", "angle_srcs", "angle_recs", "vel"):
             np.testing.assert_allclose(getattr(K, k), g[k], rtol=1e-12, atol=1e-14, err_msg=k)
