@@ -263,7 +263,7 @@ def run_gpu(args):
 
     # forward-kernel variants, timed on this workload; the fastest is used
     variant_ms = {}
-    for v in ((0, 1, 2) if args.variant < 0 else (args.variant,)):
+    for v in ((0, 1, 2, 3) if args.variant < 0 else (args.variant,)):
         K.set_spread_variant(v)
         step()
         torch.cuda.synchronize()

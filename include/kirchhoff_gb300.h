@@ -149,10 +149,14 @@ int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x_dev, float* y_dev, i
                           void* stream);
 
 /* Choose the forward (spreading) kernel: 0 = fixed-point shared-memory
- * accumulation (the default, fastest on every workload measured),
- * 1 = warp-binned (one trace per warp), 2 = warp-binned with two traces per
- * warp.  All three are deterministic and give the same result up to float32
- * rounding.  The host-buffer forward overlaps its copies with variant 0 only.
+ * accumulation (the default, fastest on every workload measured; it uses
+ * the split accumulation of two fire-and-forget atomics per contribution
+ * when the operator's bins receive at most 65535 contributions each, see
+ * kgb_kirchhoff_info), 1 = warp-binned (one trace per warp), 2 = warp-binned
+ * with two traces per warp, 3 = fixed-point with the carry accumulation
+ * only (the same traces as 0 bit for bit).  All are deterministic and give
+ * the same result up to float32 rounding.  The host-buffer forward overlaps
+ * its copies with variants 0 and 3 only.
  * No reference counterpart
  * (the reference has one CUDA kernel per mode, _kirchhoff_cuda.py:55-298);
  * used by the tile autotuner. */
@@ -162,7 +166,8 @@ int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant);
  * {ns, nr, nt, ni, fixed-point fraction bits, padded wavelet length,
  *  offset-aperture gate active, dynamic, all times non-negative,
  *  adjoint receiver splits, kernels per forward, kernels per adjoint,
- *  spread variant, 0...}. */
+ *  spread variant, split accumulation used by the forward (0/1), most
+ *  contributions any forward bin can receive, 0}. */
 int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* info16);
 
 /* Deterministic float64 reductions of float32 vectors (fixed launch shape

@@ -124,4 +124,51 @@ __device__ __forceinline__ long long fixed_get(const uint32_t* __restrict__ row,
     return (long long)(u - kFixedBias);
 }
 
+// ---------------------------------------------------------------------------
+// Split accumulation: the same exact integer sums without returned atomics
+// or carries, for traces whose bins provably receive at most
+// kSplitMaxCount contributions each (counted once per operator when its
+// tables are set, spread_count_kernel).
+//
+// Each bin keeps two 32-bit words, both cleared to 0:
+//   L = sum of x           mod 2^32   (low plane, [0, nt_pad))
+//   H = sum of floor(x/2^16) mod 2^32 (high plane, [nt_pad, 2 nt_pad))
+// each added with one fire-and-forget shared atomic (the value is not read
+// back).  With R = sum of (x mod 2^16), 0 <= R < count * 2^16 <= 2^32, so
+// R = (L - 2^16 H) mod 2^32 exactly, and S = 2^16 H + R mod 2^48 is the
+// exact sum when |S| < 2^47 -- true for at most kSplitMaxCount
+// contributions of |x| < 2^31.  Larger contributions (the points the scale
+// marks wide) are added exactly with 64-bit global atomics into a per-trace
+// accumulator instead (split_add_wide).  Integer sums commute, so the
+// result equals the carry scheme's bit for bit.
+// ---------------------------------------------------------------------------
+constexpr unsigned kSplitMaxCount = 65535u;
+
+__device__ __forceinline__ void split_clear(uint32_t* __restrict__ acc, int nrows, int nt_pad, int t, int nthreads) {
+    uint4* a4 = reinterpret_cast<uint4*>(acc);  // 2 nt_pad words per row, nt_pad a multiple of 4
+    for (int k = t; k < nrows * nt_pad / 2; k += nthreads) a4[k] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+// Add x (|x| < 2^31) to bin `bin`; x == 0 touches nothing.
+__device__ __forceinline__ void split_add(uint32_t* __restrict__ row, int nt_pad, int bin, int x) {
+    if (x != 0) {
+        atomicAdd(row + bin, (uint32_t)x);
+        atomicAdd(row + nt_pad + bin, (uint32_t)(x >> 16));
+    }
+}
+
+// A wide contribution (scaled value v, |v| < 2^62, rounded to the nearest
+// integer) into the trace's 64-bit global accumulator.
+__device__ __forceinline__ void split_add_wide(unsigned long long* __restrict__ wrow, int bin, float v) {
+    const long long x = __float2ll_rn(v);
+    if (x != 0) atomicAdd(wrow + bin, (unsigned long long)x);
+}
+
+__device__ __forceinline__ long long split_get(const uint32_t* __restrict__ row, int nt_pad, int bin) {
+    const uint32_t L = row[bin], H = row[nt_pad + bin];
+    const uint32_t R = L - (H << 16);
+    const unsigned long long u = ((unsigned long long)H << 16) + R;
+    return (long long)(u << 16) >> 16;  // sign-extend the 48-bit sum
+}
+
 }  // namespace kgb

@@ -109,6 +109,11 @@ extern "C" int kgb_kirchhoff_forward_static(kgb_kirchhoff* op, const float* m_de
     kgb::KirchDev K = op->view();
     K.mv = scratch;
     K.absmax = reinterpret_cast<unsigned*>(scratch + kStaticMaxImagePoints);
+    // the split accumulation keeps wide contributions in operator memory;
+    // this entry point uses the carry accumulation, whose traces are the
+    // same bit for bit, and no scratch beyond the static array
+    K.split_ok = 0;
+    K.wacc = nullptr;
     return kgb::launch_spread(K, op->dynamic, op->has_gate, m_dev, d_dev, op->h_dev, op->L, true,
                               (cudaStream_t)stream);
 }

@@ -37,7 +37,8 @@ struct KirchDev {
     int frac_bits;
     int nonneg;        // every ts + tr >= 0: index math without the negative-time case
     float wmax;        // bound on |dynamic weight| (1 for kinematic), for the fixed-point scale
-    int spread_variant; // 0: fixed-point shared-memory atomics (the default); 1/2: warp-binned, 1/2 traces per warp
+    int spread_variant; // 0: fixed-point shared-memory atomics (the default); 1/2: warp-binned, 1/2 traces per warp;
+                        // 3: fixed-point with the carry accumulation only
     float* mv;         // scratch: m * 2/v per application (ni)
     unsigned* absmax;  // scratch: the forward's scale block (kScaleWords, see fixed_acc.cuh) per application
     const int32_t* tsq;
@@ -74,6 +75,14 @@ struct KirchDev {
     // an earlier launch on an ordered stream already did)
     int g0, g1;
     int prepass;
+    // fixed-point spread: split accumulation (two fire-and-forget shared
+    // atomics per contribution) when every bin of the operator receives at
+    // most kSplitMaxCount contributions (split_ok, counted when the tables
+    // were set) and the 64-bit accumulator of wide contributions wacc
+    // ([ns*nr][nt], zero between applications) exists
+    int split_ok;
+    unsigned long long* wacc;
+    unsigned* count_out;  // spread_count: the largest contribution count of any bin
 };
 
 // u32 words of the forward's fixed-point scale block: [0] bits of max |mv|,
@@ -102,6 +111,11 @@ int launch_pack_tables(const KirchDev& K, const float* wsc, const float* wss, co
 // operator, 0 when the forward does not run that kernel (binned variants,
 // single traveltime table, traces too long for shared memory).
 int spread_group_size(const KirchDev& K, int L);
+// Largest number of contributions any bin of the fixed-point spread can
+// receive (valid time and nonzero weight, any model), into *count (device
+// word, cleared by the call); 0xffffffff when the forward's spread does not
+// run in groups of 8 receivers (L: the padded wavelet length of the forward).
+int launch_spread_count(const KirchDev& K, bool dynamic, bool gate, int L, unsigned* count, cudaStream_t stream);
 // The forward's prepass alone (mv = m * 2/v or m, and its scale block).
 int launch_spread_prepass(const KirchDev& K, bool dynamic, const float* m, cudaStream_t stream);
 // Union ranges of groups of 8 receivers from the per-receiver ranges.
@@ -159,6 +173,10 @@ struct kgb_kirchhoff {
     int2* stab2 = nullptr;     // bf16-weight records (when bf16_weights), see KirchDev
     int2* rtab2 = nullptr;
     bool bf16_weights = false;
+    unsigned long long* wacc = nullptr;  // wide contributions of the split spread, see KirchDev
+    bool split_ok = false;
+    unsigned* count_buf = nullptr;       // one device word for launch_spread_count
+    unsigned max_bin_count = 0;          // its last result
     int32_t* tq1 = nullptr;    // single traveltime table (trace-major), see KirchDev
     float* tw1 = nullptr;
     float* dcorr = nullptr;    // scratch: correlated data for the adjoint, interleaved pairs (2 x ndata)
@@ -186,6 +204,7 @@ struct kgb_kirchhoff {
         K.tq1 = tq1; K.tw1 = tw1;
         K.stab2 = bf16_weights ? stab2 : nullptr; K.rtab2 = bf16_weights ? rtab2 : nullptr;
         K.g0 = 0; K.g1 = 1 << 30; K.prepass = 1;
+        K.split_ok = split_ok ? 1 : 0; K.wacc = wacc; K.count_out = count_buf;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "fixed_acc.cuh"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -107,6 +108,28 @@ static int repack(kgb_kirchhoff* op) {
     return KGB_OK;
 }
 
+// Whether the fixed-point spread may use split accumulation: count, once
+// per table change, the most contributions any bin can receive, and keep
+// the 64-bit accumulator of wide contributions (zeroed once; each forward
+// leaves it zero) when that count is small enough.
+static int update_split(kgb_kirchhoff* op) {
+    op->split_ok = false;
+    if (!op->trav_ready || (op->dynamic && !op->dyn_ready) || op->tq1) return KGB_OK;
+    int rc;
+    if (!op->count_buf && (rc = dev_alloc(&op->count_buf, 1, "alloc count word"))) return rc;
+    if ((rc = launch_spread_count(op->view(), op->dynamic, op->has_gate, op->L, op->count_buf, nullptr))) return rc;
+    unsigned count = 0u;
+    KGB_CUDA_TRY(cudaMemcpy(&count, op->count_buf, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    op->max_bin_count = count;
+    if (count > kSplitMaxCount) return KGB_OK;
+    if (!op->wacc) {
+        if ((rc = dev_alloc(&op->wacc, (size_t)op->ndata(), "alloc wide accumulator"))) return rc;
+        KGB_CUDA_TRY(cudaMemset(op->wacc, 0, (size_t)op->ndata() * sizeof(unsigned long long)));
+    }
+    op->split_ok = true;
+    return KGB_OK;
+}
+
 }  // namespace kgb
 
 using namespace kgb;
@@ -179,7 +202,7 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
                     op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
                     op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng, op->tq1, op->tw1,
-                    op->stab2, op->rtab2, op->grng};
+                    op->stab2, op->rtab2, op->grng, op->wacc, op->count_buf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);
@@ -241,7 +264,8 @@ int kgb_kirchhoff_set_traveltimes(kgb_kirchhoff* op, const double* ts, const dou
     op->nonneg = (int64_t)qmin_s + (int64_t)qmin_r >= 0;
     (void)mins; (void)minr;
     op->trav_ready = true;
-    return repack(op);
+    int rc = repack(op);
+    return rc ? rc : update_split(op);
 }
 
 int kgb_kirchhoff_set_weight_precision(kgb_kirchhoff* op, int bf16) {
@@ -258,6 +282,7 @@ int kgb_kirchhoff_set_weight_precision(kgb_kirchhoff* op, int bf16) {
             return rc;
         }
     }
+    if (op->bf16_weights != was) return update_split(op);
     return KGB_OK;
 }
 
@@ -429,7 +454,8 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const doub
     op->has_gate = gate;
     op->wmax = (float)std::max(wmax, 1e-30);
     op->dyn_ready = true;
-    return repack(op);
+    rc = repack(op);
+    return rc ? rc : update_split(op);
 }
 
 static int check_ready(const kgb_kirchhoff* op) {
@@ -575,7 +601,8 @@ int kgb_kirchhoff_adjoint_host(kgb_kirchhoff* op, const float* d_host, float* m_
 
 int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant) {
     if (!op) return set_error(KGB_ERR_STATE, "null operator");
-    if (spread_variant < 0 || spread_variant > 2) return set_error(KGB_ERR_VALUE, "set_variant: spread variant must be 0, 1 or 2");
+    if (spread_variant < 0 || spread_variant > 3)
+        return set_error(KGB_ERR_VALUE, "set_variant: spread variant must be 0, 1, 2 or 3");
     op->spread_variant = spread_variant;
     return KGB_OK;
 }
@@ -592,6 +619,8 @@ int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
     s[10] = 3;
     s[11] = 2 + (s[9] > 1 ? 1 : 0);
     s[12] = op->spread_variant;
+    s[13] = op->split_ok ? 1 : 0;
+    s[14] = op->max_bin_count;
     return KGB_OK;
 }
 

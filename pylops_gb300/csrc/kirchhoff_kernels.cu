@@ -280,13 +280,26 @@ __host__ __device__ __forceinline__ float spread_wfactor(float wmax, bool nonneg
 // source and at least one receiver of the group have a nonzero weight,
 // loads the source-side entry once per point and, for each of its R traces,
 // accumulates the two contributions v*(1-w), v*w into that trace's shared-
-// memory time bins as 64-bit fixed point (fixed_add: each contribution
-// scaled by a power of two chosen from a bound on |v|, rounded to an integer
-// of at most kFixedBits bits plus sign and added exactly), so the trace is
-// independent of the order in which threads arrive.  The finished traces
-// are converted back to float, convolved with the wavelet in shared memory
-// and written once.
-template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false>
+// memory time bins as 64-bit fixed point (each contribution scaled by a
+// power of two chosen from a bound on |v|, rounded to an integer of at most
+// kFixedBits bits plus sign and added exactly), so the trace is independent
+// of the order in which threads arrive.  The finished traces are converted
+// back to float, convolved with the wavelet in shared memory and written
+// once.
+//
+// ACC selects how a bin adds:
+//   kAccCarry  one returned 32-bit atomic per contribution plus a rare carry
+//              (fixed_add), valid for any number of contributions per bin;
+//   kAccSplit  two fire-and-forget 32-bit atomics (split_add), for operators
+//              whose bins receive at most kSplitMaxCount contributions; wide
+//              contributions go to the 64-bit global accumulator K.wacc;
+//   kAccCount  no model: counts the contributions every bin can receive
+//              (valid time, nonzero weight) and writes the largest count of
+//              the CTA's bins to *K.count_out (atomicMax).
+// kAccCarry and kAccSplit give bitwise identical traces.
+constexpr int kAccCarry = 0, kAccSplit = 1, kAccCount = 2;
+
+template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false, int ACC = kAccCarry>
 __global__ void __launch_bounds__(kSpreadThreads, 2)
 spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__ y,
               const float* __restrict__ h, int L, int nt_pad, int fuse) {
@@ -308,12 +321,15 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     if (g >= ngroups || g >= K.g1) return;
     const int r0 = g * R;
     const int nrr = min(R, K.nr - r0);
-    fixed_clear(acc32, R, nt_pad, tid, blockDim.x);
-    if (fuse) {
+    __shared__ int wide_any;  // kAccSplit: a wide contribution went to K.wacc
+    if (ACC == kAccCarry) fixed_clear(acc32, R, nt_pad, tid, blockDim.x);
+    else split_clear(acc32, R, nt_pad, tid, blockDim.x);
+    if (tid == 0) wide_any = 0;
+    if (fuse && ACC != kAccCount) {
         for (int k = tid; k < fir_lpad(L); k += blockDim.x) hs[k] = k < L ? h[k] : 0.f;
         for (int k = tid; k < fir_span(L, K.nt); k += blockDim.x) ftr[k] = 0.f;
     }
-    const int e = (int)K.absmax[1];  // spread_scale_kernel
+    const int e = ACC == kAccCount ? 0 : (int)K.absmax[1];  // spread_scale_kernel
     const float S = ldexpf(1.f, e);
     // first depth of each receiver's gate, in shared memory (read as a warp
     // broadcast; held in registers it costs spills)
@@ -335,26 +351,44 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
         for (int r = 0; r < R; ++r)
             re[r] = (FULL || r < nrr) ? load_entry<DYN, false, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2)
                                       : zero_entry();
+        if (WIDE && ACC == kAccSplit && !wide_any) wide_any = 1;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int s = se.t + re[r].t;
             float val = v;
+            float wt = 1.f;
             if (DYN) {
-                float wt = fmaf(se.c, re[r].c, se.s * re[r].s);
+                wt = fmaf(se.c, re[r].c, se.s * re[r].s);
                 if (GATE && izp < izmin[r]) wt = 0.f;
                 val *= wt;
             }
             // straight-line code: an invalid time or a missing receiver
-            // gives zero contributions, which fixed_add skips
+            // gives zero contributions, which the adds skip
             const bool ok = (FULL || r < nrr) && fp.valid(s);
             const int it = fp.index(s);
+            uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
+            if (ACC == kAccCount) {
+                if (ok && (!DYN || wt != 0.f)) {
+                    atomicAdd(row + it, 1u);
+                    atomicAdd(row + it + 1, 1u);
+                }
+                continue;
+            }
             const float w = fp.frac(s, it);
             const float v1 = val * w;
             const float v0 = val - v1;
-            uint32_t* row = acc32 + (size_t)r * 2 * nt_pad;
-            if (WIDE) {
+            if (WIDE && ACC == kAccSplit) {
+                unsigned long long* wrow = K.wacc + ((size_t)is * K.nr + r0 + r) * nt;
+                if (ok) {
+                    split_add_wide(wrow, it, v0);
+                    split_add_wide(wrow, it + 1, v1);
+                }
+            } else if (WIDE) {
                 fixed_add_wide(row, nt_pad, it, ok ? v0 : 0.f);
                 fixed_add_wide(row, nt_pad, it + 1, ok ? v1 : 0.f);
+            } else if (ACC == kAccSplit) {
+                split_add(row, nt_pad, it, ok ? __float2int_rn(v0) : 0);
+                split_add(row, nt_pad, it + 1, ok ? __float2int_rn(v1) : 0);
             } else {
                 fixed_add(row, nt_pad, it, ok ? __float2int_rn(v0) : 0);
                 fixed_add(row, nt_pad, it + 1, ok ? __float2int_rn(v1) : 0);
@@ -362,7 +396,7 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
         }
     };
     auto point = [&](int64_t ii, int64_t colp, int izp, float v) {
-        if (fixed_wide(v, spread_wfactor(K.wmax, NONNEG))) {
+        if (ACC != kAccCount && fixed_wide(v, spread_wfactor(K.wmax, NONNEG))) {
             if (nrr == R) point_t(std::true_type{}, std::true_type{}, ii, colp, izp, v);
             else point_t(std::false_type{}, std::true_type{}, ii, colp, izp, v);
         } else if (nrr == R) {
@@ -371,6 +405,8 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
             point_t(std::false_type{}, std::false_type{}, ii, colp, izp, v);
         }
     };
+    // scaled model value of point ii (every point counts as nonzero when counting)
+    auto model = [&](int64_t ii) { return ACC == kAccCount ? 1.f : __ldg(K.mv + ii) * S; };
     if (DYN && R == 8 && K.grng) {
         // a warp per depth column, over the depths where both the source
         // and at least one receiver of this group of 8 have a nonzero weight
@@ -383,7 +419,7 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
             const int hi = min((int)(a >> 16), (int)(b >> 16));
             for (int iz = lo + lane; iz < hi; iz += 32) {
                 const int64_t ii = c * K.nz + iz;
-                const float v = __ldg(K.mv + ii) * S;
+                const float v = model(ii);
                 if (v != 0.f) point(ii, c, iz, v);
             }
         }
@@ -402,17 +438,43 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
                 iz -= K.nz;
                 ++col;
             }
-            const float v = __ldg(K.mv + ii) * S;
+            const float v = model(ii);
             if (v == 0.f) continue;  // zero model point: no contribution
             if (DYN && !in_range(K.srng, (size_t)is * ncol + colp, izp)) continue;  // source weight zero here
             point(ii, colp, izp, v);
         }
     }
     __syncthreads();
+    if (ACC == kAccCount) {
+        // the largest count of the CTA's bins (low plane of each row)
+        unsigned mx = 0u;
+        for (int r = 0; r < nrr; ++r)
+            for (int n = tid; n < nt; n += blockDim.x) mx = max(mx, acc32[(size_t)r * 2 * nt_pad + n]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, o));
+        if ((tid & 31) == 0 && mx) atomicMax(K.count_out, mx);
+        return;
+    }
     const float invS = ldexpf(1.f, -e);
+    const bool wide_rows = ACC == kAccSplit && wide_any;
     float* xt = fuse ? ftr + fir_q(L) : ftr;
     for (int r = 0; r < nrr; ++r) {
-        for (int n = tid; n < nt; n += blockDim.x) xt[n] = (float)fixed_get(acc32 + (size_t)r * 2 * nt_pad, nt_pad, n) * invS;
+        const uint32_t* arow = acc32 + (size_t)r * 2 * nt_pad;
+        unsigned long long* wrow = wide_rows ? K.wacc + ((size_t)is * K.nr + r0 + r) * nt : nullptr;
+        for (int n = tid; n < nt; n += blockDim.x) {
+            long long q;
+            if (ACC == kAccSplit) {
+                q = split_get(arow, nt_pad, n);
+                if (wide_rows) {
+                    // the wide part, read and cleared for the next application
+                    q += (long long)wrow[n];
+                    wrow[n] = 0ull;
+                }
+            } else {
+                q = fixed_get(arow, nt_pad, n);
+            }
+            xt[n] = (float)q * invS;
+        }
         __syncthreads();
         // the convolved trace goes to this receiver's accumulator row, which
         // is no longer needed (2 * nt_pad >= fir_out(nt) floats)
@@ -796,9 +858,19 @@ int launch_prepass(const KirchDev& K, const float* m, cudaStream_t stream, float
 template <bool DYN, bool GATE, bool NONNEG, int R, bool HALF = false>
 int spread_launch_r(const KirchDev& K, const float* m, float* y, const float* h, int L, bool fuse,
                     const SpreadShape& sh, cudaStream_t stream, bool prepare_only) {
-    auto kern = spread_kernel<DYN, GATE, NONNEG, R, HALF>;
+    // split accumulation (R = 8 only): see spread_kernel
+    constexpr int ACC2 = R == 8 ? kAccSplit : kAccCarry;
+    const bool split = R == 8 && K.split_ok && K.wacc != nullptr && K.spread_variant != 3;
+    auto kern = split ? spread_kernel<DYN, GATE, NONNEG, R, HALF, ACC2> : spread_kernel<DYN, GATE, NONNEG, R, HALF>;
     if (prepare_only) {
-        KGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
+        KGB_CUDA_TRY(cudaFuncSetAttribute(spread_kernel<DYN, GATE, NONNEG, R, HALF>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
+        if (R == 8) {
+            KGB_CUDA_TRY(cudaFuncSetAttribute(spread_kernel<DYN, GATE, NONNEG, R, HALF, ACC2>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
+            KGB_CUDA_TRY(cudaFuncSetAttribute(spread_kernel<DYN, GATE, NONNEG, R, HALF, kAccCount>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh.smem));
+        }
         return KGB_OK;
     }
     if (K.prepass) {
@@ -886,6 +958,29 @@ int spread_dispatch(const KirchDev& K, bool dynamic, bool gate, const float* m, 
         return spread_dispatch_nn<true, false>(K, m, y, h, L, fuse, stream, prep);
     }
     return spread_dispatch_nn<false, false>(K, m, y, h, L, fuse, stream, prep);
+}
+
+template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
+int spread_count_t(const KirchDev& K, int L, unsigned* count, cudaStream_t stream) {
+    const SpreadShape sh = spread_shape(K, L);
+    if (sh.R != 8) {  // the split kernels exist for groups of 8 receivers only
+        KGB_CUDA_TRY(cudaMemsetAsync(count, 0xff, sizeof(unsigned), stream));
+        return KGB_OK;
+    }
+    KirchDev Kc = K;
+    Kc.count_out = count;
+    const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
+    const int64_t blocks = (int64_t)K.ns * ((K.nr + 7) / 8);
+    spread_kernel<DYN, GATE, NONNEG, 8, HALF, kAccCount>
+        <<<(unsigned)blocks, kSpreadThreads, sh.smem, stream>>>(Kc, fp, nullptr, nullptr, L, sh.nt_pad, 0);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+template <bool DYN, bool GATE, bool HALF = false>
+int spread_count_nn(const KirchDev& K, int L, unsigned* count, cudaStream_t stream) {
+    if (K.nonneg) return spread_count_t<DYN, GATE, true, HALF>(K, L, count, stream);
+    return spread_count_t<DYN, GATE, false, HALF>(K, L, count, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -1231,7 +1326,7 @@ int spread1_dispatch_t(const KirchDev& K, const float* m, float* y, const float*
     if (prep && binned_fits) {
         int rc = spread1_binned_launch<FIXED>(K, m, y, h, L, fuse, stream, true);
         if (rc) return rc;
-    } else if (!prep && K.spread_variant != 0 && binned_fits) {
+    } else if (!prep && (K.spread_variant == 1 || K.spread_variant == 2) && binned_fits) {
         return spread1_binned_launch<FIXED>(K, m, y, h, L, fuse, stream, false);
     }
     const size_t fixed = (size_t)(fir_span(L, K.nt) + fir_lpad(L)) * sizeof(float);
@@ -1338,6 +1433,21 @@ int wavelet_blocks_per_sm(int threads, size_t smem) {
 
 }  // namespace
 
+int launch_spread_count(const KirchDev& K, bool dynamic, bool gate, int L, unsigned* count, cudaStream_t stream) {
+    KGB_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(unsigned), stream));
+    if (K.ns <= 0 || K.nr <= 0 || K.tq1) return KGB_OK;
+    if (dynamic && K.stab2) {
+        if (gate) return spread_count_nn<true, true, true>(K, L, count, stream);
+        return spread_count_nn<true, false, true>(K, L, count, stream);
+    }
+    if (dynamic) {
+        if (gate) return spread_count_nn<true, true>(K, L, count, stream);
+        return spread_count_nn<true, false>(K, L, count, stream);
+    }
+    return spread_count_nn<false, false>(K, L, count, stream);
+}
+
+
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
     int bps;
@@ -1386,7 +1496,7 @@ int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, fl
 }
 
 int spread_group_size(const KirchDev& K, int L) {
-    if (K.tq1 || K.spread_variant != 0 || K.ns <= 0 || K.nr <= 0 || K.nt <= 0) return 0;
+    if (K.tq1 || K.spread_variant == 1 || K.spread_variant == 2 || K.ns <= 0 || K.nr <= 0 || K.nt <= 0) return 0;
     return spread_shape(K, L).R;
 }
 

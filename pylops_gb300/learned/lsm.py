@@ -21,6 +21,7 @@ reference's ``lsqr(Kop * Diagonal(p), d, x0=z0)``.
 from __future__ import annotations
 
 import math
+import sys
 import time
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
@@ -144,7 +145,7 @@ def train(net: UNet, X, M, steps: int, batch: int = 8, lr: float = 1e-3, lr_fina
         cur = lr_final + 0.5 * (lr - lr_final) * (1 + math.cos(math.pi * k / max(steps - 1, 1)))
         losses[k] = net.train_step(xb, mb, lr=cur)
         if log_every and (k % log_every == 0 or k == steps - 1):
-            print(f"step {k:5d} lr {cur:.2e} loss {float(losses[k]):.4f}", flush=True)
+            print(f"step {k:5d} lr {cur:.2e} loss {float(losses[k]):.4f}", file=sys.stderr, flush=True)
     net.check_errors()
     return losses.cpu().tolist()
 

@@ -328,7 +328,8 @@ class Kirchhoff(LinearOperator):
         v = (ctypes.c_int64 * 16)()
         _native.check(_native.lib().kgb_kirchhoff_info(self._h, v))
         keys = ("ns", "nr", "nt", "ni", "frac_bits", "wavelet_len", "offset_gate", "dynamic", "nonneg",
-                "adjoint_splits", "kernels_forward", "kernels_adjoint", "spread_variant")
+                "adjoint_splits", "kernels_forward", "kernels_adjoint", "spread_variant", "spread_split",
+                "max_bin_count")
         return {k: int(v[i]) for i, k in enumerate(keys)}
 
     def set_spread_variant(self, variant: int) -> None:
