@@ -102,6 +102,38 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_srcs_host,
                               const double* aperturetap21_host, const int64_t* six_host,
                               const int64_t* rix_host);
 
+/* Build the tables on the device instead of uploading them: mode 0 =
+ * analytic (constant velocity *vel, nvel = 1; 2-D or 3-D), mode 1 = eikonal
+ * (2-D; vel of ni values in the image order, or one constant), on the
+ * operator's grid given by its axes (y of ny samples in 3-D, else NULL; x;
+ * z) with sources and receivers (ndim, ns) / (ndim, nr) in the reference's
+ * coordinate order ((x, z) or (y, x, z)).  Traveltimes, distances, their
+ * gradients, angles and amplitudes are computed as the reference's
+ * constructor does and go straight into the operator's fixed-point and
+ * folded-weight rows; dynamic operators also take the apertures, the taper
+ * and six/rix as in kgb_kirchhoff_set_dynamic.  *maxdist_out receives
+ * 1e-2 (max dist_s + max dist_r).  The float64 rows stay on the device for
+ * kgb_kirchhoff_get_table.  Eikonal tables solve the fast-marching
+ * equations of kgb_eikonal_tables by sweeping; they agree with it to
+ * rounding where both converge to the same upwind solution.
+ * Replaces: Kirchhoff._traveltime_table and the table set-up of
+ * Kirchhoff.__init__ (kirchhoff.py:303-393, 503-657); the eikonal solves
+ * replace scikit-fmm's travel_time / distance (kirchhoff.py:609-638). */
+int kgb_kirchhoff_build_tables(kgb_kirchhoff* op, int mode, int ndim, const double* y_axis, int ny,
+                               const double* x_axis, int nx, const double* z_axis, int nz,
+                               const double* srcs, const double* recs, const double* vel, int64_t nvel,
+                               const double* aperture2_host, const double* angleaperture2_host,
+                               const double* aperturetap21_host, const int64_t* six_host,
+                               const int64_t* rix_host, double* maxdist_out);
+
+/* One device-built table in the reference layout (ni, n) float64 into
+ * out_host: which = 0/1 traveltimes of sources/receivers, 2/3 amplitudes,
+ * 4/5 angles (dynamic operators).  KGB_ERR_STATE if the operator's tables
+ * were uploaded rather than built.
+ * Replaces: reading trav_srcs, trav_recs, amp_srcs, amp_recs, angle_srcs,
+ * angle_recs (kirchhoff.py:310-393). */
+int kgb_kirchhoff_get_table(kgb_kirchhoff* op, int which, double* out_host);
+
 /* Forward d = K m: spreading along traveltime curves then wavelet
  * convolution.  m_dev (ni) float32, d_dev (ns*nr, nt) float32.
  * Replaces: Kirchhoff._matvec (kirchhoff.py:1048-1094). */
@@ -162,12 +194,20 @@ int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x_dev, float* y_dev, i
  * used by the tile autotuner. */
 int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant);
 
+/* Adjoint of dynamic operators: 1 (the default) stages the source records
+ * through shared memory with TMA bulk-tensor copies, 0 loads them from
+ * global memory in the gather itself.  Both give the same image bit for bit.
+ * No reference counterpart (the reference's adjoint kernels,
+ * _kirchhoff_cuda.py:194-298, read their tables directly). */
+int kgb_kirchhoff_set_adjoint_staging(kgb_kirchhoff* op, int on);
+
 /* Introspection used by the host wrapper and the tests.  info16 receives
  * {ns, nr, nt, ni, fixed-point fraction bits, padded wavelet length,
  *  offset-aperture gate active, dynamic, all times non-negative,
  *  adjoint receiver splits, kernels per forward, kernels per adjoint,
  *  spread variant, split accumulation used by the forward (0/1), most
- *  contributions any forward bin can receive, 0}. */
+ *  contributions any forward bin can receive, staged adjoint (bit 0: the
+ *  source records arrive by TMA) | error word of the bounded waits << 1}. */
 int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* info16);
 
 /* Deterministic float64 reductions of float32 vectors (fixed launch shape

@@ -49,6 +49,9 @@ _SIGNATURES = {
     "kgb_kirchhoff_set_traveltime_table": ([c_vp, c_dp], c_int),
     "kgb_kirchhoff_set_weight_precision": ([c_vp, c_int], c_int),
     "kgb_kirchhoff_set_dynamic": ([c_vp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_dp, c_i64p, c_i64p], c_int),
+    "kgb_kirchhoff_build_tables": ([c_vp, c_int, c_int, c_dp, c_int, c_dp, c_int, c_dp, c_int, c_dp, c_dp, c_dp,
+                                    ctypes.c_int64, c_dp, c_dp, c_dp, c_i64p, c_i64p, c_dp], c_int),
+    "kgb_kirchhoff_get_table": ([c_vp, c_int, c_dp], c_int),
     "kgb_kirchhoff_forward": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_kirchhoff_forward_static": ([c_vp, c_vp, c_vp, c_vp], c_int),
@@ -59,6 +62,7 @@ _SIGNATURES = {
     "kgb_kirchhoff_wavelet": ([c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     "kgb_kirchhoff_info": ([c_vp, c_i64p], c_int),
     "kgb_kirchhoff_set_variant": ([c_vp, c_int], c_int),
+    "kgb_kirchhoff_set_adjoint_staging": ([c_vp, c_int], c_int),
     "kgb_dot_f64": ([c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
     "kgb_solver_create": ([ctypes.POINTER(c_vp), c_vp, c_int], c_int),
     "kgb_solver_destroy": ([c_vp], c_int),

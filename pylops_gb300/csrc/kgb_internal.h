@@ -2,6 +2,7 @@
 // libpylops_gb300.so.  Not part of the public C ABI (include/kirchhoff_gb300.h).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -83,6 +84,11 @@ struct KirchDev {
     int split_ok;
     unsigned long long* wacc;
     unsigned* count_out;  // spread_count: the largest contribution count of any bin
+    // adjoint: a TMA tensor map over the source records in use (stab, or
+    // stab2 with bf16 weights) -- a HOST pointer, read by the launcher and
+    // passed to the kernel by value; null: the gather loads records itself
+    const CUtensorMap* rec_map;
+    unsigned* err;  // device word: nonzero after a bounded wait of a kernel gave up
 };
 
 // u32 words of the forward's fixed-point scale block: [0] bits of max |mv|,
@@ -95,6 +101,10 @@ int launch_spread(const KirchDev& K, bool dynamic, bool gate, const float* m, fl
                   const float* h, int L, bool fuse_wavelet, cudaStream_t stream);
 int launch_gather(const KirchDev& K, bool dynamic, bool gate, const float* d, float* img,
                   float* partial, int64_t partial_capacity, cudaStream_t stream);
+// TMA tensor map over dynamic-mode source records ([ns][ni] int4, or int2
+// with bf16 weights) for the staged adjoint; KGB_ERR_NOT_IMPLEMENTED when
+// the layout does not allow one (the gather then loads records itself).
+int make_record_map(CUtensorMap* map, const void* records, int64_t ni, int ns, bool half);
 // Set the kernels' shared-memory attributes once, outside any stream capture.
 int prepare_kernels(const KirchDev& K, int L);
 // Wavelet filter along time.  interleave = 0 writes y[tr][n]; interleave = 1
@@ -131,6 +141,28 @@ int gather_nsplit(const KirchDev& K, bool dynamic, bool gate);
 // Look up and cache, for the current device, the address of the static
 // scratch array of kgb_kirchhoff_forward_static (forward_static.cu).
 int static_scratch_prepare();
+
+// Device table builder (tables.cu).  Rows are [n][ni] float64.
+struct TableGeom {
+    int ndim, ny, nx, nz;  // ny = 1 in 2-D
+    int64_t ni;
+    double hy, hx, hz;     // sample spacings
+};
+int launch_analytic_rows(const TableGeom& g, const double* yax, const double* xax, const double* zax,
+                         const double* pts, int np, double vel, double* trav, double* dist, cudaStream_t s);
+int launch_eikonal_rows(const TableGeom& g, const double* speed, const int* pts, int np, double* out, unsigned* err,
+                        cudaStream_t s);
+int launch_angle_rows(const TableGeom& g, const double* trav, const double* sign_rows, int np, double* ang,
+                      cudaStream_t s);
+int launch_fold_rows(int ndim, double maxdist, double amin, double amax, const double* taper21,
+                     const double* dist, const double* ang, int64_t n, float* wc, float* ws,
+                     unsigned long long* wabs, cudaStream_t s);
+int launch_absmax(const double* x, int64_t n, unsigned long long* out, cudaStream_t s);
+int launch_finite_check(const double* x, int64_t n, long long* bad, cudaStream_t s);
+int launch_quantise(const double* t, int64_t n, double inv_dt, double scale, int32_t* q, int* qmin, cudaStream_t s);
+int launch_vscale(const double* vel, int64_t nvel, int64_t ni, float* vs, cudaStream_t s);
+int launch_rows_to_reference(const double* rows, int n, int64_t ni, double* out, cudaStream_t s);
+int launch_amplitude_rows(const double* dist, int64_t n, double maxdist, int ndim, double* amp, cudaStream_t s);
 
 // Deterministic float64 reductions (solver.cu).
 int launch_dot_f64(const float* a, const float* b, int64_t n, double* out, double* block_scratch,
@@ -177,6 +209,20 @@ struct kgb_kirchhoff {
     bool split_ok = false;
     unsigned* count_buf = nullptr;       // one device word for launch_spread_count
     unsigned max_bin_count = 0;          // its last result
+    CUtensorMap stab_map, stab2_map;     // TMA maps over stab / stab2 (see KirchDev::rec_map)
+    bool stab_map_ok = false, stab2_map_ok = false;
+    bool adjoint_staging = true;         // use the TMA-staged adjoint where a record map exists
+    // tables built on the device (kgb_kirchhoff_build_tables): [n][ni]
+    // float64 rows kept for kgb_kirchhoff_get_table
+    double* trav64_s = nullptr;
+    double* trav64_r = nullptr;
+    double* dist64_s = nullptr;
+    double* dist64_r = nullptr;
+    double* ang64_s = nullptr;
+    double* ang64_r = nullptr;
+    double maxdist = 0.0;
+    int table_ndim = 0;
+    unsigned* err = nullptr;             // device error word of the bounded waits
     int32_t* tq1 = nullptr;    // single traveltime table (trace-major), see KirchDev
     float* tw1 = nullptr;
     float* dcorr = nullptr;    // scratch: correlated data for the adjoint, interleaved pairs (2 x ndata)
@@ -205,6 +251,9 @@ struct kgb_kirchhoff {
         K.stab2 = bf16_weights ? stab2 : nullptr; K.rtab2 = bf16_weights ? rtab2 : nullptr;
         K.g0 = 0; K.g1 = 1 << 30; K.prepass = 1;
         K.split_ok = split_ok ? 1 : 0; K.wacc = wacc; K.count_out = count_buf;
+        K.rec_map = !adjoint_staging ? nullptr
+                    : bf16_weights ? (stab2_map_ok ? &stab2_map : nullptr) : (stab_map_ok ? &stab_map : nullptr);
+        K.err = err;
         return K;
     }
     int64_t npair() const { return (int64_t)ns * nr; }

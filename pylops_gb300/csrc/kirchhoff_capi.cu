@@ -96,6 +96,7 @@ static int repack(kgb_kirchhoff* op) {
     if (!op->grng && (rc = dev_alloc(&op->grng, (size_t)((op->nr + 7) / 8) * ncol, "alloc receiver group ranges")))
         return rc;
     if ((rc = launch_group_ranges(op->rrng, op->grng, op->nr, ncol, nullptr))) return rc;
+    op->stab_map_ok = make_record_map(&op->stab_map, op->stab, op->ni, op->ns, false) == KGB_OK;
     if (op->bf16_weights) {
         if (!op->stab2 && (rc = dev_alloc(&op->stab2, (size_t)op->ns * op->ni, "alloc bf16 source records"))) return rc;
         if (!op->rtab2 && (rc = dev_alloc(&op->rtab2, (size_t)op->nr * op->ni, "alloc bf16 receiver records")))
@@ -103,8 +104,31 @@ static int repack(kgb_kirchhoff* op) {
         if ((rc = launch_pack_tables_bf16(op->view(), op->wsc, op->wss, op->wrc, op->wrs, op->stab2, op->rtab2,
                                           nullptr)))
             return rc;
+        op->stab2_map_ok = make_record_map(&op->stab2_map, op->stab2, op->ni, op->ns, true) == KGB_OK;
     }
     KGB_CUDA_TRY(cudaDeviceSynchronize());
+    return KGB_OK;
+}
+
+// Offset aperture (kirchhoff.py:866-880): |six-rix|/(iz+1) < apmax, which
+// holds from the first passing depth downwards; inside it the reference's
+// taper index is 0 and taper[0] == 1, so only this cut-off acts.  Uploads
+// the first passing depth per trace.
+static int set_offset_gate(kgb_kirchhoff* op, double apmax, const int64_t* six, const int64_t* rix) {
+    const int64_t npair = op->npair();
+    std::vector<int32_t> izmin(npair);
+    bool gate = false;
+    for (int64_t p = 0; p < npair; ++p) {
+        const double off = fabs((double)(six[p] - rix[p]));
+        int iz = 0;
+        while (iz < op->nz && !(off / (double)(iz + 1) < apmax)) ++iz;
+        izmin[p] = iz;
+        gate = gate || iz > 0;
+    }
+    int rc;
+    if ((rc = dev_alloc(&op->izmin, izmin.size(), "alloc aperture"))) return rc;
+    KGB_CUDA_TRY(cudaMemcpy(op->izmin, izmin.data(), izmin.size() * 4, cudaMemcpyHostToDevice));
+    op->has_gate = gate;
     return KGB_OK;
 }
 
@@ -181,6 +205,9 @@ int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni
         if ((rc = dev_alloc(&op->partial, (size_t)op->partial_elems, "alloc partial images"))) break;
         if ((rc = dev_alloc(&op->mv, (size_t)ni, "alloc scaled model"))) break;
         if ((rc = dev_alloc(&op->absmax, kScaleWords, "alloc forward scale block"))) break;
+        if ((rc = dev_alloc(&op->err, 1, "alloc error word"))) break;
+        e = cudaMemset(op->err, 0, sizeof(unsigned));
+        if (e != cudaSuccess) { rc = cuda_error(e, "clear error word"); break; }
         if ((rc = prepare_kernels(op->view(), op->L))) break;
         if ((rc = static_scratch_prepare())) break;
         e = cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking);
@@ -202,7 +229,8 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     void* ptrs[] = {op->h_dev, op->hflip_dev, op->tsq, op->trq, op->wsc, op->wss, op->wrc, op->wrs,
                     op->vscale, op->izmin, op->dcorr, op->partial, op->m_stage, op->d_stage,
                     op->mv, op->absmax, op->stab, op->rtab, op->srng, op->rrng, op->tq1, op->tw1,
-                    op->stab2, op->rtab2, op->grng, op->wacc, op->count_buf};
+                    op->stab2, op->rtab2, op->grng, op->wacc, op->count_buf, op->err, op->trav64_s,
+                    op->trav64_r, op->dist64_s, op->dist64_r, op->ang64_s, op->ang64_r};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (op->stream) cudaStreamDestroy(op->stream);
@@ -426,17 +454,6 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const doub
     // offset aperture (kirchhoff.py:866-880): |six-rix|/(iz+1) < apmax, which
     // holds from the first passing depth downwards; inside it the reference's
     // taper index is 0 and taper[0] == 1, so only this cut-off acts.
-    const double apmax = aperture2[1];
-    const int64_t npair = op->npair();
-    std::vector<int32_t> izmin(npair);
-    bool gate = false;
-    for (int64_t p = 0; p < npair; ++p) {
-        const double off = fabs((double)(six[p] - rix[p]));
-        int iz = 0;
-        while (iz < op->nz && !(off / (double)(iz + 1) < apmax)) ++iz;
-        izmin[p] = iz;
-        gate = gate || iz > 0;
-    }
     KGB_CUDA_TRY(cudaSetDevice(op->device));
     int rc;
     if ((rc = dev_alloc(&op->wsc, wsc.size(), "alloc weights"))) return rc;
@@ -444,14 +461,12 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_s, const doub
     if ((rc = dev_alloc(&op->wrc, wrc.size(), "alloc weights"))) return rc;
     if ((rc = dev_alloc(&op->wrs, wrs.size(), "alloc weights"))) return rc;
     if ((rc = dev_alloc(&op->vscale, vs.size(), "alloc velocity"))) return rc;
-    if ((rc = dev_alloc(&op->izmin, izmin.size(), "alloc aperture"))) return rc;
     KGB_CUDA_TRY(cudaMemcpy(op->wsc, wsc.data(), wsc.size() * 4, cudaMemcpyHostToDevice));
     KGB_CUDA_TRY(cudaMemcpy(op->wss, wss.data(), wss.size() * 4, cudaMemcpyHostToDevice));
     KGB_CUDA_TRY(cudaMemcpy(op->wrc, wrc.data(), wrc.size() * 4, cudaMemcpyHostToDevice));
     KGB_CUDA_TRY(cudaMemcpy(op->wrs, wrs.data(), wrs.size() * 4, cudaMemcpyHostToDevice));
     KGB_CUDA_TRY(cudaMemcpy(op->vscale, vs.data(), vs.size() * 4, cudaMemcpyHostToDevice));
-    KGB_CUDA_TRY(cudaMemcpy(op->izmin, izmin.data(), izmin.size() * 4, cudaMemcpyHostToDevice));
-    op->has_gate = gate;
+    if ((rc = set_offset_gate(op, aperture2[1], six, rix))) return rc;
     op->wmax = (float)std::max(wmax, 1e-30);
     op->dyn_ready = true;
     rc = repack(op);
@@ -607,6 +622,13 @@ int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant) {
     return KGB_OK;
 }
 
+int kgb_kirchhoff_set_adjoint_staging(kgb_kirchhoff* op, int on) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (on != 0 && on != 1) return set_error(KGB_ERR_VALUE, "adjoint staging: 0 or 1");
+    op->adjoint_staging = on == 1;
+    return KGB_OK;
+}
+
 int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
     if (!op || !s) return set_error(KGB_ERR_VALUE, "info: null pointer");
     for (int k = 0; k < 16; ++k) s[k] = 0;
@@ -621,7 +643,232 @@ int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
     s[12] = op->spread_variant;
     s[13] = op->split_ok ? 1 : 0;
     s[14] = op->max_bin_count;
+    // staged adjoint in use, and the error word of the bounded waits
+    unsigned err = 0u;
+    if (op->err && cudaMemcpy(&err, op->err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return set_error(KGB_ERR_CUDA, "info: reading the error word failed");
+    s[15] = ((op->dynamic && op->view().rec_map) ? 1 : 0) | ((int64_t)err << 1);
     return KGB_OK;
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Tables built on the device (tables.cu)
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+struct DevBuf {  // scratch freed on every return path
+    T* p = nullptr;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+template <typename T>
+int upload(DevBuf<T>& b, const T* host, size_t n, const char* what) {
+    int rc = dev_alloc(&b.p, n, what);
+    if (rc) return rc;
+    KGB_CUDA_TRY(cudaMemcpy(b.p, host, n * sizeof(T), cudaMemcpyHostToDevice));
+    return KGB_OK;
+}
+
+double read_absmax(const unsigned long long* dev) {
+    unsigned long long bits = 0;
+    cudaMemcpy(&bits, dev, sizeof(bits), cudaMemcpyDeviceToHost);
+    double v;
+    memcpy(&v, &bits, sizeof(v));
+    return v;
+}
+
+}  // namespace
+
+int kgb_kirchhoff_build_tables(kgb_kirchhoff* op, int mode, int ndim, const double* yax, int ny, const double* xax,
+                               int nx, const double* zax, int nz, const double* srcs, const double* recs,
+                               const double* vel, int64_t nvel, const double* aperture2,
+                               const double* angleaperture2, const double* taper21, const int64_t* six,
+                               const int64_t* rix, double* maxdist_out) {
+    if (!op) return set_error(KGB_ERR_STATE, "null operator");
+    if (mode != 0 && mode != 1) return set_error(KGB_ERR_VALUE, "build_tables: mode must be 0 (analytic) or 1 (eikonal)");
+    if (ndim != 2 && ndim != 3) return set_error(KGB_ERR_VALUE, "build_tables: ndim must be 2 or 3");
+    if (ndim == 2) ny = 1;
+    if (!xax || !zax || (ndim == 3 && !yax) || !srcs || !recs || !vel)
+        return set_error(KGB_ERR_VALUE, "build_tables: null argument");
+    if (nx < 1 || nz < 1 || ny < 1 || (int64_t)ny * nx * nz != op->ni || nz != op->nz)
+        return set_error(KGB_ERR_VALUE, "build_tables: grid %d x %d x %d does not match the operator", ny, nx, nz);
+    if (mode == 0 && nvel != 1) return set_error(KGB_ERR_VALUE, "vel must be scalar for mode=analytical");
+    if (mode == 1 && ndim != 2) return set_error(KGB_ERR_NOT_IMPLEMENTED, "build_tables: device eikonal tables are 2-D");
+    if (mode == 1 && nvel != op->ni && nvel != 1) return set_error(KGB_ERR_VALUE, "build_tables: velocity size");
+    if (nvel != 1 && nvel != op->ni) return set_error(KGB_ERR_VALUE, "build_tables: velocity size");
+    for (int64_t k = 0; k < nvel; ++k)
+        if (!(vel[k] > 0.0) || !isfinite(vel[k]))
+            return set_error(KGB_ERR_VALUE, "build_tables: velocity must be positive and finite");
+    if (op->dynamic && (!aperture2 || !angleaperture2 || !taper21 || !six || !rix))
+        return set_error(KGB_ERR_VALUE, "build_tables: dynamic operator needs apertures, taper and six/rix");
+    if (op->dynamic && taper21[0] != 1.0)
+        return set_error(KGB_ERR_VALUE, "build_tables: aperture taper must start at 1 (taper(41, 20, 'hanning')[20:])");
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    const int ns = op->ns, nr = op->nr;
+    const int64_t ni = op->ni;
+    TableGeom g;
+    g.ndim = ndim;
+    g.ny = ny;
+    g.nx = nx;
+    g.nz = nz;
+    g.ni = ni;
+    g.hy = ndim == 3 && ny > 1 ? yax[1] - yax[0] : 1.0;
+    g.hx = nx > 1 ? xax[1] - xax[0] : 1.0;
+    g.hz = nz > 1 ? zax[1] - zax[0] : 1.0;
+    int rc;
+    if ((rc = dev_alloc(&op->trav64_s, (size_t)ns * ni, "alloc source traveltime rows"))) return rc;
+    if ((rc = dev_alloc(&op->trav64_r, (size_t)nr * ni, "alloc receiver traveltime rows"))) return rc;
+    if ((rc = dev_alloc(&op->dist64_s, (size_t)ns * ni, "alloc source distance rows"))) return rc;
+    if ((rc = dev_alloc(&op->dist64_r, (size_t)nr * ni, "alloc receiver distance rows"))) return rc;
+    if (mode == 0) {
+        DevBuf<double> dy, dx, dz, ps, pr;
+        if (ndim == 3 && (rc = upload(dy, yax, ny, "upload y axis"))) return rc;
+        if ((rc = upload(dx, xax, nx, "upload x axis"))) return rc;
+        if ((rc = upload(dz, zax, nz, "upload z axis"))) return rc;
+        if ((rc = upload(ps, srcs, (size_t)ndim * ns, "upload sources"))) return rc;
+        if ((rc = upload(pr, recs, (size_t)ndim * nr, "upload receivers"))) return rc;
+        if ((rc = launch_analytic_rows(g, dy.p, dx.p, dz.p, ps.p, ns, vel[0], op->trav64_s, op->dist64_s, nullptr)))
+            return rc;
+        if ((rc = launch_analytic_rows(g, dy.p, dx.p, dz.p, pr.p, nr, vel[0], op->trav64_r, op->dist64_r, nullptr)))
+            return rc;
+    } else {
+        // grid coordinates of the points: round((p - origin) / spacing) (kirchhoff.py:615, 627)
+        std::vector<int> is_(2 * (size_t)ns), ir_(2 * (size_t)nr);
+        auto coords = [&](const double* pts, int np, std::vector<int>& out) {
+            for (int k = 0; k < np; ++k) {
+                const double cx = nearbyint((pts[k] - xax[0]) / g.hx);
+                const double cz = nearbyint((pts[np + k] - zax[0]) / g.hz);
+                if (!(cx >= 0 && cx < nx && cz >= 0 && cz < nz)) return false;
+                out[2 * k] = (int)cx;
+                out[2 * k + 1] = (int)cz;
+            }
+            return true;
+        };
+        if (!coords(srcs, ns, is_) || !coords(recs, nr, ir_))
+            return set_error(KGB_ERR_VALUE, "build_tables: a source or receiver lies outside the grid");
+        DevBuf<int> ds, dr;
+        DevBuf<double> sp;
+        if ((rc = upload(ds, is_.data(), is_.size(), "upload source points"))) return rc;
+        if ((rc = upload(dr, ir_.data(), ir_.size(), "upload receiver points"))) return rc;
+        std::vector<double> vfull;
+        const double* vp = vel;
+        if (nvel == 1) {
+            vfull.assign((size_t)ni, vel[0]);
+            vp = vfull.data();
+        }
+        if ((rc = upload(sp, vp, (size_t)ni, "upload velocity"))) return rc;
+        KGB_CUDA_TRY(cudaMemset(op->err, 0, sizeof(unsigned)));
+        if ((rc = launch_eikonal_rows(g, sp.p, ds.p, ns, op->trav64_s, op->err, nullptr))) return rc;
+        if ((rc = launch_eikonal_rows(g, sp.p, dr.p, nr, op->trav64_r, op->err, nullptr))) return rc;
+        if ((rc = launch_eikonal_rows(g, nullptr, ds.p, ns, op->dist64_s, op->err, nullptr))) return rc;
+        if ((rc = launch_eikonal_rows(g, nullptr, dr.p, nr, op->dist64_r, op->err, nullptr))) return rc;
+        unsigned err = 0;
+        KGB_CUDA_TRY(cudaMemcpy(&err, op->err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+        if (err) return set_error(KGB_ERR_CUDA, "build_tables: the eikonal sweeps did not converge");
+    }
+    // fixed-point traveltimes (the quantisation of kgb_kirchhoff_set_traveltimes)
+    DevBuf<unsigned long long> red;
+    if ((rc = dev_alloc(&red.p, 4, "alloc reduction words"))) return rc;
+    DevBuf<long long> bad;
+    if ((rc = dev_alloc(&bad.p, 1, "alloc check word"))) return rc;
+    KGB_CUDA_TRY(cudaMemset(red.p, 0, 4 * sizeof(unsigned long long)));
+    KGB_CUDA_TRY(cudaMemset(bad.p, 0xff, sizeof(long long)));
+    if ((rc = launch_finite_check(op->trav64_s, (int64_t)ns * ni, bad.p, nullptr))) return rc;
+    if ((rc = launch_finite_check(op->trav64_r, (int64_t)nr * ni, bad.p, nullptr))) return rc;
+    if ((rc = launch_absmax(op->trav64_s, (int64_t)ns * ni, red.p, nullptr))) return rc;
+    if ((rc = launch_absmax(op->trav64_r, (int64_t)nr * ni, red.p, nullptr))) return rc;
+    long long badk = -1;
+    KGB_CUDA_TRY(cudaMemcpy(&badk, bad.p, sizeof(badk), cudaMemcpyDeviceToHost));
+    if (badk >= 0) return set_error(KGB_ERR_VALUE, "build_tables: non-finite traveltime");
+    const double inv_dt = 1.0 / op->dt;
+    const double maxs = read_absmax(red.p) * inv_dt;
+    const int F = choose_frac_bits(maxs, op->nt);
+    if (F < 8)
+        return set_error(KGB_ERR_VALUE, "build_tables: traveltimes up to %.3g samples exceed the 32-bit fixed-point range",
+                         maxs);
+    DevBuf<int> qmin;
+    if ((rc = dev_alloc(&qmin.p, 2, "alloc check word"))) return rc;
+    const int big[2] = {INT32_MAX, INT32_MAX};
+    KGB_CUDA_TRY(cudaMemcpy(qmin.p, big, sizeof(big), cudaMemcpyHostToDevice));
+    const double scale = ldexp(1.0, F);
+    if ((rc = launch_quantise(op->trav64_s, (int64_t)ns * ni, inv_dt, scale, op->tsq, qmin.p, nullptr))) return rc;
+    if ((rc = launch_quantise(op->trav64_r, (int64_t)nr * ni, inv_dt, scale, op->trq, qmin.p + 1, nullptr))) return rc;
+    int qm[2];
+    KGB_CUDA_TRY(cudaMemcpy(qm, qmin.p, sizeof(qm), cudaMemcpyDeviceToHost));
+    op->frac_bits = F;
+    op->nonneg = (int64_t)qm[0] + (int64_t)qm[1] >= 0;
+    op->trav_ready = true;
+    op->table_ndim = ndim;
+    // distances and amplitudes (kirchhoff.py:316-330)
+    if ((rc = launch_absmax(op->dist64_s, (int64_t)ns * ni, red.p + 1, nullptr))) return rc;
+    if ((rc = launch_absmax(op->dist64_r, (int64_t)nr * ni, red.p + 2, nullptr))) return rc;
+    op->maxdist = 1e-2 * (read_absmax(red.p + 1) + read_absmax(red.p + 2));
+    if (maxdist_out) *maxdist_out = op->maxdist;
+    if (op->dynamic) {
+        if ((rc = dev_alloc(&op->ang64_s, (size_t)ns * ni, "alloc source angle rows"))) return rc;
+        if ((rc = dev_alloc(&op->ang64_r, (size_t)nr * ni, "alloc receiver angle rows"))) return rc;
+        if ((rc = launch_angle_rows(g, op->trav64_s, nullptr, ns, op->ang64_s, nullptr))) return rc;
+        // 3-D receivers: the x-gradient sign of the source row of the same
+        // index when ns == nr (kirchhoff.py:386-393), else their own
+        if ((rc = launch_angle_rows(g, op->trav64_r, (ndim == 3 && ns == nr) ? op->trav64_s : nullptr, nr,
+                                    op->ang64_r, nullptr)))
+            return rc;
+        DevBuf<double> tap;
+        if ((rc = upload(tap, taper21, 21, "upload taper"))) return rc;
+        if ((rc = dev_alloc(&op->wsc, (size_t)ns * ni, "alloc weights"))) return rc;
+        if ((rc = dev_alloc(&op->wss, (size_t)ns * ni, "alloc weights"))) return rc;
+        if ((rc = dev_alloc(&op->wrc, (size_t)nr * ni, "alloc weights"))) return rc;
+        if ((rc = dev_alloc(&op->wrs, (size_t)nr * ni, "alloc weights"))) return rc;
+        KGB_CUDA_TRY(cudaMemset(red.p, 0, 2 * sizeof(unsigned long long)));
+        const double amin = angleaperture2[0], amax = angleaperture2[1];
+        if ((rc = launch_fold_rows(ndim, op->maxdist, amin, amax, tap.p, op->dist64_s, op->ang64_s, (int64_t)ns * ni,
+                                   op->wsc, op->wss, red.p, nullptr)))
+            return rc;
+        if ((rc = launch_fold_rows(ndim, op->maxdist, amin, amax, tap.p, op->dist64_r, op->ang64_r, (int64_t)nr * ni,
+                                   op->wrc, op->wrs, red.p + 1, nullptr)))
+            return rc;
+        const double wmax = read_absmax(red.p) * read_absmax(red.p + 1) * 1.0001;
+        if (!isfinite(wmax)) return set_error(KGB_ERR_VALUE, "build_tables: non-finite amplitude or angle table");
+        if ((rc = dev_alloc(&op->vscale, (size_t)ni, "alloc velocity"))) return rc;
+        DevBuf<double> dv;
+        if ((rc = upload(dv, vel, (size_t)nvel, "upload velocity"))) return rc;
+        if ((rc = launch_vscale(dv.p, nvel, ni, op->vscale, nullptr))) return rc;
+        if ((rc = set_offset_gate(op, aperture2[1], six, rix))) return rc;
+        op->wmax = (float)std::max(wmax, 1e-30);
+        op->dyn_ready = true;
+    }
+    KGB_CUDA_TRY(cudaDeviceSynchronize());
+    rc = repack(op);
+    return rc ? rc : update_split(op);
+}
+
+int kgb_kirchhoff_get_table(kgb_kirchhoff* op, int which, double* out_host) {
+    if (!op || !out_host) return set_error(KGB_ERR_VALUE, "get_table: null argument");
+    if (which < 0 || which > 5) return set_error(KGB_ERR_VALUE, "get_table: which must be 0..5");
+    const bool src = which % 2 == 0;
+    const int n = src ? op->ns : op->nr;
+    const double* rows = nullptr;
+    if (which < 2) rows = src ? op->trav64_s : op->trav64_r;
+    else if (which < 4) rows = src ? op->dist64_s : op->dist64_r;
+    else rows = src ? op->ang64_s : op->ang64_r;
+    if (!rows) return set_error(KGB_ERR_STATE, "get_table: the table was not built on the device");
+    KGB_CUDA_TRY(cudaSetDevice(op->device));
+    const size_t cnt = (size_t)n * op->ni;
+    DevBuf<double> tmp, amp;
+    int rc;
+    if (which == 2 || which == 3) {
+        // amplitudes from the distance rows (kirchhoff.py:316-330)
+        if ((rc = dev_alloc(&amp.p, cnt, "alloc amplitude rows"))) return rc;
+        if ((rc = launch_amplitude_rows(rows, (int64_t)cnt, op->maxdist, op->table_ndim, amp.p, nullptr))) return rc;
+        rows = amp.p;
+    }
+    if ((rc = dev_alloc(&tmp.p, cnt, "alloc table transpose"))) return rc;
+    if ((rc = launch_rows_to_reference(rows, n, op->ni, tmp.p, nullptr))) return rc;
+    KGB_CUDA_TRY(cudaMemcpy(out_host, tmp.p, cnt * sizeof(double), cudaMemcpyDeviceToHost));
+    return KGB_OK;
+}

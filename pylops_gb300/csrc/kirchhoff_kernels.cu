@@ -32,6 +32,7 @@
 #include "fir.cuh"
 #include "fixed_acc.cuh"
 #include "kgb_internal.h"
+#include "tma.cuh"
 
 namespace kgb {
 
@@ -224,6 +225,236 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
     }
     if (DYN) total *= __ldg(K.vscale + ii);
     out[(size_t)blockIdx.y * K.ni + ii] = total;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint with the source records staged by TMA.  Same per-point arithmetic
+// and summation order as gather_kernel (so the same bits), but the source
+// record a thread needs at each step of its source loop is already in shared
+// memory: the CTA's 256 image points' records of one source are one 4 KB
+// (2 KB for bf16 weights) box of a 3-D bulk-tensor copy {record words,
+// points, sources}, and kGatherStages boxes are in flight ahead of the
+// consumers in a ring of full/empty mbarriers.  The dependent chain per
+// source step becomes shared-memory record -> data load instead of global
+// record -> data load.
+//
+// Work items are (source, receiver chunk) pairs in the order of
+// gather_kernel's loops, skipping the sources and receiver groups that have
+// zero weight at every point of the CTA (their contributions are exactly
+// zero).  Thread 0 issues them: items 0..kGatherStages-1 up front, then item
+// k + kGatherStages once all 8 warps released item k's stage; an item with
+// source -1 ends the sequence.  Every wait is bounded; on a timeout the CTA
+// records an error code in *err, stops, and thread 0 waits (bounded) for the
+// copies it issued before the CTA exits.
+// ---------------------------------------------------------------------------
+constexpr int kGatherStages = 4;
+constexpr int kGatherWarps = kGatherThreads / 32;
+constexpr int kGatherTmaBlocks = 6;  // resident CTAs per SM the register budget is sized for
+
+// Thread 0's producer state, in shared memory (it would otherwise take
+// registers in every thread of the hot loop).
+struct GatherProducer {
+    int p_is, p_r0;          // last source issued, and its chunk
+    int issued, consumed;    // items issued (the end marker included) and consumed by thread 0
+    int stop;                // the end marker was issued
+    unsigned smask[2];       // sources 0..63 with a nonzero weight at some point of the CTA
+    unsigned gmask[2];       // receiver groups 0..63 of the split likewise
+};
+
+// The next (source, chunk) item that may have a nonzero weight, or src = -1.
+__device__ __forceinline__ void gather_next_item(GatherProducer& P, int ns, int r_begin, int r_end, int g_begin,
+                                                 bool groups, int& src, int& r0) {
+    for (;;) {
+        if (++P.p_is >= ns) {
+            P.p_is = 0;
+            P.p_r0 += kGatherRC;
+        }
+        if (P.p_r0 >= r_end) {
+            src = -1;
+            r0 = -1;
+            return;
+        }
+        const int gi = (P.p_r0 >> 3) - g_begin;
+        if (groups && gi < 64 && !((P.gmask[gi >> 5] >> (gi & 31)) & 1u)) {  // no point of the CTA in this group
+            P.p_is = ns - 1;
+            continue;
+        }
+        if (P.p_is < 64 && !((P.smask[P.p_is >> 5] >> (P.p_is & 31)) & 1u)) continue;  // zero at every point
+        src = P.p_is;
+        r0 = P.p_r0;
+        return;
+    }
+}
+
+template <bool GATE, bool NONNEG, bool HALF>
+__global__ void __launch_bounds__(kGatherThreads, kGatherTmaBlocks)
+gather_tma_kernel(const __grid_constant__ CUtensorMap smap, const KirchDev K, const FixedPoint<NONNEG> fp,
+                  const float2* __restrict__ d2, float* __restrict__ out, int r_per_split, unsigned* __restrict__ err) {
+    using Rec = typename std::conditional<HALF, int2, int4>::type;
+    constexpr uint32_t kBox = kGatherThreads * sizeof(Rec);
+    __shared__ __align__(128) Rec stage[kGatherStages][kGatherThreads];
+    __shared__ __align__(8) unsigned long long full_bar[kGatherStages], empty_bar[kGatherStages];
+    __shared__ int meta_src[kGatherStages], meta_r0[kGatherStages];
+    __shared__ unsigned long long warp_groups[kGatherWarps];
+    __shared__ GatherProducer P;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t ii = (int64_t)blockIdx.x * kGatherThreads + tid;
+    const bool live = ii < K.ni;
+    const int r_begin = blockIdx.y * r_per_split;
+    const int r_end = min(K.nr, r_begin + r_per_split);
+    const int64_t ncol = K.ni / K.nz;
+    int col = 0, iz = 0;
+    if (live) {
+        col = (int)(ii / K.nz);
+        iz = (int)(ii - (int64_t)col * K.nz);
+    }
+    const int nt = K.nt;
+    const int g_begin = r_begin >> 3;
+    if (tid == 0) {
+        P.p_is = -1;
+        P.p_r0 = r_begin;
+        P.issued = P.consumed = P.stop = 0;
+        P.smask[0] = P.smask[1] = P.gmask[0] = P.gmask[1] = 0u;
+        for (int s = 0; s < kGatherStages; ++s) {
+            tma::mbar_init(tma::smem_u32(&full_bar[s]), 1);
+            tma::mbar_init(tma::smem_u32(&empty_bar[s]), kGatherWarps);
+        }
+        tma::mbar_fence_init();
+    }
+    __syncthreads();
+    // sources 0..63 with a nonzero weight at this point
+    unsigned long long smask = 0ull;
+    if (live)
+        for (int is = 0; is < min(K.ns, 64); ++is)
+            if (in_range(K.srng, (size_t)is * ncol + col, iz)) smask |= 1ull << is;
+    {
+        // receiver groups of 8 (the first 64 of this split) with a nonzero
+        // weight at some point of this warp; later groups are tested per chunk
+        const int g_count = r_end > r_begin ? ((r_end - 1) >> 3) - g_begin + 1 : 0;
+        unsigned long long wg = 0ull;
+        if (K.grng)
+            for (int g = 0; g < min(g_count, 64); ++g)
+                if (__any_sync(FULL, live && in_range(K.grng, (size_t)(g_begin + g) * ncol + col, iz))) wg |= 1ull << g;
+        const unsigned lo = __reduce_or_sync(FULL, (unsigned)smask);
+        const unsigned hi = __reduce_or_sync(FULL, (unsigned)(smask >> 32));
+        if (lane == 0) {
+            warp_groups[warp] = wg;
+            if (lo) atomicOr(&P.smask[0], lo);
+            if (hi) atomicOr(&P.smask[1], hi);
+            if ((unsigned)wg) atomicOr(&P.gmask[0], (unsigned)wg);
+            if ((unsigned)(wg >> 32)) atomicOr(&P.gmask[1], (unsigned)(wg >> 32));
+        }
+    }
+    __syncthreads();
+    // thread 0: item j into stage j % kGatherStages
+    auto issue = [&](int j) {
+        const int s = j % kGatherStages;
+        int src, r0;
+        gather_next_item(P, K.ns, r_begin, r_end, g_begin, K.grng != nullptr, src, r0);
+        meta_src[s] = src;
+        meta_r0[s] = r0;
+        const uint32_t fb = tma::smem_u32(&full_bar[s]);
+        if (src < 0) {
+            tma::mbar_arrive(fb);
+            P.stop = 1;
+        } else {
+            tma::mbar_expect_tx(fb, kBox);
+            const int64_t ii0 = (int64_t)blockIdx.x * kGatherThreads;
+            tma::load_3d(tma::smem_u32(&stage[s][0]), &smap, fb, 0, HALF ? (int)(ii0 >> 1) : (int)ii0, src);
+        }
+        P.issued = j + 1;
+    };
+    if (tid == 0)
+        for (int j = 0; j < kGatherStages && !P.stop; ++j) issue(j);
+    Entry re[kGatherRC];
+    int cur_r0 = -1;
+    bool wact = false;
+    float total = 0.f, chunk = 0.f;
+    bool failed = false;
+    for (int k = 0;; ++k) {
+        const int s = k % kGatherStages;
+        const uint32_t par = (uint32_t)(k / kGatherStages) & 1u;
+        if (!tma::mbar_wait(tma::smem_u32(&full_bar[s]), par)) {
+            atomicExch(err, 1u);
+            failed = true;
+            break;
+        }
+        if (tid == 0) P.consumed = k + 1;
+        const int src = meta_src[s];
+        const int r0 = meta_r0[s];
+        if (src < 0) break;
+        if (r0 != cur_r0) {
+            if (wact) total += chunk;
+            chunk = 0.f;
+            cur_r0 = r0;
+            const int gi = (r0 >> 3) - g_begin;
+            wact = !K.grng ? true
+                           : (gi < 64 ? ((warp_groups[warp] >> gi) & 1ull) != 0ull
+                                      : __any_sync(FULL, live && in_range(K.grng, (size_t)(r0 >> 3) * ncol + col, iz)));
+            if (wact && live) {
+                const int nrc = min(kGatherRC, r_end - r0);
+#pragma unroll
+                for (int r = 0; r < kGatherRC; ++r) {
+                    re[r] = zero_entry();
+                    if (r < nrc) re[r] = load_entry<true, true, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
+                }
+            }
+        }
+        if (wact && live &&
+            (src < 64 ? ((smask >> src) & 1ull) != 0ull : in_range(K.srng, (size_t)src * ncol + col, iz))) {
+            Entry se;
+            if (HALF) {
+                const int2 v = *reinterpret_cast<const int2*>(&stage[s][tid]);
+                se.t = v.x;
+                se.c = __uint_as_float((unsigned)v.y << 16);
+                se.s = __uint_as_float((unsigned)v.y & 0xffff0000u);
+            } else {
+                const int4 v = *reinterpret_cast<const int4*>(&stage[s][tid]);
+                se.t = v.x;
+                se.c = __int_as_float(v.y);
+                se.s = __int_as_float(v.z);
+            }
+            if (se.c != 0.f || se.s != 0.f) {
+                const int nrc = min(kGatherRC, r_end - r0);
+                const size_t pair0 = (size_t)src * K.nr + r0;
+                const float2* __restrict__ drow = d2 + pair0 * nt;
+#pragma unroll
+                for (int r = 0; r < kGatherRC; ++r) {
+                    if (r < nrc) {
+                        const int sum = se.t + re[r].t;
+                        float wt = fmaf(se.c, re[r].c, se.s * re[r].s);
+                        if (GATE && iz < __ldg(K.izmin + pair0 + r)) wt = 0.f;
+                        if (fp.valid(sum) && wt != 0.f) {
+                            const int it = fp.index(sum);
+                            const float w = fp.frac(sum, it);
+                            const float2 dd = __ldg(drow + ((size_t)r * nt + it));
+                            const float val = fmaf(w, dd.y - dd.x, dd.x);
+                            chunk = fmaf(val, wt, chunk);
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) tma::mbar_arrive(tma::smem_u32(&empty_bar[s]));
+        if (tid == 0 && !P.stop) {
+            // stage s is free once every warp released item k
+            if (!tma::mbar_wait(tma::smem_u32(&empty_bar[s]), par)) {
+                atomicExch(err, 2u);
+                failed = true;
+                break;
+            }
+            issue(k + kGatherStages);
+        }
+    }
+    if (tid == 0) {
+        // no copy of this CTA may still be in flight when it exits
+        for (int j = P.consumed; j < P.issued; ++j)
+            tma::mbar_wait(tma::smem_u32(&full_bar[j % kGatherStages]), (uint32_t)(j / kGatherStages) & 1u);
+    }
+    if (failed) return;
+    if (wact) total += chunk;
+    if (live) out[(size_t)blockIdx.y * K.ni + ii] = total * __ldg(K.vscale + ii);
 }
 
 // Fixed-order sum of the per-split partial images.
@@ -796,12 +1027,31 @@ int choose_split(int64_t blocks, int capacity, int nr) {
     return best;
 }
 
+template <bool GATE, bool NONNEG, bool HALF>
+int gather_tma_blocks_per_sm() {
+    static int cached = 0;
+    if (!cached) {
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gather_tma_kernel<GATE, NONNEG, HALF>, kGatherThreads, 0);
+        cached = nb > 0 ? nb : 1;
+    }
+    return cached;
+}
+
+// the staged (TMA) adjoint applies: dynamic tables with a record map
+template <bool DYN>
+bool gather_staged(const KirchDev& K) {
+    return DYN && K.rec_map != nullptr && K.err != nullptr;
+}
+
 template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
 int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* partial, int64_t cap,
                     cudaStream_t stream) {
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
-    const int capacity = num_sms() * gather_blocks_per_sm<DYN, GATE, NONNEG, HALF>();
+    const bool staged = gather_staged<DYN>(K);
+    const int capacity = num_sms() * (staged ? gather_tma_blocks_per_sm<GATE, NONNEG, HALF>()
+                                             : gather_blocks_per_sm<DYN, GATE, NONNEG, HALF>());
     int split = choose_split(blocks, capacity, K.nr);
     if (partial == nullptr || cap < (int64_t)split * K.ni) split = 1;
     const int nchunks = (K.nr + kGatherRC - 1) / kGatherRC;
@@ -809,7 +1059,11 @@ int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* part
     split = (nchunks + c_per - 1) / c_per;
     float* out = split > 1 ? partial : img;
     dim3 grid((unsigned)blocks, (unsigned)split);
-    gather_kernel<DYN, GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
+    if (staged)
+        gather_tma_kernel<GATE, NONNEG, HALF>
+            <<<grid, kGatherThreads, 0, stream>>>(*K.rec_map, K, fp, d2, out, c_per * kGatherRC, K.err);
+    else
+        gather_kernel<DYN, GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
     KGB_CUDA_TRY(cudaGetLastError());
     if (split > 1) {
         const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
@@ -1433,6 +1687,26 @@ int wavelet_blocks_per_sm(int threads, size_t smem) {
 
 }  // namespace
 
+int make_record_map(CUtensorMap* map, const void* records, int64_t ni, int ns, bool half) {
+    tma::EncodeTiledFn fn = tma::encode_fn();
+    if (!fn) return set_error(KGB_ERR_NOT_IMPLEMENTED, "record map: cuTensorMapEncodeTiled unavailable");
+    // {4 words, points, sources} with one 16-byte record per point, or two
+    // 8-byte bf16-weight records per 16 bytes; box: the records of one CTA's
+    // kGatherThreads points of one source
+    const int64_t per16 = half ? 2 : 1;
+    if (!records || ni % per16 != 0 || ni / per16 > ((int64_t)1 << 31) - 1 || ns <= 0)
+        return set_error(KGB_ERR_NOT_IMPLEMENTED, "record map: layout not supported");
+    cuuint64_t dims[3] = {4, (cuuint64_t)(ni / per16), (cuuint64_t)ns};
+    cuuint64_t strides[2] = {16, (cuuint64_t)ni * 16 / per16};
+    cuuint32_t box[3] = {4, (cuuint32_t)(kGatherThreads / per16), 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void*>(records), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(KGB_ERR_NOT_IMPLEMENTED, "record map rejected (CUresult %d)", (int)r);
+    return KGB_OK;
+}
+
 int launch_spread_count(const KirchDev& K, bool dynamic, bool gate, int L, unsigned* count, cudaStream_t stream) {
     KGB_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(unsigned), stream));
     if (K.ns <= 0 || K.nr <= 0 || K.tq1) return KGB_OK;
@@ -1451,7 +1725,14 @@ int launch_spread_count(const KirchDev& K, bool dynamic, bool gate, int L, unsig
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
     int bps;
-    if (dynamic && K.stab2)
+    if (dynamic && gather_staged<true>(K)) {
+        if (K.stab2)
+            bps = gate ? (K.nonneg ? gather_tma_blocks_per_sm<true, true, true>() : gather_tma_blocks_per_sm<true, false, true>())
+                       : (K.nonneg ? gather_tma_blocks_per_sm<false, true, true>() : gather_tma_blocks_per_sm<false, false, true>());
+        else
+            bps = gate ? (K.nonneg ? gather_tma_blocks_per_sm<true, true, false>() : gather_tma_blocks_per_sm<true, false, false>())
+                       : (K.nonneg ? gather_tma_blocks_per_sm<false, true, false>() : gather_tma_blocks_per_sm<false, false, false>());
+    } else if (dynamic && K.stab2)
         bps = gate ? (K.nonneg ? gather_blocks_per_sm<true, true, true, true>() : gather_blocks_per_sm<true, true, false, true>())
                    : (K.nonneg ? gather_blocks_per_sm<true, false, true, true>() : gather_blocks_per_sm<true, false, false, true>());
     else if (dynamic) bps = gate ? (K.nonneg ? gather_blocks_per_sm<true, true, true>() : gather_blocks_per_sm<true, true, false>())

@@ -1,0 +1,463 @@
+// Traveltime, amplitude and angle tables of Kirchhoff(mode='analytic' |
+// 'eikonal') built on the device (pylops/waveeqprocessing/kirchhoff.py:
+// 303-393 and 503-657), written straight into the operator's layouts
+// (fixed-point traveltime rows, folded weight rows) with no host round trip.
+//
+// Every table is a row per source or receiver point, [n][ni] float64, with
+// the image index ii = ix*nz + iz (2-D) or (iy*nx + ix)*nz + iz (3-D):
+//  * analytic: dist^2 = (X - px)^2 + (Z - pz)^2 (+ (Y - py)^2), trav =
+//    sqrt(dist^2)/v, dist = trav*v, in the reference's order of operations
+//    (kirchhoff.py:576-607), so the rows equal numpy's bit for bit;
+//  * eikonal (2-D): the fast-marching equations of the package's host
+//    solver (eikonal.cpp, the method scikit-fmm implements) solved by
+//    Gauss-Seidel sweeps in the four diagonal orders until no value
+//    changes: one CTA per table, anti-diagonals of the sweep in parallel
+//    (their points do not neighbour one another), the same upwind
+//    second-order local solver;
+//  * gradients: numpy.gradient with the sample spacing (central differences
+//    inside, one-sided at the ends, kirchhoff.py:642-648);
+//  * angles with the vertical: atan2(dT/dx, dT/dz) in 2-D;
+//    sign(dTs/dx) acos(dT/dz / |grad T|) in 3-D, where the receiver angle
+//    takes the sign of the source table of the same index when ns == nr
+//    (kirchhoff.py:364-393) and its own otherwise;
+//  * amplitudes 1/sqrt(dist + maxdist) (2-D) or 1/(dist + maxdist) (3-D),
+//    maxdist = 1e-2 (max dist_s + max dist_r) (kirchhoff.py:316-330).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "kgb_internal.h"
+
+namespace kgb {
+namespace {
+
+// ---------------------------------------------------------------------------
+// analytic rows
+// ---------------------------------------------------------------------------
+__global__ void analytic_kernel(const double* __restrict__ yax, const double* __restrict__ xax,
+                                const double* __restrict__ zax, int ndim, int nx, int nz, int64_t ni,
+                                const double* __restrict__ pts, int np, double vel, double* __restrict__ trav,
+                                double* __restrict__ dist) {
+    const int p = blockIdx.y;
+    const double py = ndim == 3 ? pts[p] : 0.0;
+    const double px = pts[(ndim - 2) * np + p];
+    const double pz = pts[(ndim - 1) * np + p];
+    for (int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ii < ni; ii += (int64_t)gridDim.x * blockDim.x) {
+        const int iz = (int)(ii % nz);
+        const int64_t r = ii / nz;
+        const int ix = (int)(r % nx);
+        // squares rounded before the sum (no fused multiply-add), as numpy does
+        const double dxp = xax[ix] - px, dzp = zax[iz] - pz;
+        double d2 = __dadd_rn(__dmul_rn(dxp, dxp), __dmul_rn(dzp, dzp));
+        if (ndim == 3) {
+            const double dyp = yax[r / nx] - py;
+            d2 = __dadd_rn(d2, __dmul_rn(dyp, dyp));
+        }
+        const double t = sqrt(d2) / vel;
+        trav[(size_t)p * ni + ii] = t;
+        if (dist) dist[(size_t)p * ni + ii] = __dmul_rn(t, vel);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2-D eikonal by diagonal Gauss-Seidel sweeps
+// ---------------------------------------------------------------------------
+// larger root of sum_i c[i] (T - b[i])^2 = rhs if it is not below any b[i]
+__device__ __forceinline__ bool ek_root(int m, const double* c, const double* b, double rhs, double* T) {
+    double A = 0.0, B = 0.0, C = -rhs, bmax = -INFINITY;
+    for (int i = 0; i < m; ++i) {
+        A += c[i];
+        B += -2.0 * c[i] * b[i];
+        C += c[i] * b[i] * b[i];
+        bmax = fmax(bmax, b[i]);
+    }
+    const double disc = B * B - 4.0 * A * C;
+    if (disc < 0.0) return false;
+    const double t = (-B + sqrt(disc)) / (2.0 * A);
+    if (t < bmax) return false;
+    *T = t;
+    return true;
+}
+
+// the host solver's local update (eikonal.cpp, update()) with every finite
+// neighbour taken as known; +inf when no neighbour is finite
+__device__ double ek_update(const double* T, int n0, int n1, double h0, double h1, int i0, int i1,
+                            double slow2) {
+    const int64_t k = (int64_t)i0 * n1 + i1;
+    double a2o[2], b2o[2], a1[2], b1[2];
+    int m = 0;
+    for (int a = 0; a < 2; ++a) {
+        const int c = a == 0 ? i0 : i1;
+        const int n = a == 0 ? n0 : n1;
+        const int64_t st = a == 0 ? n1 : 1;
+        const double h = a == 0 ? h0 : h1;
+        double best = INFINITY, second = INFINITY;
+        bool have2 = false;
+        for (int dir = -1; dir <= 1; dir += 2) {
+            const int c1 = c + dir;
+            if (c1 < 0 || c1 >= n) continue;
+            const double v1 = T[k + dir * st];
+            if (!(v1 < INFINITY)) continue;
+            if (v1 < best) {
+                best = v1;
+                have2 = false;
+                const int c2 = c + 2 * dir;
+                if (c2 >= 0 && c2 < n) {
+                    const double v2 = T[k + 2 * dir * st];
+                    if (v2 < INFINITY && v2 <= v1) {
+                        have2 = true;
+                        second = v2;
+                    }
+                }
+            }
+        }
+        if (best < INFINITY) {
+            a1[m] = 1.0 / (h * h);
+            b1[m] = best;
+            if (have2) {
+                a2o[m] = 9.0 / (4.0 * h * h);
+                b2o[m] = (4.0 * best - second) / 3.0;
+            } else {
+                a2o[m] = a1[m];
+                b2o[m] = best;
+            }
+            ++m;
+        }
+    }
+    if (m == 0) return INFINITY;
+    double t;
+    if (ek_root(m, a2o, b2o, slow2, &t)) return t;
+    int o0 = 0, o1 = 1;
+    if (m == 2 && b1[1] < b1[0]) {
+        o0 = 1;
+        o1 = 0;
+    }
+    if (m == 2) {
+        const double aa[2] = {a1[o0], a1[o1]}, bb[2] = {b1[o0], b1[o1]};
+        if (ek_root(2, aa, bb, slow2, &t)) return t;
+    }
+    {
+        const double aa[1] = {a1[o0]}, bb[1] = {b1[o0]};
+        if (ek_root(1, aa, bb, slow2, &t)) return t;
+    }
+    return b1[o0] + sqrt(slow2 / a1[o0]);
+}
+
+constexpr int kEikThreads = 320;
+constexpr int kEikMaxSets = 64;  // sweep sets before giving up (each set is 4 sweeps)
+
+// One CTA per table: blockIdx.x = point (traveltimes with `speed`, or
+// distances with speed 1 when speed == nullptr).
+__global__ void __launch_bounds__(kEikThreads)
+eikonal_sweep_kernel(int n0, int n1, double h0, double h1, const double* __restrict__ speed,
+                     const int* __restrict__ pts, int np, double* out, unsigned* __restrict__ err) {
+    const int p = blockIdx.x;
+    double* T = out + (size_t)p * n0 * n1;  // read and written by all threads between barriers
+    const int s0 = pts[2 * p], s1 = pts[2 * p + 1];
+    const int64_t N = (int64_t)n0 * n1;
+    const double r0 = 0.5 / sqrt(1.0 / (h0 * h0) + 1.0 / (h1 * h1));
+    auto spd = [&](int64_t i) { return speed ? speed[i] : 1.0; };
+    // the point and its axis neighbours start on the level set (half a cell
+    // from the point); they never change
+    auto frozen = [&](int i0, int i1) { return abs(i0 - s0) + abs(i1 - s1) <= 1; };
+    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
+        const int i0 = (int)(i / n1), i1 = (int)(i - (int64_t)i0 * n1);
+        double v = INFINITY;
+        if (i0 == s0 && i1 == s1) v = r0 / spd(i);
+        else if (frozen(i0, i1)) v = 0.5 * (i0 != s0 ? h0 : h1) / spd(i);
+        T[i] = v;
+    }
+    __shared__ int changed;
+    int sets = 0;
+    for (;;) {
+        if (threadIdx.x == 0) changed = 0;
+        __syncthreads();
+        for (int dir = 0; dir < 4; ++dir) {
+            const bool f0 = dir == 0 || dir == 3;  // i0 increasing
+            const bool f1 = dir < 2;               // i1 increasing
+            for (int d = 0; d < n0 + n1 - 1; ++d) {
+                // points with u0 + u1 = d, u = the sweep's coordinates
+                const int lo = max(0, d - (n0 - 1)), hi = min(d, n1 - 1);
+                for (int u1 = lo + (int)threadIdx.x; u1 <= hi; u1 += blockDim.x) {
+                    const int u0 = d - u1;
+                    const int i0 = f0 ? u0 : n0 - 1 - u0;
+                    const int i1 = f1 ? u1 : n1 - 1 - u1;
+                    if (frozen(i0, i1)) continue;
+                    const int64_t k = (int64_t)i0 * n1 + i1;
+                    const double sp = spd(k);
+                    const double t = ek_update(T, n0, n1, h0, h1, i0, i1, 1.0 / (sp * sp));
+                    if (t < T[k]) {
+                        T[k] = t;
+                        changed = 1;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        const int c = changed;
+        __syncthreads();
+        if (!c) break;
+        if (++sets >= kEikMaxSets) {
+            if (threadIdx.x == 0) atomicExch(err, 3u);
+            break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// gradients, angles, amplitudes, folded weights
+// ---------------------------------------------------------------------------
+// numpy.gradient of row f along axis a (stride st, length n, spacing h) at
+// coordinate c: central difference inside, one-sided at the ends
+__device__ __forceinline__ double grad1(const double* __restrict__ f, int64_t k, int c, int n, int64_t st, double h) {
+    if (n < 2) return 0.0;
+    if (c == 0) return (f[k + st] - f[k]) / h;
+    if (c == n - 1) return (f[k] - f[k - st]) / h;
+    return (f[k + st] - f[k - st]) / (2.0 * h);
+}
+
+struct Geo {
+    int ndim, ny, nx, nz;
+    int64_t ni;
+    double hy, hx, hz;
+};
+
+// gradient components of row p at ii: {d/dy, d/dx, d/dz} (3-D) or {d/dx, d/dz}
+__device__ __forceinline__ void row_grad(const Geo& g, const double* __restrict__ row, int64_t ii, double* gy,
+                                         double* gx, double* gz) {
+    const int iz = (int)(ii % g.nz);
+    const int64_t r = ii / g.nz;
+    const int ix = (int)(r % g.nx);
+    *gz = grad1(row, ii, iz, g.nz, 1, g.hz);
+    *gx = grad1(row, ii, ix, g.nx, g.nz, g.hx);
+    *gy = g.ndim == 3 ? grad1(row, ii, (int)(r / g.nx), g.ny, (int64_t)g.nx * g.nz, g.hy) : 0.0;
+}
+
+// angle of row p at every image point; sign_rows: the rows whose x-gradient
+// signs the 3-D angle (the source rows for receivers when ns == nr)
+__global__ void angle_kernel(Geo g, const double* __restrict__ trav, const double* __restrict__ sign_rows,
+                             double* __restrict__ ang) {
+    const int p = blockIdx.y;
+    const double* row = trav + (size_t)p * g.ni;
+    const double* srow = sign_rows + (size_t)p * g.ni;
+    for (int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; ii < g.ni;
+         ii += (int64_t)gridDim.x * blockDim.x) {
+        double gy, gx, gz;
+        row_grad(g, row, ii, &gy, &gx, &gz);
+        double a;
+        if (g.ndim == 2) {
+            a = atan2(gx, gz);
+        } else {
+            double sy, sx, sz;
+            row_grad(g, srow, ii, &sy, &sx, &sz);
+            const double sg = sx > 0.0 ? 1.0 : (sx < 0.0 ? -1.0 : 0.0);
+            const double nrm = __dadd_rn(__dadd_rn(__dmul_rn(gy, gy), __dmul_rn(gx, gx)), __dmul_rn(gz, gz));
+            a = sg * acos(gz / sqrt(nrm));
+        }
+        ang[(size_t)p * g.ni + ii] = a;
+    }
+}
+
+// numpy/CPython float floor division (as the angle taper index uses it)
+__device__ double py_floordiv_d(double a, double b) {
+    const double mod = fmod(a, b);
+    double div = (a - mod) / b;
+    if (mod != 0.0 && ((b < 0) != (mod < 0))) div -= 1.0;
+    double fl;
+    if (div != 0.0) {
+        fl = floor(div);
+        if (div - fl > 0.5) fl += 1.0;
+    } else {
+        fl = copysign(0.0, a / b);
+    }
+    return fl;
+}
+
+struct FoldArgs {
+    double maxdist, amin, amax;
+    const double* taper;  // 21 values
+    int ndim;
+};
+
+// amplitude and angle taper folded with the half-angle cosines/sines into
+// the operator's float32 weight rows (as the host upload does)
+__global__ void fold_kernel(FoldArgs f, const double* __restrict__ dist, const double* __restrict__ ang,
+                            int64_t n, float* __restrict__ wc, float* __restrict__ ws,
+                            unsigned long long* __restrict__ wabs) {
+    double mx = 0.0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const double a = ang[k];
+        const double dd = dist[k] + f.maxdist;
+        const double A = f.ndim == 2 ? 1.0 / sqrt(dd) : 1.0 / dd;
+        const double aa = fabs(a);
+        double tap = 0.0;
+        if (aa < f.amax) {
+            tap = 1.0;
+            if (aa >= f.amin) {
+                long idx = (long)py_floordiv_d(20.0 * (aa - f.amin), f.amax - f.amin);
+                idx = idx < 0 ? 0 : (idx > 20 ? 20 : idx);
+                tap = f.taper[idx];
+            }
+        }
+        const double base = A * tap;
+        const float c = (float)(base * cos(a / 2.0)), s = (float)(base * sin(a / 2.0));
+        wc[k] = c;
+        ws[k] = s;
+        mx = fmax(mx, sqrt(__dadd_rn(__dmul_rn((double)c, (double)c), __dmul_rn((double)s, (double)s))));
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx > 0.0) atomicMax(wabs, (unsigned long long)__double_as_longlong(mx));
+}
+
+// ---------------------------------------------------------------------------
+// reductions and quantisation
+// ---------------------------------------------------------------------------
+// max of |x| over n values into bits of a non-negative double (*out, zeroed)
+__global__ void absmax_kernel(const double* __restrict__ x, int64_t n, unsigned long long* __restrict__ out) {
+    double m = 0.0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(x[k]));
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// non-finite values: the flat index of one in *bad (atomicMax; -1 if none)
+__global__ void finite_kernel(const double* __restrict__ x, int64_t n, long long* __restrict__ bad) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        if (!isfinite(x[k])) atomicMax(bad, (long long)k);
+}
+
+// fixed-point rows: q = rint(t * inv_dt * 2^F), and the smallest q (*qmin)
+__global__ void quantise_kernel(const double* __restrict__ t, int64_t n, double inv_dt, double scale,
+                                int32_t* __restrict__ q, int* __restrict__ qmin) {
+    int mn = INT32_MAX;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = (int32_t)__double2ll_rn(t[k] * inv_dt * scale);
+        q[k] = v;
+        mn = min(mn, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    if ((threadIdx.x & 31) == 0) atomicMin(qmin, mn);
+}
+
+// amplitude rows from distance rows: 1/sqrt(d + maxdist) (2-D), 1/(d + maxdist) (3-D)
+__global__ void amplitude_kernel(const double* __restrict__ dist, int64_t n, double maxdist, int ndim,
+                                 double* __restrict__ amp) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const double dd = dist[k] + maxdist;
+        amp[k] = ndim == 2 ? 1.0 / sqrt(dd) : 1.0 / dd;
+    }
+}
+
+__global__ void vscale_kernel(const double* __restrict__ vel, int64_t nvel, int64_t ni, float* __restrict__ vs) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ni; k += (int64_t)gridDim.x * blockDim.x)
+        vs[k] = (float)(2.0 / vel[nvel == 1 ? 0 : k]);
+}
+
+// [n][ni] rows -> (ni, n) reference layout
+__global__ void transpose_kernel(const double* __restrict__ rows, int n, int64_t ni, double* __restrict__ out) {
+    __shared__ double tile[32][33];
+    const int64_t i0 = (int64_t)blockIdx.x * 32;
+    const int j0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int j = j0 + r;
+        const int64_t i = i0 + threadIdx.x;
+        if (j < n && i < ni) tile[r][threadIdx.x] = rows[(size_t)j * ni + i];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t i = i0 + r;
+        const int j = j0 + threadIdx.x;
+        if (j < n && i < ni) out[(size_t)i * n + j] = tile[threadIdx.x][r];
+    }
+}
+
+}  // namespace
+}  // namespace kgb
+
+// ---------------------------------------------------------------------------
+// launchers (declared in kgb_internal.h)
+// ---------------------------------------------------------------------------
+namespace kgb {
+
+static int grid_for(int64_t n) {
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (int)std::min<int64_t>((n + 255) / 256, (int64_t)std::max(sms, 1) * 8);
+}
+
+int launch_analytic_rows(const TableGeom& g, const double* yax, const double* xax, const double* zax,
+                         const double* pts, int np, double vel, double* trav, double* dist, cudaStream_t s) {
+    dim3 grid((unsigned)std::max(1, grid_for(g.ni) / std::max(1, np / 8 + 1)), (unsigned)np);
+    analytic_kernel<<<grid, 256, 0, s>>>(yax, xax, zax, g.ndim, g.nx, g.nz, g.ni, pts, np, vel, trav, dist);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_eikonal_rows(const TableGeom& g, const double* speed, const int* pts, int np, double* out, unsigned* err,
+                        cudaStream_t s) {
+    if (g.ndim != 2) return set_error(KGB_ERR_NOT_IMPLEMENTED, "device eikonal tables: 2-D only");
+    eikonal_sweep_kernel<<<np, kEikThreads, 0, s>>>(g.nx, g.nz, g.hx, g.hz, speed, pts, np, out, err);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_angle_rows(const TableGeom& g, const double* trav, const double* sign_rows, int np, double* ang,
+                      cudaStream_t s) {
+    Geo geo{g.ndim, g.ny, g.nx, g.nz, g.ni, g.hy, g.hx, g.hz};
+    dim3 grid((unsigned)std::max(1, grid_for(g.ni) / std::max(1, np / 8 + 1)), (unsigned)np);
+    angle_kernel<<<grid, 256, 0, s>>>(geo, trav, sign_rows ? sign_rows : trav, ang);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_fold_rows(int ndim, double maxdist, double amin, double amax, const double* taper21,
+                     const double* dist, const double* ang, int64_t n, float* wc, float* ws,
+                     unsigned long long* wabs, cudaStream_t s) {
+    FoldArgs f{maxdist, amin, amax, taper21, ndim};
+    fold_kernel<<<grid_for(n), 256, 0, s>>>(f, dist, ang, n, wc, ws, wabs);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_absmax(const double* x, int64_t n, unsigned long long* out, cudaStream_t s) {
+    absmax_kernel<<<grid_for(n), 256, 0, s>>>(x, n, out);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_finite_check(const double* x, int64_t n, long long* bad, cudaStream_t s) {
+    finite_kernel<<<grid_for(n), 256, 0, s>>>(x, n, bad);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_quantise(const double* t, int64_t n, double inv_dt, double scale, int32_t* q, int* qmin, cudaStream_t s) {
+    quantise_kernel<<<grid_for(n), 256, 0, s>>>(t, n, inv_dt, scale, q, qmin);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_vscale(const double* vel, int64_t nvel, int64_t ni, float* vs, cudaStream_t s) {
+    vscale_kernel<<<grid_for(ni), 256, 0, s>>>(vel, nvel, ni, vs);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_amplitude_rows(const double* dist, int64_t n, double maxdist, int ndim, double* amp, cudaStream_t s) {
+    amplitude_kernel<<<grid_for(n), 256, 0, s>>>(dist, n, maxdist, ndim, amp);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_rows_to_reference(const double* rows, int n, int64_t ni, double* out, cudaStream_t s) {
+    dim3 grid((unsigned)((ni + 31) / 32), (unsigned)((n + 31) / 32));
+    transpose_kernel<<<grid, dim3(32, 8), 0, s>>>(rows, n, ni, out);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+}  // namespace kgb

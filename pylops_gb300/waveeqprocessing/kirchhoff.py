@@ -33,6 +33,8 @@ logger = logging.getLogger(__name__)
 
 _TABLE_ATTRS = ("trav", "trav_srcs", "trav_recs", "amp_srcs", "amp_recs", "angle_srcs", "angle_recs",
                 "vel", "aperture", "angleaperture", "aperturetap", "six", "rix")
+# tables built on the device, read back on first access (kgb_kirchhoff_get_table)
+_DEVICE_TABLES = {"trav_srcs": 0, "trav_recs": 1, "amp_srcs": 2, "amp_recs": 3, "angle_srcs": 4, "angle_recs": 5}
 
 
 def _value_or_sized_to_array(v, repeat: int = 1):
@@ -133,11 +135,15 @@ class Kirchhoff(LinearOperator):
         engine: str = "numpy",
         dtype="float64",
         name: str = "K",
+        tables: str = "device",
     ) -> None:
         if engine not in ["numpy", "numba", "cuda"]:
             raise KeyError("engine must be numpy or numba or cuda")
+        if tables not in ("device", "host"):
+            raise ValueError("tables must be 'device' or 'host'")
         object.__setattr__(self, "_h", None)
         object.__setattr__(self, "_dirty", set())
+        object.__setattr__(self, "_device_built", False)
         (self.ndims, _, dims, self.ny, self.nx, self.nz, ns, nr, _, _, _, dsamp,
          origin) = Kirchhoff._identify_geometry(z, x, srcs, recs, y=y)
         self.dt = t[1] - t[0]
@@ -156,8 +162,15 @@ class Kirchhoff(LinearOperator):
 
         # tables (kirchhoff.py:303-362)
         self.travsrcrec = True
+        # analytic tables and 2-D eikonal tables are built on the device
+        # (after the operator exists, below); 3-D eikonal tables on the host
+        device_tables = tables == "device" and (mode == "analytic" or (mode == "eikonal" and self.ndims == 2))
+        if device_tables and mode == "analytic" and not isinstance(vel, (float, int)):
+            raise ValueError("vel must be scalar for mode=analytical")
         if mode in ["analytic", "eikonal", "byot"]:
-            if mode in ["analytic", "eikonal"]:
+            if mode in ["analytic", "eikonal"] and device_tables:
+                pass
+            elif mode in ["analytic", "eikonal"]:
                 (trav_srcs, trav_recs, dist_srcs, dist_recs, trav_srcs_grad,
                  trav_recs_grad) = Kirchhoff._traveltime_table(z, x, srcs, recs, vel, y=y, mode=mode)
                 self.trav_srcs, self.trav_recs = trav_srcs, trav_recs
@@ -194,7 +207,7 @@ class Kirchhoff(LinearOperator):
             raise NotImplementedError("method must be analytic, eikonal or byot")
 
         # angles with the vertical (kirchhoff.py:364-393)
-        if self.dynamic:
+        if self.dynamic and not device_tables:
             ni_ = int(np.prod(dims))
             if self.ndims == 2:
                 self.angle_srcs = np.arctan2(trav_srcs_grad[0], trav_srcs_grad[1]).reshape(ni_, ns)
@@ -247,7 +260,10 @@ class Kirchhoff(LinearOperator):
             self.vel = (np.asarray(vel).flatten() if not isinstance(vel, (float, int))
                         else vel * np.ones(int(np.prod(dims))))
         self.cop = _WaveletOperator(self, np.asarray(self.wav), self.wavcenter, dtype)
-        self._create_native()
+        if device_tables:
+            self._create_native(build=dict(mode=mode, y=y, x=x, z=z, srcs=srcs, recs=recs, vel=vel))
+        else:
+            self._create_native()
 
     # single-table traveltimes: index and fraction (kirchhoff.py:395-398),
     # computed on first access (the device copy is made from `trav` itself,
@@ -270,7 +286,7 @@ class Kirchhoff(LinearOperator):
         if name in _TABLE_ATTRS:
             self._dirty.add(name)
 
-    def _create_native(self):
+    def _create_native(self, build=None):
         L = _native.lib()
         wav = np.ascontiguousarray(np.asarray(self.wav, dtype=np.float64))
         h = ctypes.c_void_p()
@@ -278,8 +294,47 @@ class Kirchhoff(LinearOperator):
                                              float(self.dt), int(bool(self.dynamic)), _native.dptr(wav),
                                              int(wav.size), self.wavcenter))
         object.__setattr__(self, "_h", h)
-        self._dirty.update(_TABLE_ATTRS)
-        self._sync_tables()
+        if build is None:
+            self._dirty.update(_TABLE_ATTRS)
+            self._sync_tables()
+            return
+        # tables on the device: traveltimes, distances, gradients, angles and
+        # amplitudes computed where the kernels read them
+        f64 = lambda a: np.ascontiguousarray(np.asarray(a, dtype=np.float64))  # noqa: E731
+        ax = [None if build["y"] is None else f64(build["y"]), f64(build["x"]), f64(build["z"])]
+        vel = build["vel"]
+        velv = f64([vel]) if isinstance(vel, (float, int)) else f64(vel).ravel()
+        md = ctypes.c_double(0.0)
+        if self.dynamic:
+            dyn = [f64(self.aperture), f64(self.angleaperture), f64(self.aperturetap)]
+            six = np.ascontiguousarray(np.asarray(self.six).astype(np.int64))
+            rix = np.ascontiguousarray(np.asarray(self.rix).astype(np.int64))
+            dptrs = [_native.dptr(a) for a in dyn] + [_native.i64ptr(six), _native.i64ptr(rix)]
+        else:
+            dptrs = [None] * 5
+        _native.check(L.kgb_kirchhoff_build_tables(
+            h, 0 if build["mode"] == "analytic" else 1, self.ndims,
+            None if ax[0] is None else _native.dptr(ax[0]), 0 if ax[0] is None else ax[0].size,
+            _native.dptr(ax[1]), ax[1].size, _native.dptr(ax[2]), ax[2].size,
+            _native.dptr(f64(build["srcs"])), _native.dptr(f64(build["recs"])), _native.dptr(velv), velv.size,
+            *dptrs, ctypes.byref(md)))
+        if self.dynamic:
+            object.__setattr__(self, "maxdist", md.value)
+        object.__setattr__(self, "_device_built", True)
+        self._dirty.clear()
+
+    def __getattr__(self, name):
+        # tables built on the device are read back on first access
+        if name in _DEVICE_TABLES and self.__dict__.get("_device_built") and self.__dict__.get("_h") is not None:
+            if name[:3] in ("amp", "ang") and not self.__dict__.get("dynamic"):
+                raise AttributeError(name)
+            n = self.__dict__["ns"] if name.endswith("srcs") else self.__dict__["nr"]
+            out = np.empty((self.__dict__["ni"], n), dtype=np.float64)
+            _native.check(_native.lib().kgb_kirchhoff_get_table(self.__dict__["_h"], _DEVICE_TABLES[name],
+                                                                _native.dptr(out)))
+            object.__setattr__(self, name, out)
+            return out
+        raise AttributeError(f"{type(self).__name__!r} object has no attribute {name!r}")
 
     def _sync_tables(self):
         if not self._dirty:
@@ -330,12 +385,21 @@ class Kirchhoff(LinearOperator):
         keys = ("ns", "nr", "nt", "ni", "frac_bits", "wavelet_len", "offset_gate", "dynamic", "nonneg",
                 "adjoint_splits", "kernels_forward", "kernels_adjoint", "spread_variant", "spread_split",
                 "max_bin_count")
-        return {k: int(v[i]) for i, k in enumerate(keys)}
+        out = {k: int(v[i]) for i, k in enumerate(keys)}
+        out["adjoint_staged"] = int(v[15]) & 1  # source records staged by TMA
+        out["wait_error"] = int(v[15]) >> 1     # nonzero: a bounded wait of a kernel gave up
+        return out
 
     def set_spread_variant(self, variant: int) -> None:
         """Select the forward kernel: 0 fixed-point atomics, 1 warp-binned
         (one trace per warp), 2 warp-binned (two traces per warp)."""
         _native.check(_native.lib().kgb_kirchhoff_set_variant(self._h, int(variant)))
+
+    def set_adjoint_staging(self, on: bool = True) -> None:
+        """Dynamic operators: stage the source records of the adjoint through
+        shared memory with TMA copies (the default) or let the gather load
+        them itself; the image is the same bit for bit."""
+        _native.check(_native.lib().kgb_kirchhoff_set_adjoint_staging(self._h, 1 if on else 0))
 
     def set_weight_precision(self, precision: str = "float32") -> None:
         """Store the dynamic weights as ``'bfloat16'`` (8-byte table records,
