@@ -194,9 +194,10 @@ int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x_dev, float* y_dev, i
  * used by the tile autotuner. */
 int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant);
 
-/* Adjoint of dynamic operators: 1 (the default) stages the source records
- * through shared memory with TMA bulk-tensor copies, 0 loads them from
- * global memory in the gather itself.  Both give the same image bit for bit.
+/* Adjoint of dynamic operators: 1 stages the source records through shared
+ * memory with TMA bulk-tensor copies, 0 (the default; faster on the
+ * workloads measured) loads them from global memory in the gather itself.
+ * Both give the same image bit for bit.
  * No reference counterpart (the reference's adjoint kernels,
  * _kirchhoff_cuda.py:194-298, read their tables directly). */
 int kgb_kirchhoff_set_adjoint_staging(kgb_kirchhoff* op, int on);

@@ -211,7 +211,7 @@ struct kgb_kirchhoff {
     unsigned max_bin_count = 0;          // its last result
     CUtensorMap stab_map, stab2_map;     // TMA maps over stab / stab2 (see KirchDev::rec_map)
     bool stab_map_ok = false, stab2_map_ok = false;
-    bool adjoint_staging = true;         // use the TMA-staged adjoint where a record map exists
+    bool adjoint_staging = false;        // use the TMA-staged adjoint where a record map exists (off: slower)
     // tables built on the device (kgb_kirchhoff_build_tables): [n][ni]
     // float64 rows kept for kgb_kirchhoff_get_table
     double* trav64_s = nullptr;

@@ -81,8 +81,38 @@ __device__ __forceinline__ bool ek_root(int m, const double* c, const double* b,
     return true;
 }
 
-// the host solver's local update (eikonal.cpp, update()) with every finite
-// neighbour taken as known; +inf when no neighbour is finite
+// The host solver's local update (eikonal.cpp, update()) on a set of m
+// axes: second order on every axis that has it, else first order dropping
+// the latest axes.  `drop2` first retries second order on the earliest axis
+// alone: in a marching order that axis would have been the only one known.
+__device__ double ek_solve(int m, const double* a2o, const double* b2o, const double* a1, const double* b1,
+                           double slow2, bool drop2) {
+    double t;
+    if (ek_root(m, a2o, b2o, slow2, &t)) return t;
+    const int o0 = (m == 2 && b1[1] < b1[0]) ? 1 : 0, o1 = 1 - o0;
+    if (m == 2 && drop2) {
+        const double aa[1] = {a2o[o0]}, bb[1] = {b2o[o0]};
+        if (ek_root(1, aa, bb, slow2, &t)) return t;
+    }
+    if (m == 2) {
+        const double aa[2] = {a1[o0], a1[o1]}, bb[2] = {b1[o0], b1[o1]};
+        if (ek_root(2, aa, bb, slow2, &t)) return t;
+    }
+    {
+        const double aa[1] = {a1[o0]}, bb[1] = {b1[o0]};
+        if (ek_root(1, aa, bb, slow2, &t)) return t;
+    }
+    return b1[o0] + sqrt(slow2 / a1[o0]);
+}
+
+// Tentative time of node (i0, i1) from its finite neighbours, reproducing
+// what fast marching computes for it: marching accepts nodes in increasing
+// time, so a node's neighbours become known in increasing order and its
+// value is the smaller of the update with the earliest axis alone and the
+// update with both axes (each with the host solver's stencil rules).  With
+// every finite neighbour taken as known, this keeps a later (larger)
+// neighbour from turning a valid second-order solve into a first-order
+// one.  +inf when no neighbour is finite.
 __device__ double ek_update(const double* T, int n0, int n1, double h0, double h1, int i0, int i1,
                             double slow2) {
     const int64_t k = (int64_t)i0 * n1 + i1;
@@ -127,22 +157,11 @@ __device__ double ek_update(const double* T, int n0, int n1, double h0, double h
         }
     }
     if (m == 0) return INFINITY;
-    double t;
-    if (ek_root(m, a2o, b2o, slow2, &t)) return t;
-    int o0 = 0, o1 = 1;
-    if (m == 2 && b1[1] < b1[0]) {
-        o0 = 1;
-        o1 = 0;
-    }
-    if (m == 2) {
-        const double aa[2] = {a1[o0], a1[o1]}, bb[2] = {b1[o0], b1[o1]};
-        if (ek_root(2, aa, bb, slow2, &t)) return t;
-    }
-    {
-        const double aa[1] = {a1[o0]}, bb[1] = {b1[o0]};
-        if (ek_root(1, aa, bb, slow2, &t)) return t;
-    }
-    return b1[o0] + sqrt(slow2 / a1[o0]);
+    const double both = ek_solve(m, a2o, b2o, a1, b1, slow2, true);
+    if (m == 1) return both;
+    const int o = b1[1] < b1[0] ? 1 : 0;
+    const double one = ek_solve(1, a2o + o, b2o + o, a1 + o, b1 + o, slow2, false);
+    return one < both ? one : both;
 }
 
 constexpr int kEikThreads = 320;

@@ -9,10 +9,12 @@ produces its own traces); the adjoint sums the ranks' partial images with one
 all-reduce; a solver needs global norms and dot products of data-space
 vectors (one scalar all-reduce each), while model-space vectors are the same
 on every rank.  :class:`DistributedKirchhoff` and :func:`cgls` implement
-that on ``torch.distributed`` (NCCL for CUDA tensors, gloo for host ones).
+that on ``torch.distributed`` (NCCL for CUDA tensors, gloo for host ones);
+:func:`lsqr` does the same for LSQR.
 
 The reference has no distributed code (PyLops runs one process); the
-recurrences are those of ``pylops/optimization/cls_basic.py:334-708``.
+recurrences are those of ``pylops/optimization/cls_basic.py:334-708`` (CGLS)
+and ``:711-1351`` (LSQR).
 With two ranks the image sum is exact-order-independent (a + b = b + a); with
 more, the order of the all-reduce is the backend's.
 """
@@ -26,7 +28,7 @@ import numpy as np
 from .linearoperator import LinearOperator
 from .utils.backend import is_torch
 
-__all__ = ["source_shard", "DistributedKirchhoff", "cgls"]
+__all__ = ["source_shard", "DistributedKirchhoff", "cgls", "lsqr"]
 
 
 def source_shard(ns: int, rank: int, world: int) -> Tuple[int, int]:
@@ -127,3 +129,118 @@ def cgls(Op: DistributedKirchhoff, y, x0: Optional = None, niter: int = 10, damp
         cost1.append(np.sqrt(cost[-1] ** 2 + dampsq * abs(_local_dot(x, x))))
     istop = 1 if kold < tol else 2
     return x, istop, iiter, kold, cost1[iiter], np.array(cost)
+
+
+def _global_norm(a, group=None) -> float:
+    return float(np.sqrt(_global_dot(a, a, group)))
+
+
+def lsqr(Op: DistributedKirchhoff, y, x0: Optional = None, niter: int = 10, damp: float = 0.0, atol: float = 1e-8,
+         btol: float = 1e-8, conlim: float = 1e8):
+    """LSQR (``cls_basic.py:835-1136``) on a source-sharded operator: ``y`` is
+    this rank's data, x0 and the result the (replicated) model.  The
+    data-space vector u is sharded, so its norm is one float64 all-reduce per
+    iteration; the model-space vectors v, w, x are the same on every rank and
+    their norms are local.  Every scalar of the Golub-Kahan bidiagonalisation
+    and the Paige-Saunders rotations is float64 and identical on all ranks.
+    Returns ``(x, istop, iiter, r1norm, r2norm, anorm, acond, arnorm, xnorm,
+    var, cost)`` as ``pylops.optimization.basic.lsqr`` (var is not computed:
+    None)."""
+    g = Op.group
+    ctol = 1.0 / conlim if conlim > 0 else 0.0
+    dampsq = damp * damp
+    anorm = acond = ddnorm = res2 = xnorm = xxnorm = z = 0.0
+    cs2, sn2 = -1.0, 0.0
+    if x0 is None:
+        x = y.new_zeros(Op.shape[1]) if is_torch(y) else np.zeros(Op.shape[1], dtype=np.float64)
+        u = y.clone() if is_torch(y) else np.array(y, dtype=np.float64, copy=True)
+    else:
+        x = x0.clone() if is_torch(x0) else np.array(x0, dtype=np.float64, copy=True)
+        u = y - Op.matvec(x)
+    alfa = 0.0
+    beta = _global_norm(u, g)
+    if beta > 0:
+        u = u / beta
+        v = Op.rmatvec(u)
+        alfa = float(np.sqrt(abs(_local_dot(v, v))))
+        if alfa > 0:
+            v = v / alfa
+    else:
+        v = x.clone() if is_torch(x) else x.copy()
+    w = v.clone() if is_torch(v) else v.copy()
+    arnorm0 = alfa * beta
+    rhobar, phibar, bnorm = alfa, beta, beta
+    r1norm = r2norm = rnorm = beta
+    arnorm = arnorm0
+    cost = [beta]
+    istop, iiter = 0, 0
+    if arnorm0 == 0:
+        return x, istop, iiter, r1norm, r2norm, anorm, acond, arnorm, xnorm, None, np.array(cost)
+    while iiter < niter and istop == 0:
+        # bidiagonalisation: u (sharded) and v (replicated)
+        u = Op.matvec(v) - alfa * u
+        beta = _global_norm(u, g)
+        if beta > 0:
+            u = u / beta
+            anorm = float(np.sqrt(anorm ** 2 + alfa ** 2 + beta ** 2 + dampsq))
+            v = Op.rmatvec(u) - beta * v
+            alfa = float(np.sqrt(abs(_local_dot(v, v))))
+            if alfa > 0:
+                v = v / alfa
+        # plane rotations (damping, then the bidiagonal)
+        rhobar1 = float(np.hypot(rhobar, damp))
+        cs1, sn1 = rhobar / rhobar1, damp / rhobar1
+        psi = sn1 * phibar
+        phibar = cs1 * phibar
+        rho = float(np.hypot(rhobar1, beta))
+        cs, sn = rhobar1 / rho, beta / rho
+        theta = sn * alfa
+        rhobar = -cs * alfa
+        phi = cs * phibar
+        phibar = sn * phibar
+        tau = sn * phi
+        t1, t2 = phi / rho, -theta / rho
+        ddnorm += float(abs(_local_dot(w, w))) / (rho * rho)
+        x = x + t1 * w
+        w = v + t2 * w
+        # norms and stopping tests (cls_basic.py:1066-1133)
+        delta = sn2 * rho
+        gambar = -cs2 * rho
+        rhs = phi - delta * z
+        zbar = rhs / gambar
+        xnorm = float(np.sqrt(xxnorm + zbar ** 2))
+        gamma = float(np.hypot(gambar, theta))
+        cs2, sn2 = gambar / gamma, theta / gamma
+        z = rhs / gamma
+        xxnorm += z ** 2
+        acond = anorm * float(np.sqrt(ddnorm))
+        res2 += psi ** 2
+        rnorm = float(np.sqrt(phibar ** 2 + res2))
+        arnorm = alfa * abs(tau)
+        r1sq = rnorm ** 2 - dampsq * xxnorm
+        r1norm = float(np.sqrt(abs(r1sq))) * (-1.0 if r1sq < 0 else 1.0)
+        r2norm = rnorm
+        cost.append(abs(r1norm))
+        test1 = rnorm / bnorm
+        test2 = arnorm / arnorm0
+        test3 = 1.0 / acond
+        t1_ = test1 / (1.0 + anorm * xnorm / bnorm)
+        rtol = btol + atol * anorm * xnorm / bnorm
+        # the reference tests iiter before counting this iteration, so a run
+        # that ends on niter leaves istop = 0 (cls_basic.py:1110-1136)
+        if iiter >= niter:
+            istop = 7
+        if 1 + test3 <= 1:
+            istop = 6
+        if 1 + test2 <= 1:
+            istop = 5
+        if 1 + t1_ <= 1:
+            istop = 4
+        if test3 <= ctol:
+            istop = 3
+        if test2 <= atol:
+            istop = 2
+        if test1 <= rtol:
+            istop = 1
+        iiter += 1
+    return x, istop, iiter, r1norm, r2norm, anorm, acond, arnorm, xnorm, None, np.array(cost)

@@ -397,8 +397,9 @@ class Kirchhoff(LinearOperator):
 
     def set_adjoint_staging(self, on: bool = True) -> None:
         """Dynamic operators: stage the source records of the adjoint through
-        shared memory with TMA copies (the default) or let the gather load
-        them itself; the image is the same bit for bit."""
+        shared memory with TMA copies, or let the gather load them itself
+        (the default, faster on the workloads measured); the image is the
+        same bit for bit."""
         _native.check(_native.lib().kgb_kirchhoff_set_adjoint_staging(self._h, 1 if on else 0))
 
     def set_weight_precision(self, precision: str = "float32") -> None:

@@ -1,8 +1,8 @@
-"""Source-sharded operator and CGLS with two gloo ranks on the CPU; each
+"""Source-sharded operator, CGLS and LSQR with two gloo ranks on the CPU; each
 rank's local operator is the float64 oracle of its sources (the GPU operator
 takes its place on a GPU).  The sharded forward must reproduce the
-unsharded rows, the adjoint the unsharded image, and CGLS the unsharded
-iterates, to float64 rounding."""
+unsharded rows, the adjoint the unsharded image, and CGLS and LSQR the
+unsharded iterates, stopping reasons and norms, to float64 rounding."""
 
 import os
 import socket
@@ -24,8 +24,8 @@ def _free_port():
 def _rank_main(rank, world, port, errfile):
     import torch.distributed as dist
 
-    from oracle.kirchhoff_oracle import KirchhoffOracle, cgls as oracle_cgls
-    from pylops_gb300.distributed import DistributedKirchhoff, cgls, source_shard
+    from oracle.kirchhoff_oracle import KirchhoffOracle, cgls as oracle_cgls, lsqr as oracle_lsqr
+    from pylops_gb300.distributed import DistributedKirchhoff, cgls, lsqr, source_shard
     from pylops_gb300.linearoperator import LinearOperator
     from tests.helpers import kwargs_from_golden, load
 
@@ -65,6 +65,19 @@ def _rank_main(rank, world, port, errfile):
         assert np.linalg.norm(x - xr) / np.linalg.norm(xr) < 1e-10
         assert np.allclose(cost, cost_r, rtol=1e-10)
         assert abs(r1 - r1_r) <= 1e-10 * abs(r1_r)
+        # LSQR: the data-space norm is the one all-reduce per iteration
+        out = lsqr(D, y[rows], niter=6)
+        ref_l = oracle_lsqr(full.matvec, full.rmatvec, y, full.ni, niter=6)
+        assert out[2] == ref_l[2] and out[1] == ref_l[1]
+        assert np.linalg.norm(out[0] - ref_l[0]) / np.linalg.norm(ref_l[0]) < 1e-10
+        assert np.allclose(out[10], ref_l[9], rtol=1e-10)
+        for k in range(3, 9):  # r1norm, r2norm, anorm, acond, arnorm, xnorm
+            assert abs(out[k] - ref_l[k]) <= 1e-9 * abs(ref_l[k]), (k, out[k], ref_l[k])
+        # with damping and an early stop on atol/btol
+        out = lsqr(D, y[rows], niter=50, damp=0.3, atol=1e-3, btol=1e-3)
+        ref_l = oracle_lsqr(full.matvec, full.rmatvec, y, full.ni, niter=50, damp=0.3, atol=1e-3, btol=1e-3)
+        assert out[2] == ref_l[2] and out[1] == ref_l[1] and out[1] != 0
+        assert np.linalg.norm(out[0] - ref_l[0]) / np.linalg.norm(ref_l[0]) < 1e-9
     except Exception as e:  # report to the parent, which fails the test
         with open(f"{errfile}.{rank}", "w") as f:
             f.write(repr(e))
@@ -86,7 +99,7 @@ def test_source_shard_covers_every_source_once():
             assert max(b - a for a, b in blocks) - min(b - a for a, b in blocks) <= 1
 
 
-def test_two_rank_sharded_operator_and_cgls(tmp_path):
+def test_two_rank_sharded_operator_cgls_and_lsqr(tmp_path):
     import torch.multiprocessing as mp
 
     errfile = str(tmp_path / "err")
