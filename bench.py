@@ -610,7 +610,7 @@ def batch_record(args):
     t0 = time.perf_counter()
     probs = random_problems(args.batch_problems, seed=3)
     B = build_batch(probs)
-    tune = B.autotune(candidates=(2, 4, 8), reps=2)
+    tune = B.autotune(candidates=(2, 4, 8), reps=2)  # forward tile and adjoint shape
     t_setup = time.perf_counter() - t0
     y = torch.cat([torch.as_tensor(K @ p["refl"].ravel().astype(np.float32), device="cuda")
                    for K, p in zip(B.ops, probs)])
@@ -640,6 +640,8 @@ def batch_record(args):
         "config": {"workload": "batched_lsm_256x2d_kinematic_nt501", "problems": len(B.ops),
                    "cgls_iterations": args.cgls_iters, "model_total": B.shape[1], "data_total": B.shape[0],
                    "tile_ms": {str(k): round(v, 3) for k, v in tune.items()}, "tile": B.tile,
+                   "gather_shape": {"receivers_in_registers": B.gather_shape[0],
+                                    "points_per_thread": B.gather_shape[1]},
                    "setup_s": round(t_setup, 2)},
         "problems_per_s": round(len(B.ops) / step, 2),
         "residual_reduction_median": round(float(np.median(rels)), 5),

@@ -284,6 +284,11 @@ int kgb_batch_create(kgb_batch** batch, kgb_kirchhoff* const* ops, int nops);
 int kgb_batch_destroy(kgb_batch* batch);
 int kgb_batch_sizes(const kgb_batch* batch, int64_t* sizes4); /* {P, model, data, tile} */
 int kgb_batch_set_tile(kgb_batch* batch, int receivers_per_item); /* 1, 2, 4 or 8 (autotuner) */
+/* Shape of the batched adjoint (autotuner): receiver traveltimes held in
+ * registers per image point (4 or 8) and image points per thread (1 or 2);
+ * the result is the same for every shape (fixed summation order per point).
+ * No reference counterpart. */
+int kgb_batch_set_gather(kgb_batch* batch, int receivers_in_registers, int points_per_thread);
 int kgb_batch_forward(kgb_batch* batch, const float* m_dev, float* d_dev, void* stream);
 int kgb_batch_adjoint(kgb_batch* batch, const float* d_dev, float* m_dev, void* stream);
 int kgb_batch_cgls(kgb_batch* batch, const float* y_dev, float* x_dev, int niter, double damp, double tol,

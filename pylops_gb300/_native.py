@@ -76,6 +76,7 @@ _SIGNATURES = {
     "kgb_batch_destroy": ([c_vp], c_int),
     "kgb_batch_sizes": ([c_vp, c_i64p], c_int),
     "kgb_batch_set_tile": ([c_vp, c_int], c_int),
+    "kgb_batch_set_gather": ([c_vp, c_int, c_int], c_int),
     "kgb_batch_forward": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_batch_adjoint": ([c_vp, c_vp, c_vp, c_vp], c_int),
     "kgb_batch_cgls": ([c_vp, c_vp, c_vp, c_int, c_dbl, c_dbl, c_int, c_dp, c_ip, c_dp, c_vp], c_int),

@@ -184,42 +184,77 @@ batch_correlate_kernel(const Prob* __restrict__ probs, int nprob, const float* _
     }
 }
 
-// One CTA per item (problem, tile of kTile image points); each thread sums
-// its image point over all traces of its problem in a fixed order.
-__global__ void __launch_bounds__(kTile, 8)  // 30 registers: the SM's 64 warps hide the load chain
-batch_gather_kernel(const Prob* __restrict__ probs, const GatherItem* __restrict__ items,
+// Adjoint: one CTA per (problem, tile) item of the work list, one launch for
+// the whole batch; a tile is kTile * PPT image points, each thread sums PPT
+// of them (kTile apart) over all traces of its problem in a fixed order,
+// with RC receiver traveltimes per point in registers.  (A persistent grid
+// walking the list costs the loop's registers: ~200 bytes of spills at the
+// 32-register budget that keeps the SM's 64 warps resident.)
+// RC and PPT are chosen per batch by the autotuner (kgb_batch_set_gather):
+// more points per thread put more independent record -> data load chains
+// in flight per thread, more receivers in registers read the source
+// traveltimes fewer times; both cost registers and so resident warps.
+template <int RC, int PPT>
+__global__ void __launch_bounds__(kTile, 8 / PPT)
+batch_gather_kernel(const Prob* __restrict__ probs, const GatherItem* __restrict__ items, int nitems,
                     const float2* __restrict__ dc, float* __restrict__ img) {
-    const GatherItem it_ = items[blockIdx.x];
-    const Prob P = probs[it_.p];
-    const int64_t ii = (int64_t)it_.tile * kTile + threadIdx.x;
-    if (ii >= P.ni) return;
-    const float2* __restrict__ d2 = dc + P.d_off;
-    float total = 0.f;
-    for (int r0 = 0; r0 < P.nr; r0 += kRC) {
-        int tr[kRC];
-        const int nrc = min(kRC, P.nr - r0);
+    {
+        const int item = blockIdx.x;
+        if (item >= nitems) return;
+        const GatherItem it_ = items[item];
+        const Prob& P = probs[it_.p];
+        const int ni = (int)P.ni, ns = P.ns, nr = P.nr, nt = P.nt, F = P.F, nonneg = P.nonneg;
+        const int i0 = it_.tile * PPT * kTile + (int)threadIdx.x;  // first point of this thread (problem-local)
+        if (i0 >= ni) return;
+        const int32_t* __restrict__ tsq = P.tsq;
+        const int32_t* __restrict__ trq = P.trq;
+        const float2* __restrict__ d2 = dc + P.d_off;
+        float total[PPT];
 #pragma unroll
-        for (int r = 0; r < kRC; ++r) tr[r] = r < nrc ? __ldg(P.trq + (size_t)(r0 + r) * P.ni + ii) : 0;
-        float chunk = 0.f;
-        for (int is = 0; is < P.ns; ++is) {
-            const int ts = __ldg(P.tsq + (size_t)is * P.ni + ii);
-            const float2* __restrict__ drow = d2 + ((size_t)is * P.nr + r0) * P.nt;
+        for (int q = 0; q < PPT; ++q) total[q] = 0.f;
+        for (int r0 = 0; r0 < nr; r0 += RC) {
+            int tr[PPT][RC];
+            const int nrc = min(RC, nr - r0);
 #pragma unroll
-            for (int r = 0; r < kRC; ++r) {
-                if (r < nrc) {
-                    const int s = ts + tr[r];
-                    if (fp_valid(s, P.F, P.nt, P.nonneg)) {
-                        const int t = fp_index(s, P.F, P.nonneg);
-                        const float w = fp_frac(s, t, P.F);
-                        const float2 dd = __ldg(drow + ((size_t)r * P.nt + t));
-                        chunk += fmaf(w, dd.y - dd.x, dd.x);
+            for (int q = 0; q < PPT; ++q)
+#pragma unroll
+                for (int r = 0; r < RC; ++r) {
+                    const int ii = i0 + q * kTile;
+                    tr[q][r] = (r < nrc && ii < ni) ? __ldg(trq + (size_t)(r0 + r) * ni + ii) : 0;
+                }
+            float chunk[PPT];
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) chunk[q] = 0.f;
+            for (int is = 0; is < ns; ++is) {
+                const float2* __restrict__ drow = d2 + ((size_t)is * nr + r0) * nt;
+#pragma unroll
+                for (int q = 0; q < PPT; ++q) {
+                    const int ii = i0 + q * kTile;
+                    if (ii >= ni) continue;
+                    const int ts = __ldg(tsq + (size_t)is * ni + ii);
+#pragma unroll
+                    for (int r = 0; r < RC; ++r) {
+                        if (r < nrc) {
+                            const int s = ts + tr[q][r];
+                            if (fp_valid(s, F, nt, nonneg)) {
+                                const int t = fp_index(s, F, nonneg);
+                                const float w = fp_frac(s, t, F);
+                                const float2 dd = __ldg(drow + ((size_t)r * nt + t));
+                                chunk[q] += fmaf(w, dd.y - dd.x, dd.x);
+                            }
+                        }
                     }
                 }
             }
+#pragma unroll
+            for (int q = 0; q < PPT; ++q) total[q] += chunk[q];
         }
-        total += chunk;
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const int ii = i0 + q * kTile;
+            if (ii < ni) img[P.m_off + ii] = total[q];
+        }
     }
-    img[P.m_off + ii] = total;
 }
 
 // ---------------------------------------------------------------- CGLS
@@ -388,8 +423,11 @@ struct kgb_batch {
     Prob* d_probs = nullptr;
     SpreadItem* d_spread[4] = {nullptr, nullptr, nullptr, nullptr};  // R = 1, 2, 4, 8
     int n_spread[4] = {0, 0, 0, 0};
-    GatherItem* d_gather = nullptr;
-    int n_gather = 0;
+    // adjoint work lists for 1 and 2 image points per thread, and the
+    // autotuned shape: receivers in registers (4 or 8), points per thread
+    GatherItem* d_gather[2] = {nullptr, nullptr};
+    int n_gather[2] = {0, 0};
+    int grc = 8, gppt = 1;
     SegItem* d_mseg = nullptr;
     SegItem* d_dseg = nullptr;
     int n_mseg = 0, n_dseg = 0;
@@ -438,10 +476,20 @@ int batch_adjoint(kgb_batch* b, const float* d, float* img, cudaStream_t s) {
     const int64_t nb = std::min<int64_t>(b->ntraces, 8 * 152);
     batch_correlate_kernel<<<(unsigned)nb, 256, smem, s>>>(b->d_probs, b->nprob, d, b->dc, b->ntraces, b->span_max,
                                                           b->Lpad_max);
-    batch_gather_kernel<<<b->n_gather, kTile, 0, s>>>(b->d_probs, b->d_gather, b->dc, img);
+    const int k = (b->grc == 8 ? 2 : 0) + (b->gppt == 2 ? 1 : 0);
+    const int n = b->n_gather[b->gppt - 1];
+    const GatherItem* items = b->d_gather[b->gppt - 1];
+    const int grid = std::max(1, n);
+    switch (k) {
+        case 0: batch_gather_kernel<4, 1><<<grid, kTile, 0, s>>>(b->d_probs, items, n, b->dc, img); break;
+        case 1: batch_gather_kernel<4, 2><<<grid, kTile, 0, s>>>(b->d_probs, items, n, b->dc, img); break;
+        case 2: batch_gather_kernel<8, 1><<<grid, kTile, 0, s>>>(b->d_probs, items, n, b->dc, img); break;
+        default: batch_gather_kernel<8, 2><<<grid, kTile, 0, s>>>(b->d_probs, items, n, b->dc, img); break;
+    }
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
+
 
 template <typename T>
 int upload(T** dst, const std::vector<T>& v) {
@@ -569,11 +617,14 @@ int kgb_batch_create(kgb_batch** out, kgb_kirchhoff* const* ops, int nops) {
             rc = upload(&b->d_spread[k], items);
         }
         if (rc) break;
-        std::vector<GatherItem> gi;
-        for (int p = 0; p < nops; ++p)
-            for (int64_t t = 0; t * kTile < probs[p].ni; ++t) gi.push_back({p, (int)t});
-        b->n_gather = (int)gi.size();
-        if ((rc = upload(&b->d_gather, gi))) break;
+        for (int ppt = 1; ppt <= 2 && !rc; ++ppt) {
+            std::vector<GatherItem> gi;
+            for (int p = 0; p < nops; ++p)
+                for (int64_t t = 0; t * kTile * ppt < probs[p].ni; ++t) gi.push_back({p, (int)t});
+            b->n_gather[ppt - 1] = (int)gi.size();
+            rc = upload(&b->d_gather[ppt - 1], gi);
+        }
+        if (rc) break;
         std::vector<SegItem> ms, ds;
         std::vector<int> fm, fd;
         seg_items(moff, mlen, 8192, ms, fm);
@@ -607,7 +658,8 @@ int kgb_batch_destroy(kgb_batch* b) {
     if (!b) return KGB_OK;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    void* ptrs[] = {b->d_probs, b->d_spread[0], b->d_spread[1], b->d_spread[2], b->d_spread[3], b->d_gather,
+    void* ptrs[] = {b->d_probs, b->d_spread[0], b->d_spread[1], b->d_spread[2], b->d_spread[3], b->d_gather[0],
+                    b->d_gather[1],
                     b->d_mseg, b->d_dseg, b->d_fm, b->d_fd, b->dc, b->absmax, b->x, b->c, b->r, b->sv, b->q,
                     b->partials, b->st, b->cost, b->cost1};
     for (void* p : ptrs)
@@ -627,6 +679,17 @@ int kgb_batch_set_tile(kgb_batch* b, int receivers_per_item) {
     const int R = receivers_per_item;
     if (R != 1 && R != 2 && R != 4 && R != 8) return set_error(KGB_ERR_VALUE, "batch_set_tile: receivers per item must be 1, 2, 4 or 8");
     b->R = R;
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    return KGB_OK;
+}
+
+int kgb_batch_set_gather(kgb_batch* b, int receivers_in_registers, int points_per_thread) {
+    if (!b) return set_error(KGB_ERR_VALUE, "batch_set_gather: null batch");
+    if ((receivers_in_registers != 4 && receivers_in_registers != 8) || (points_per_thread != 1 && points_per_thread != 2))
+        return set_error(KGB_ERR_VALUE, "batch_set_gather: receivers in registers 4 or 8, points per thread 1 or 2");
+    b->grc = receivers_in_registers;
+    b->gppt = points_per_thread;
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
     return KGB_OK;

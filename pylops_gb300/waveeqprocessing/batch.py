@@ -50,6 +50,7 @@ class KirchhoffBatch(LinearOperator):
         super().__init__(dtype=np.dtype(dtype), shape=(int(self.data_offsets[-1]), int(self.model_offsets[-1])),
                          name=name)
         self.tile = 8
+        self.gather_shape = (8, 1)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -92,9 +93,18 @@ class KirchhoffBatch(LinearOperator):
         _native.check(_native.lib().kgb_batch_set_tile(self._h, int(receivers_per_item)))
         self.tile = int(receivers_per_item)
 
-    def autotune(self, candidates=(2, 4, 8), reps: int = 3) -> dict:
-        """Time the forward and adjoint for each forward tile (receivers per
-        work item) on this batch and keep the fastest; returns the timings."""
+    def set_gather(self, receivers_in_registers: int, points_per_thread: int) -> None:
+        _native.check(_native.lib().kgb_batch_set_gather(self._h, int(receivers_in_registers),
+                                                         int(points_per_thread)))
+        self.gather_shape = (int(receivers_in_registers), int(points_per_thread))
+
+    def autotune(self, candidates=(2, 4, 8), gather_candidates=((4, 1), (8, 1), (4, 2), (8, 2)),
+                 reps: int = 3) -> dict:
+        """Time the forward for each forward tile (receivers per work item)
+        and the adjoint for each gather shape (receivers in registers, image
+        points per thread) on this batch, keep the fastest of each and
+        return the timings ({R: ms} for the forward, {"gather rc x ppt": ms}
+        for the adjoint).  Every choice gives the same result."""
         import torch
 
         m = torch.randn(self.shape[1], device="cuda")
@@ -115,6 +125,21 @@ class KirchhoffBatch(LinearOperator):
             times[R] = e0.elapsed_time(e1) / reps
         best = min(times, key=times.get)
         self.set_tile(best)
+        gtimes = {}
+        for rc, ppt in gather_candidates:
+            self.set_gather(rc, ppt)
+            _native.check(L.kgb_batch_adjoint(self._h, d.data_ptr(), m.data_ptr(), stream.cuda_stream))
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                _native.check(L.kgb_batch_adjoint(self._h, d.data_ptr(), m.data_ptr(), stream.cuda_stream))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            gtimes[(rc, ppt)] = e0.elapsed_time(e1) / reps
+        gbest = min(gtimes, key=gtimes.get)
+        self.set_gather(*gbest)
+        times.update({f"gather {rc}x{ppt}": t for (rc, ppt), t in gtimes.items()})
         return times
 
     # ------------------------------------------------------------ solver

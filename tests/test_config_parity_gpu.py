@@ -17,8 +17,9 @@ unknowns, 500 traces, strongly ill-conditioned) the iterates agree to 1e-4
 over the first 8 iterations; from there LSQR reaches the small singular
 values, where the float32 operator's rounding (1e-7 per application) is
 amplified: measured 4e-4 at iteration 8 and 6e-3 at iteration 9, so the
-last two are held to 2e-2 and the residual history to 1e-3.  The
-30-iteration history of the 300 x 800 problem is held to 1e-3.
+last two are held to 2e-2.  The residual history agrees to 1e-7 over
+iterations 0-8 (held to 1e-5) and then by 1e-4 and 1e-2 (held to 2e-2).
+The 30-iteration history of the 300 x 800 problem is held to 1e-3.
 """
 
 import numpy as np
@@ -74,7 +75,8 @@ def test_config1_lsqr_tracks_oracle_iterates():
     assert len(its) == len(ref[10]) == 10
     for k in range(10):
         assert rel(its[k], ref[10][k]) < (1e-4 if k < 8 else 2e-2), (k, rel(its[k], ref[10][k]))
-    np.testing.assert_allclose(out[-1], ref[9], rtol=1e-3)
+    np.testing.assert_allclose(out[-1][:9], ref[9][:9], rtol=1e-5)
+    np.testing.assert_allclose(out[-1][9:], ref[9][9:], rtol=2e-2)
     # the graph path (one launch for the 10 iterations) gives the same iterate
     g = lsqr(K, d.astype(np.float32), niter=10)
     assert np.array_equal(g[0], out[0])
