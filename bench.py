@@ -436,6 +436,9 @@ def run_gpu(args):
         "kernels_ms": {k: round(v, 4) for k, v in kern.items()},
         "spread_variant_ms": {str(k): round(v, 3) for k, v in variant_ms.items()},
         "spread_variant": best,
+        "spread_accumulation": {"split": bool(K.info()["spread_split"]), "max_bin_count": K.info()["max_bin_count"],
+                                "note": "split: two fire-and-forget 32-bit shared atomics per contribution, "
+                                        "exact while no bin receives more than 65535 contributions"},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": hbm,
                      "unit": "GB/s", "frac": round(achieved / hbm, 5) if hbm else None,
                      "traffic": _traffic(top, WORKLOAD), "peak_source": "measured" if hbm else "fallback",

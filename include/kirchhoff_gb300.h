@@ -285,8 +285,9 @@ int kgb_batch_destroy(kgb_batch* batch);
 int kgb_batch_sizes(const kgb_batch* batch, int64_t* sizes4); /* {P, model, data, tile} */
 int kgb_batch_set_tile(kgb_batch* batch, int receivers_per_item); /* 1, 2, 4 or 8 (autotuner) */
 /* Shape of the batched adjoint (autotuner): receiver traveltimes held in
- * registers per image point (4 or 8) and image points per thread (1 or 2);
- * the result is the same for every shape (fixed summation order per point).
+ * registers per image point (4 or 8) and image points per thread (1 or 2).
+ * Each point's sum has a fixed order; points per thread leave it unchanged,
+ * the receiver count groups it (results agree to float32 rounding).
  * No reference counterpart. */
 int kgb_batch_set_gather(kgb_batch* batch, int receivers_in_registers, int points_per_thread);
 int kgb_batch_forward(kgb_batch* batch, const float* m_dev, float* d_dev, void* stream);

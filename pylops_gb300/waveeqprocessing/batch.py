@@ -104,7 +104,9 @@ class KirchhoffBatch(LinearOperator):
         and the adjoint for each gather shape (receivers in registers, image
         points per thread) on this batch, keep the fastest of each and
         return the timings ({R: ms} for the forward, {"gather rc x ppt": ms}
-        for the adjoint).  Every choice gives the same result."""
+        for the adjoint).  Every choice is deterministic; the forward tile and
+        the receivers held in registers group the sums differently, so the
+        results agree to float32 rounding."""
         import torch
 
         m = torch.randn(self.shape[1], device="cuda")

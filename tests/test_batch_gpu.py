@@ -90,18 +90,23 @@ def test_batch_autotune_picks_a_valid_tile():
     assert B.tile in (2, 4, 8) and B.tile == min(times, key=times.get)
 
 
-def test_batch_gather_shapes_agree_bitwise():
-    """Every adjoint shape of the autotuner (receivers in registers 4 or 8,
-    image points per thread 1 or 2) sums each point over the traces in the
-    same order: identical images; the autotuner keeps one of them."""
+def test_batch_gather_shapes_agree():
+    """Adjoint shapes of the autotuner: image points per thread (1 or 2) do
+    not change any per-point sum, so they agree bit for bit; receivers in
+    registers (4 or 8) group each point's sum over receivers differently, so
+    those agree to float32 rounding (1e-6 relative).  The autotuner keeps
+    one of them."""
+    from tests.helpers import rel
+
     _, B = _batch(5, seed=13)
     d = np.random.default_rng(3).standard_normal(B.shape[0]).astype(np.float32)
-    outs = []
+    outs = {}
     for rc, ppt in ((4, 1), (8, 1), (4, 2), (8, 2)):
         B.set_gather(rc, ppt)
-        outs.append(B.H @ d)
-    assert all(np.array_equal(outs[0], o) for o in outs[1:])
+        outs[(rc, ppt)] = B.H @ d
+    assert np.array_equal(outs[(4, 1)], outs[(4, 2)]) and np.array_equal(outs[(8, 1)], outs[(8, 2)])
+    assert rel(outs[(4, 1)], outs[(8, 1)]) < 1e-6
     times = B.autotune(reps=1)
-    assert B.gather_shape in ((4, 1), (8, 1), (4, 2), (8, 2))
+    assert B.gather_shape in outs
     assert any(k.startswith("gather") for k in map(str, times))
-    assert np.array_equal(B.H @ d, outs[0])
+    assert np.array_equal(B.H @ d, outs[B.gather_shape])
