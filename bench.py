@@ -293,6 +293,21 @@ def run_gpu(args):
         variant_ms[v] = e0.elapsed_time(e1) / 2
     best = min(variant_ms, key=variant_ms.get)
     K.set_spread_variant(best)
+    # adjoint variants (same image bit for bit); the fastest is used
+    adjoint_ms = {}
+    for v in ((0, 1, 2) if args.adjoint_variant < 0 else (args.adjoint_variant,)):
+        K.set_adjoint_variant(v)
+        step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(2):
+            _native.check(L.kgb_kirchhoff_gather(h, dcorr.data_ptr(), img.data_ptr(), sp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        adjoint_ms[v] = e0.elapsed_time(e1) / 2
+    best_adj = min(adjoint_ms, key=adjoint_ms.get)
+    K.set_adjoint_variant(best_adj)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -436,6 +451,8 @@ def run_gpu(args):
         "kernels_ms": {k: round(v, 4) for k, v in kern.items()},
         "spread_variant_ms": {str(k): round(v, 3) for k, v in variant_ms.items()},
         "spread_variant": best,
+        "adjoint_variant_ms": {str(k): round(v, 3) for k, v in adjoint_ms.items()},
+        "adjoint_variant": best_adj,
         "spread_accumulation": {"split": bool(K.info()["spread_split"]), "max_bin_count": K.info()["max_bin_count"],
                                 "note": "split: two fire-and-forget 32-bit shared atomics per contribution, "
                                         "exact while no bin receives more than 65535 contributions"},
@@ -1120,7 +1137,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (end-to-end) loop")
     ap.add_argument("--sources", type=int, default=0, help="use this many of the 64 sources (small ncu cases)")
-    ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2)")
+    ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2, 3)")
+    ap.add_argument("--adjoint-variant", type=int, default=-1, help="force the adjoint kernel variant (0, 1, 2)")
     ap.add_argument("--workload", default="kirchhoff2d",
                     choices=["kirchhoff2d", "batch", "lsm", "single", "unet", "nsconv", "kirchhoff3d"],
                     help="kirchhoff2d: the headline fwd+adj workload; batch: 256 batched LSM problems; "

@@ -194,21 +194,23 @@ int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x_dev, float* y_dev, i
  * used by the tile autotuner. */
 int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant);
 
-/* Adjoint of dynamic operators: 1 stages the source records through shared
- * memory with TMA bulk-tensor copies, 0 (the default; faster on the
- * workloads measured) loads them from global memory in the gather itself.
- * Both give the same image bit for bit.
- * No reference counterpart (the reference's adjoint kernels,
- * _kirchhoff_cuda.py:194-298, read their tables directly). */
-int kgb_kirchhoff_set_adjoint_staging(kgb_kirchhoff* op, int on);
+/* Adjoint kernel of dynamic operators: 0 (the default) loads each source
+ * record in the gather; 1 keeps the next active source's record in flight
+ * while the current one's data are read (operators with at most 64 sources);
+ * 2 stages the source records through shared memory with TMA bulk-tensor
+ * copies.  All three give the same image bit for bit (Kirchhoff.autotune
+ * keeps the fastest).  No reference counterpart (the reference's adjoint
+ * kernels, _kirchhoff_cuda.py:194-298, read their tables directly). */
+int kgb_kirchhoff_set_adjoint_variant(kgb_kirchhoff* op, int variant);
 
 /* Introspection used by the host wrapper and the tests.  info16 receives
  * {ns, nr, nt, ni, fixed-point fraction bits, padded wavelet length,
  *  offset-aperture gate active, dynamic, all times non-negative,
  *  adjoint receiver splits, kernels per forward, kernels per adjoint,
  *  spread variant, split accumulation used by the forward (0/1), most
- *  contributions any forward bin can receive, staged adjoint (bit 0: the
- *  source records arrive by TMA) | error word of the bounded waits << 1}. */
+ *  contributions any forward bin can receive, adjoint variant in use (0-2,
+ *  see kgb_kirchhoff_set_adjoint_variant) | error word of the bounded
+ *  waits << 2}. */
 int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* info16);
 
 /* Deterministic float64 reductions of float32 vectors (fixed launch shape

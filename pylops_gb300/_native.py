@@ -62,7 +62,7 @@ _SIGNATURES = {
     "kgb_kirchhoff_wavelet": ([c_vp, c_vp, c_vp, c_int, c_vp], c_int),
     "kgb_kirchhoff_info": ([c_vp, c_i64p], c_int),
     "kgb_kirchhoff_set_variant": ([c_vp, c_int], c_int),
-    "kgb_kirchhoff_set_adjoint_staging": ([c_vp, c_int], c_int),
+    "kgb_kirchhoff_set_adjoint_variant": ([c_vp, c_int], c_int),
     "kgb_dot_f64": ([c_vp, c_vp, c_i64, c_vp, c_vp], c_int),
     "kgb_solver_create": ([ctypes.POINTER(c_vp), c_vp, c_int], c_int),
     "kgb_solver_destroy": ([c_vp], c_int),

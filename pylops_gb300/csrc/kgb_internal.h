@@ -89,6 +89,10 @@ struct KirchDev {
     // passed to the kernel by value; null: the gather loads records itself
     const CUtensorMap* rec_map;
     unsigned* err;  // device word: nonzero after a bounded wait of a kernel gave up
+    // adjoint kernel of dynamic operators: 0 loads each source record in the
+    // gather, 1 keeps the next active source's record in flight (at most 64
+    // sources), 2 stages the records by TMA (rec_map); all give the same image
+    int adjoint_variant;
 };
 
 // u32 words of the forward's fixed-point scale block: [0] bits of max |mv|,
@@ -211,7 +215,7 @@ struct kgb_kirchhoff {
     unsigned max_bin_count = 0;          // its last result
     CUtensorMap stab_map, stab2_map;     // TMA maps over stab / stab2 (see KirchDev::rec_map)
     bool stab_map_ok = false, stab2_map_ok = false;
-    bool adjoint_staging = false;        // use the TMA-staged adjoint where a record map exists (off: slower)
+    int adjoint_variant = 0;             // see KirchDev::adjoint_variant
     // tables built on the device (kgb_kirchhoff_build_tables): [n][ni]
     // float64 rows kept for kgb_kirchhoff_get_table
     double* trav64_s = nullptr;
@@ -251,8 +255,9 @@ struct kgb_kirchhoff {
         K.stab2 = bf16_weights ? stab2 : nullptr; K.rtab2 = bf16_weights ? rtab2 : nullptr;
         K.g0 = 0; K.g1 = 1 << 30; K.prepass = 1;
         K.split_ok = split_ok ? 1 : 0; K.wacc = wacc; K.count_out = count_buf;
-        K.rec_map = !adjoint_staging ? nullptr
+        K.rec_map = adjoint_variant != 2 ? nullptr
                     : bf16_weights ? (stab2_map_ok ? &stab2_map : nullptr) : (stab_map_ok ? &stab_map : nullptr);
+        K.adjoint_variant = adjoint_variant;
         K.err = err;
         return K;
     }

@@ -622,10 +622,10 @@ int kgb_kirchhoff_set_variant(kgb_kirchhoff* op, int spread_variant) {
     return KGB_OK;
 }
 
-int kgb_kirchhoff_set_adjoint_staging(kgb_kirchhoff* op, int on) {
+int kgb_kirchhoff_set_adjoint_variant(kgb_kirchhoff* op, int variant) {
     if (!op) return set_error(KGB_ERR_STATE, "null operator");
-    if (on != 0 && on != 1) return set_error(KGB_ERR_VALUE, "adjoint staging: 0 or 1");
-    op->adjoint_staging = on == 1;
+    if (variant < 0 || variant > 2) return set_error(KGB_ERR_VALUE, "adjoint variant: 0, 1 or 2");
+    op->adjoint_variant = variant;
     return KGB_OK;
 }
 
@@ -647,7 +647,9 @@ int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
     unsigned err = 0u;
     if (op->err && cudaMemcpy(&err, op->err, sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess)
         return set_error(KGB_ERR_CUDA, "info: reading the error word failed");
-    s[15] = ((op->dynamic && op->view().rec_map) ? 1 : 0) | ((int64_t)err << 1);
+    const kgb::KirchDev K = op->view();
+    const int used = !op->dynamic ? 0 : K.rec_map ? 2 : (K.adjoint_variant == 1 && K.ns <= 64 && K.srng) ? 1 : 0;
+    s[15] = used | ((int64_t)err << 2);
     return KGB_OK;
 }
 

@@ -457,6 +457,91 @@ gather_tma_kernel(const __grid_constant__ CUtensorMap smap, const KirchDev K, co
     if (live) out[(size_t)blockIdx.y * K.ni + ii] = total * __ldg(K.vscale + ii);
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint with the next source record in flight (dynamic tables, at most 64
+// sources).  Same sums in the same order as gather_kernel -- receiver chunks
+// in order, within a chunk the sources with a nonzero weight at the point in
+// increasing order -- so the image is the same bit for bit.  The active
+// sources are walked through the point's bit mask, and the record of the
+// next active source is loaded before the current one's data are read: the
+// record load of step k+1 overlaps the data loads of step k instead of
+// preceding them in one dependent chain.  Three more registers per thread
+// cost resident warps (kGatherPfBlocks CTAs per SM).
+// ---------------------------------------------------------------------------
+constexpr int kGatherPfBlocks = 6;
+
+template <bool GATE, bool NONNEG, bool HALF>
+__global__ void __launch_bounds__(kGatherThreads, kGatherPfBlocks)
+gather_pf_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __restrict__ d2,
+                 float* __restrict__ out, int r_per_split) {
+    const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned live = __ballot_sync(0xffffffffu, ii < K.ni);
+    if (ii >= K.ni) return;
+    const int r_begin = blockIdx.y * r_per_split;
+    const int r_end = min(K.nr, r_begin + r_per_split);
+    const int col = (int)(ii / K.nz);
+    const int iz = (int)(ii - (int64_t)col * K.nz);
+    const int ncol = (int)(K.ni / K.nz);
+    const int nt = K.nt;
+    unsigned long long smask = 0ull;
+    for (int is = 0; is < K.ns; ++is)
+        if (in_range(K.srng, (size_t)is * ncol + col, iz)) smask |= 1ull << is;
+    float total = 0.f;
+    for (int r0 = r_begin; r0 < r_end; r0 += kGatherRC) {
+        if (8 % kGatherRC == 0 && K.grng &&
+            !__any_sync(live, in_range(K.grng, (size_t)(r0 >> 3) * ncol + col, iz)))
+            continue;
+        Entry re[kGatherRC];
+        const int nrc = min(kGatherRC, r_end - r0);
+#pragma unroll
+        for (int r = 0; r < kGatherRC; ++r) {
+            re[r] = zero_entry();
+            if (r < nrc) re[r] = load_entry<true, true, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2);
+        }
+        float chunk = 0.f;
+        unsigned long long rem = smask;
+        int cur = -1;
+        Entry se = zero_entry();
+        if (rem) {
+            cur = __ffsll((long long)rem) - 1;
+            rem &= rem - 1ull;
+            se = load_entry<true, false, HALF>(K.tsq, K.stab, (size_t)cur * K.ni + ii, K.stab2);
+        }
+        while (cur >= 0) {
+            int nxt = -1;
+            Entry sn = zero_entry();
+            if (rem) {  // the next active source's record, in flight while this one is used
+                nxt = __ffsll((long long)rem) - 1;
+                rem &= rem - 1ull;
+                sn = load_entry<true, false, HALF>(K.tsq, K.stab, (size_t)nxt * K.ni + ii, K.stab2);
+            }
+            if (se.c != 0.f || se.s != 0.f) {
+                const size_t pair0 = (size_t)cur * K.nr + r0;
+                const float2* __restrict__ drow = d2 + pair0 * nt;
+#pragma unroll
+                for (int r = 0; r < kGatherRC; ++r) {
+                    if (r < nrc) {
+                        const int s = se.t + re[r].t;
+                        float wt = fmaf(se.c, re[r].c, se.s * re[r].s);
+                        if (GATE && iz < __ldg(K.izmin + pair0 + r)) wt = 0.f;
+                        if (fp.valid(s) && wt != 0.f) {
+                            const int it = fp.index(s);
+                            const float w = fp.frac(s, it);
+                            const float2 dd = __ldg(drow + ((size_t)r * nt + it));
+                            const float val = fmaf(w, dd.y - dd.x, dd.x);
+                            chunk = fmaf(val, wt, chunk);
+                        }
+                    }
+                }
+            }
+            cur = nxt;
+            se = sn;
+        }
+        total += chunk;
+    }
+    out[(size_t)blockIdx.y * K.ni + ii] = total * __ldg(K.vscale + ii);
+}
+
 // Fixed-order sum of the per-split partial images.
 __global__ void sum_partials_kernel(const float* __restrict__ partial, float* __restrict__ img,
                                     int64_t ni, int nsplit) {
@@ -1044,13 +1129,32 @@ bool gather_staged(const KirchDev& K) {
     return DYN && K.rec_map != nullptr && K.err != nullptr;
 }
 
+template <bool GATE, bool NONNEG, bool HALF>
+int gather_pf_blocks_per_sm() {
+    static int cached = 0;
+    if (!cached) {
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, gather_pf_kernel<GATE, NONNEG, HALF>, kGatherThreads, 0);
+        cached = nb > 0 ? nb : 1;
+    }
+    return cached;
+}
+
+// the adjoint with the next record in flight applies: dynamic tables, at most 64 sources
+template <bool DYN>
+bool gather_prefetch(const KirchDev& K) {
+    return DYN && K.adjoint_variant == 1 && K.ns <= 64 && K.srng != nullptr;
+}
+
 template <bool DYN, bool GATE, bool NONNEG, bool HALF = false>
 int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* partial, int64_t cap,
                     cudaStream_t stream) {
     const FixedPoint<NONNEG> fp = make_fp<NONNEG>(K.frac_bits, K.nt);
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
     const bool staged = gather_staged<DYN>(K);
+    const bool pf = !staged && gather_prefetch<DYN>(K);
     const int capacity = num_sms() * (staged ? gather_tma_blocks_per_sm<GATE, NONNEG, HALF>()
+                                      : pf   ? gather_pf_blocks_per_sm<GATE, NONNEG, HALF>()
                                              : gather_blocks_per_sm<DYN, GATE, NONNEG, HALF>());
     int split = choose_split(blocks, capacity, K.nr);
     if (partial == nullptr || cap < (int64_t)split * K.ni) split = 1;
@@ -1062,6 +1166,8 @@ int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* part
     if (staged)
         gather_tma_kernel<GATE, NONNEG, HALF>
             <<<grid, kGatherThreads, 0, stream>>>(*K.rec_map, K, fp, d2, out, c_per * kGatherRC, K.err);
+    else if (pf)
+        gather_pf_kernel<GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
     else
         gather_kernel<DYN, GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
     KGB_CUDA_TRY(cudaGetLastError());
@@ -1725,7 +1831,14 @@ int launch_spread_count(const KirchDev& K, bool dynamic, bool gate, int L, unsig
 int gather_nsplit(const KirchDev& K, bool dynamic, bool gate) {
     const int64_t blocks = (K.ni + kGatherThreads - 1) / kGatherThreads;
     int bps;
-    if (dynamic && gather_staged<true>(K)) {
+    if (dynamic && !gather_staged<true>(K) && gather_prefetch<true>(K)) {
+        if (K.stab2)
+            bps = gate ? (K.nonneg ? gather_pf_blocks_per_sm<true, true, true>() : gather_pf_blocks_per_sm<true, false, true>())
+                       : (K.nonneg ? gather_pf_blocks_per_sm<false, true, true>() : gather_pf_blocks_per_sm<false, false, true>());
+        else
+            bps = gate ? (K.nonneg ? gather_pf_blocks_per_sm<true, true, false>() : gather_pf_blocks_per_sm<true, false, false>())
+                       : (K.nonneg ? gather_pf_blocks_per_sm<false, true, false>() : gather_pf_blocks_per_sm<false, false, false>());
+    } else if (dynamic && gather_staged<true>(K)) {
         if (K.stab2)
             bps = gate ? (K.nonneg ? gather_tma_blocks_per_sm<true, true, true>() : gather_tma_blocks_per_sm<true, false, true>())
                        : (K.nonneg ? gather_tma_blocks_per_sm<false, true, true>() : gather_tma_blocks_per_sm<false, false, true>());

@@ -386,8 +386,8 @@ class Kirchhoff(LinearOperator):
                 "adjoint_splits", "kernels_forward", "kernels_adjoint", "spread_variant", "spread_split",
                 "max_bin_count")
         out = {k: int(v[i]) for i, k in enumerate(keys)}
-        out["adjoint_staged"] = int(v[15]) & 1  # source records staged by TMA
-        out["wait_error"] = int(v[15]) >> 1     # nonzero: a bounded wait of a kernel gave up
+        out["adjoint_variant"] = int(v[15]) & 3  # adjoint kernel in use (set_adjoint_variant)
+        out["wait_error"] = int(v[15]) >> 2      # nonzero: a bounded wait of a kernel gave up
         return out
 
     def set_spread_variant(self, variant: int) -> None:
@@ -395,12 +395,12 @@ class Kirchhoff(LinearOperator):
         (one trace per warp), 2 warp-binned (two traces per warp)."""
         _native.check(_native.lib().kgb_kirchhoff_set_variant(self._h, int(variant)))
 
-    def set_adjoint_staging(self, on: bool = True) -> None:
-        """Dynamic operators: stage the source records of the adjoint through
-        shared memory with TMA copies, or let the gather load them itself
-        (the default, faster on the workloads measured); the image is the
-        same bit for bit."""
-        _native.check(_native.lib().kgb_kirchhoff_set_adjoint_staging(self._h, 1 if on else 0))
+    def set_adjoint_variant(self, variant: int) -> None:
+        """Adjoint kernel of dynamic operators: 0 loads each source record in
+        the gather (default), 1 keeps the next active source's record in
+        flight (at most 64 sources), 2 stages the records by TMA; the image is
+        the same bit for bit."""
+        _native.check(_native.lib().kgb_kirchhoff_set_adjoint_variant(self._h, int(variant)))
 
     def set_weight_precision(self, precision: str = "float32") -> None:
         """Store the dynamic weights as ``'bfloat16'`` (8-byte table records,
@@ -412,30 +412,44 @@ class Kirchhoff(LinearOperator):
         self._sync_tables()
         _native.check(_native.lib().kgb_kirchhoff_set_weight_precision(self._h, int(precision == "bfloat16")))
 
-    def autotune(self, variants=(0, 1, 2), reps: int = 3) -> dict:
-        """Time the forward for each spread variant on this operator's
-        tables (random model, CUDA events on the current stream), keep the
-        fastest and return {variant: ms}.  All variants give the same result
-        to float32 rounding; which is fastest depends on the geometry (how
-        many image points each trace collects and how they bin in time)."""
+    def autotune(self, variants=(0, 1, 2, 3), adjoint_variants=(0, 1, 2), reps: int = 3) -> dict:
+        """Time the forward for each spread variant and, for dynamic
+        operators, the adjoint for each adjoint variant on this operator's
+        tables (random vectors, CUDA events on the current stream), keep the
+        fastest of each and return {variant: ms} ({"adjoint v": ms} for the
+        adjoint).  The spread variants give the same result to float32
+        rounding (0 and 3 bit for bit), the adjoint variants bit for bit;
+        which is fastest depends on the geometry."""
         import torch
 
         self._sync_tables()
-        m = torch.randn(self.ni, device="cuda", generator=torch.Generator(device="cuda").manual_seed(0))
+        g = torch.Generator(device="cuda").manual_seed(0)
+        m = torch.randn(self.ni, device="cuda", generator=g)
         d = torch.empty(self.shape[0], device="cuda")
-        times = {}
-        for v in variants:
-            self.set_spread_variant(v)
-            self.apply_into(m, d)
+
+        def timed(fn):
+            fn()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             for _ in range(reps):
-                self.apply_into(m, d)
+                fn()
             e1.record()
             e1.synchronize()
-            times[v] = e0.elapsed_time(e1) / reps
-        best = min(times, key=times.get)
-        self.set_spread_variant(best)
+            return e0.elapsed_time(e1) / reps
+
+        times = {}
+        for v in variants:
+            self.set_spread_variant(v)
+            times[v] = timed(lambda: self.apply_into(m, d))
+        self.set_spread_variant(min(times, key=times.get))
+        if self.dynamic and adjoint_variants:
+            dd = torch.randn(self.shape[0], device="cuda", generator=g)
+            adj = {}
+            for v in adjoint_variants:
+                self.set_adjoint_variant(v)
+                adj[v] = timed(lambda: self.apply_into(dd, m, adjoint=True))
+            self.set_adjoint_variant(min(adj, key=adj.get))
+            times.update({f"adjoint {v}": t for v, t in adj.items()})
         return times
 
     @property

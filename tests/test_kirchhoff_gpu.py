@@ -352,12 +352,13 @@ def test_split_accumulation_equals_carry_accumulation_bitwise(dynamic):
 
 @pytest.mark.parametrize("case", ["k2d_dyn_ap", "k2d_dyn_noap", "k3d_dyn", "k2d_dyn_byot", "grid_60", "grid_ap"])
 @pytest.mark.parametrize("bf16", [False, True])
-def test_staged_adjoint_equals_direct_adjoint_bitwise(case, bf16):
-    """The adjoint with the source records staged by TMA bulk-tensor copies
-    runs the same per-point sums in the same order as the gather that loads
-    them itself: identical images, on golden operators (offset and angle
-    apertures, 3-D, user tables, tails of partial CTAs) and the 100 x 200
-    grid, float32 and bf16 weights; no bounded wait gives up."""
+def test_adjoint_variants_equal_bitwise(case, bf16):
+    """The three adjoint kernels -- records loaded in the gather (0), the next
+    active source's record in flight (1), records staged by TMA bulk-tensor
+    copies (2) -- run the same per-point sums in the same order: identical
+    images, on golden operators (offset and angle apertures, 3-D, user
+    tables, tails of partial CTAs) and the 100 x 200 grid, float32 and bf16
+    weights; no bounded wait gives up."""
     import torch
 
     from pylops_gb300.waveeqprocessing import Kirchhoff
@@ -372,13 +373,12 @@ def test_staged_adjoint_equals_direct_adjoint_bitwise(case, bf16):
         K = _op(load(case))
     if bf16:
         K.set_weight_precision("bfloat16")
-    assert K.info()["adjoint_staged"] == 0  # the default
+    assert K.info()["adjoint_variant"] == 0  # the default
     d = torch.as_tensor(np.random.default_rng(4).standard_normal(K.shape[0]).astype(np.float32), device="cuda")
-    c_ = (K.H @ d).cpu().numpy()
-    K.set_adjoint_staging(True)
-    assert K.info()["adjoint_staged"] == 1
-    a = (K.H @ d).cpu().numpy()
-    b = (K.H @ d).cpu().numpy()
-    K.set_adjoint_staging(False)
-    assert np.array_equal(a, b) and np.array_equal(a, c_)
+    out = []
+    for v in (0, 1, 2, 0):
+        K.set_adjoint_variant(v)
+        assert K.info()["adjoint_variant"] == v
+        out.append((K.H @ d).cpu().numpy())
+    assert all(np.array_equal(out[0], a) for a in out[1:])
     assert K.info()["wait_error"] == 0
