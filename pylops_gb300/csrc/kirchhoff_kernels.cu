@@ -659,15 +659,14 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
     auto point_t = [&](auto full, auto wide, int64_t ii, int64_t colp, int izp, float v) {
         constexpr bool FULL = decltype(full)::value;
         constexpr bool WIDE = decltype(wide)::value;
-        // the source record and all R receiver records in flight together
-        // (one load latency per point, not two in a row)
         const Entry se = load_entry<DYN, false, HALF>(K.tsq, K.stab, (size_t)is * K.ni + ii, K.stab2);
+        if (DYN && se.c == 0.f && se.s == 0.f) return;  // source outside the angle aperture
+        // all R receiver records in flight before any is used
         Entry re[R];
 #pragma unroll
         for (int r = 0; r < R; ++r)
             re[r] = (FULL || r < nrr) ? load_entry<DYN, false, HALF>(K.trq, K.rtab, (size_t)(r0 + r) * K.ni + ii, K.rtab2)
                                       : zero_entry();
-        if (DYN && se.c == 0.f && se.s == 0.f) return;  // source outside the angle aperture
         if (WIDE && ACC == kAccSplit && !wide_any) wide_any = 1;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -734,13 +733,10 @@ spread_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __restrict__
             const uint32_t b = __ldg(K.grng + (size_t)g * ncol + c);
             const int lo = max((int)(a & 0xffffu), (int)(b & 0xffffu));
             const int hi = min((int)(a >> 16), (int)(b >> 16));
-            // the next point's model value is loaded while this one is used
-            float v = lo + lane < hi ? model(c * K.nz + lo + lane) : 0.f;
             for (int iz = lo + lane; iz < hi; iz += 32) {
                 const int64_t ii = c * K.nz + iz;
-                const float vn = iz + 32 < hi ? model(ii + 32) : 0.f;
+                const float v = model(ii);
                 if (v != 0.f) point(ii, c, iz, v);
-                v = vn;
             }
         }
     } else {
