@@ -254,6 +254,10 @@ struct kgb_kirchhoff {
     cudaStream_t stream2 = nullptr;
     cudaStream_t cstream = nullptr;
     cudaEvent_t ev[kHostChunks + 1] = {};
+    // device adjoint: a second stream and fork/join events, created with the
+    // operator (so that the first call may come inside a stream capture)
+    cudaStream_t astream = nullptr;
+    cudaEvent_t aev[2] = {};
     int device = 0;
 
     kgb::KirchDev view() const {
