@@ -93,10 +93,6 @@ struct KirchDev {
     // gather, 1 keeps the next active source's record in flight (at most 64
     // sources), 2 stages the records by TMA (rec_map); all give the same image
     int adjoint_variant;
-    // adjoint: receiver splits [split_lo, split_hi) of the gather only, into
-    // the partial images, without the final sum (split_hi < 0: all, summed);
-    // split0: the first split of a launch (set by the launcher)
-    int split_lo, split_hi, split0;
 };
 
 // u32 words of the forward's fixed-point scale block: [0] bits of max |mv|,
@@ -118,15 +114,6 @@ int prepare_kernels(const KirchDev& K, int L);
 // Wavelet filter along time.  interleave = 0 writes y[tr][n]; interleave = 1
 // writes the pair (o[n], o[n+1]) at y[tr][2n] (o[nt] = 0), the layout the
 // gather reads with one 8-byte load.  g == nullptr copies (no filter).
-// The same for receivers [r0, r1) of every one of ns sources (traces
-// s * nr + r of x and y).
-int launch_wavelet_block(const float* x, float* y, int ns, int nr, int r0, int r1, int nt, const float* g, int L,
-                         int interleave, cudaStream_t stream);
-// Fixed-order sum of nsplit partial images.
-int launch_sum_partials(const float* partial, float* img, int64_t ni, int nsplit, cudaStream_t stream);
-// Receiver splits of the gather for this operator (as launch_gather makes
-// them) and the receivers per split.
-int gather_split_receivers(const KirchDev& K, bool dynamic, bool gate, int* r_per_split);
 int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L,
                    int interleave, cudaStream_t stream);
 // Build the dynamic-mode records and the active depth ranges from the
@@ -254,10 +241,6 @@ struct kgb_kirchhoff {
     cudaStream_t stream2 = nullptr;
     cudaStream_t cstream = nullptr;
     cudaEvent_t ev[kHostChunks + 1] = {};
-    // device adjoint: a second stream and fork/join events, created with the
-    // operator (so that the first call may come inside a stream capture)
-    cudaStream_t astream = nullptr;
-    cudaEvent_t aev[2] = {};
     int device = 0;
 
     kgb::KirchDev view() const {
@@ -275,7 +258,6 @@ struct kgb_kirchhoff {
         K.rec_map = adjoint_variant != 2 ? nullptr
                     : bf16_weights ? (stab2_map_ok ? &stab2_map : nullptr) : (stab_map_ok ? &stab_map : nullptr);
         K.adjoint_variant = adjoint_variant;
-        K.split_lo = 0; K.split_hi = -1; K.split0 = 0;
         K.err = err;
         return K;
     }

@@ -212,10 +212,6 @@ int kgb_kirchhoff_create(kgb_kirchhoff** out, int ns, int nr, int nt, int64_t ni
         if ((rc = static_scratch_prepare())) break;
         e = cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) { rc = cuda_error(e, "create stream"); break; }
-        e = cudaStreamCreateWithFlags(&op->astream, cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&op->aev[0], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&op->aev[1], cudaEventDisableTiming);
-        if (e != cudaSuccess) { rc = cuda_error(e, "create adjoint stream"); break; }
     } while (0);
     if (rc != KGB_OK) {
         kgb_kirchhoff_destroy(op);
@@ -240,9 +236,6 @@ int kgb_kirchhoff_destroy(kgb_kirchhoff* op) {
     if (op->stream) cudaStreamDestroy(op->stream);
     if (op->stream2) cudaStreamDestroy(op->stream2);
     if (op->cstream) cudaStreamDestroy(op->cstream);
-    if (op->astream) cudaStreamDestroy(op->astream);
-    for (cudaEvent_t e : op->aev)
-        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : op->ev)
         if (e) cudaEventDestroy(e);
     cudaSetDevice(dev);
@@ -510,44 +503,13 @@ int kgb_kirchhoff_gather(kgb_kirchhoff* op, const float* d, float* m, void* stre
     return launch_gather(op->view(), op->dynamic, op->has_gate, op->dcorr, m, op->partial, op->partial_elems, s);
 }
 
-// Adjoint.  When the gather runs in receiver splits (partial images summed
-// at the end), the correlation and the gather go block by block of those
-// splits' receivers, alternating between the caller's stream and the
-// operator's second stream (forked and joined with events, which a stream
-// capture records as graph edges), so that one block's correlation
-// overlaps another's gather; the partial images are summed in their fixed
-// order, so the image is the same bit for bit.
 int kgb_kirchhoff_adjoint(kgb_kirchhoff* op, const float* d, float* m, void* stream) {
     int rc = check_ready(op);
     if (rc) return rc;
     if (!m || !d) return set_error(KGB_ERR_VALUE, "adjoint: null pointer");
     cudaStream_t s = (cudaStream_t)stream;
-    kgb::KirchDev K = op->view();
-    int rps = 0;
-    const int nsplit = op->tq1 ? 1 : gather_split_receivers(K, op->dynamic, op->has_gate, &rps);
-    if (nsplit >= 2 && op->partial_elems >= (int64_t)nsplit * op->ni && op->astream) {
-        KGB_CUDA_TRY(cudaEventRecord(op->aev[0], s));
-        KGB_CUDA_TRY(cudaStreamWaitEvent(op->astream, op->aev[0], 0));
-        const int nblk = std::min(kgb_kirchhoff::kHostChunks, nsplit);
-        for (int b = 0; b < nblk; ++b) {
-            const int lo = (int)((int64_t)b * nsplit / nblk), hi = (int)((int64_t)(b + 1) * nsplit / nblk);
-            const int r0 = lo * rps, r1 = std::min(op->nr, hi * rps);
-            if (r1 <= r0) continue;
-            cudaStream_t sc = (b & 1) ? op->astream : s;
-            if ((rc = launch_wavelet_block(d, op->dcorr, op->ns, op->nr, r0, r1, op->nt, op->hflip_dev, op->L, 1, sc)))
-                return rc;
-            kgb::KirchDev Kb = K;
-            Kb.split_lo = lo;
-            Kb.split_hi = hi;
-            if ((rc = launch_gather(Kb, op->dynamic, op->has_gate, op->dcorr, m, op->partial, op->partial_elems, sc)))
-                return rc;
-        }
-        KGB_CUDA_TRY(cudaEventRecord(op->aev[1], op->astream));
-        KGB_CUDA_TRY(cudaStreamWaitEvent(s, op->aev[1], 0));
-        return launch_sum_partials(op->partial, m, op->ni, nsplit, s);
-    }
     if ((rc = launch_wavelet(d, op->dcorr, op->npair(), op->nt, op->hflip_dev, op->L, 1, s))) return rc;
-    return launch_gather(K, op->dynamic, op->has_gate, op->dcorr, m, op->partial, op->partial_elems, s);
+    return launch_gather(op->view(), op->dynamic, op->has_gate, op->dcorr, m, op->partial, op->partial_elems, s);
 }
 
 int kgb_kirchhoff_wavelet(kgb_kirchhoff* op, const float* x, float* y, int adjoint, void* stream) {
@@ -677,11 +639,7 @@ int kgb_kirchhoff_info(const kgb_kirchhoff* op, int64_t* s) {
     // kernels per application: forward = prepass + scale choice + spread;
     // adjoint = correlation + gather (+ partial-image sum when split)
     s[10] = 3;
-    // adjoint: correlation + gather, or, with receiver splits and partial
-    // images, a correlation and a gather per block of splits plus the sum
-    s[11] = (s[9] > 1 && op->partial_elems >= s[9] * op->ni && op->astream)
-                ? 2 * std::min<int64_t>(kgb_kirchhoff::kHostChunks, s[9]) + 1
-                : 2 + (s[9] > 1 ? 1 : 0);
+    s[11] = 2 + (s[9] > 1 ? 1 : 0);
     s[12] = op->spread_variant;
     s[13] = op->split_ok ? 1 : 0;
     s[14] = op->max_bin_count;

@@ -160,7 +160,7 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
     // which are re-streamed per receiver chunk anyway, so splitting adds no
     // table traffic
     const int s_begin = 0, s_end = K.ns;
-    const int r_begin = (K.split0 + (int)blockIdx.y) * r_per_split;
+    const int r_begin = blockIdx.y * r_per_split;
     const int r_end = min(K.nr, r_begin + r_per_split);
     int col = 0, iz = 0;  // depth column and depth (column counts fit in int)
     if (DYN || GATE) {
@@ -224,7 +224,7 @@ gather_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __res
         total += chunk;
     }
     if (DYN) total *= __ldg(K.vscale + ii);
-    out[(size_t)(K.split0 + blockIdx.y) * K.ni + ii] = total;
+    out[(size_t)blockIdx.y * K.ni + ii] = total;
 }
 
 // ---------------------------------------------------------------------------
@@ -300,7 +300,7 @@ gather_tma_kernel(const __grid_constant__ CUtensorMap smap, const KirchDev K, co
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t ii = (int64_t)blockIdx.x * kGatherThreads + tid;
     const bool live = ii < K.ni;
-    const int r_begin = (K.split0 + (int)blockIdx.y) * r_per_split;
+    const int r_begin = blockIdx.y * r_per_split;
     const int r_end = min(K.nr, r_begin + r_per_split);
     const int64_t ncol = K.ni / K.nz;
     int col = 0, iz = 0;
@@ -454,7 +454,7 @@ gather_tma_kernel(const __grid_constant__ CUtensorMap smap, const KirchDev K, co
     }
     if (failed) return;
     if (wact) total += chunk;
-    if (live) out[(size_t)(K.split0 + blockIdx.y) * K.ni + ii] = total * __ldg(K.vscale + ii);
+    if (live) out[(size_t)blockIdx.y * K.ni + ii] = total * __ldg(K.vscale + ii);
 }
 
 // ---------------------------------------------------------------------------
@@ -477,7 +477,7 @@ gather_pf_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __
     const int64_t ii = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned live = __ballot_sync(0xffffffffu, ii < K.ni);
     if (ii >= K.ni) return;
-    const int r_begin = (K.split0 + (int)blockIdx.y) * r_per_split;
+    const int r_begin = blockIdx.y * r_per_split;
     const int r_end = min(K.nr, r_begin + r_per_split);
     const int col = (int)(ii / K.nz);
     const int iz = (int)(ii - (int64_t)col * K.nz);
@@ -539,7 +539,7 @@ gather_pf_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, const float2* __
         }
         total += chunk;
     }
-    out[(size_t)(K.split0 + blockIdx.y) * K.ni + ii] = total * __ldg(K.vscale + ii);
+    out[(size_t)blockIdx.y * K.ni + ii] = total * __ldg(K.vscale + ii);
 }
 
 // Fixed-order sum of the per-split partial images.
@@ -987,7 +987,7 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, int nt,
-               const float* __restrict__ g, int L, int interleave, int64_t nb, int64_t nrow, int64_t r0) {
+               const float* __restrict__ g, int L, int interleave) {
     extern __shared__ __align__(16) float smem[];
     const int Lp = fir_lpad(L);
     const int span = fir_span(L, nt);
@@ -999,10 +999,7 @@ wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, 
         for (int k = threadIdx.x; k < Lp; k += blockDim.x) gs[k] = k < L ? g[k] : 0.f;
         for (int i = threadIdx.x; i < span; i += blockDim.x) xp[i] = 0.f;
     }
-    for (int64_t t = blockIdx.x; t < ntr; t += gridDim.x) {
-        // trace t of the launch is trace (t / nb) * nrow + r0 + t % nb of the
-        // arrays (a block of receivers of every source; nb = ntr: trace t)
-        const int64_t tr = (t / nb) * nrow + r0 + t % nb;
+    for (int64_t tr = blockIdx.x; tr < ntr; tr += gridDim.x) {
         __syncthreads();
         const float* xrow = x + tr * nt;
         float* dst = g ? xp + q : os;
@@ -1164,26 +1161,17 @@ int gather_launch_t(const KirchDev& K, const float2* d2, float* img, float* part
     const int nchunks = (K.nr + kGatherRC - 1) / kGatherRC;
     const int c_per = (nchunks + split - 1) / split;
     split = (nchunks + c_per - 1) / c_per;
-    KirchDev Ks = K;
-    int s_lo = 0, s_hi = split;
-    if (K.split_hi >= 0) {  // only splits [split_lo, split_hi), into the partial images; no sum
-        if (split < 2 || partial == nullptr) return set_error(KGB_ERR_STATE, "gather: no receiver splits to launch");
-        s_lo = std::max(0, K.split_lo);
-        s_hi = std::min(split, K.split_hi);
-        if (s_hi <= s_lo) return KGB_OK;
-        Ks.split0 = s_lo;
-    }
-    float* out = (split > 1 || K.split_hi >= 0) ? partial : img;
-    dim3 grid((unsigned)blocks, (unsigned)(s_hi - s_lo));
+    float* out = split > 1 ? partial : img;
+    dim3 grid((unsigned)blocks, (unsigned)split);
     if (staged)
         gather_tma_kernel<GATE, NONNEG, HALF>
-            <<<grid, kGatherThreads, 0, stream>>>(*K.rec_map, Ks, fp, d2, out, c_per * kGatherRC, K.err);
+            <<<grid, kGatherThreads, 0, stream>>>(*K.rec_map, K, fp, d2, out, c_per * kGatherRC, K.err);
     else if (pf)
-        gather_pf_kernel<GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(Ks, fp, d2, out, c_per * kGatherRC);
+        gather_pf_kernel<GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
     else
-        gather_kernel<DYN, GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(Ks, fp, d2, out, c_per * kGatherRC);
+        gather_kernel<DYN, GATE, NONNEG, HALF><<<grid, kGatherThreads, 0, stream>>>(K, fp, d2, out, c_per * kGatherRC);
     KGB_CUDA_TRY(cudaGetLastError());
-    if (split > 1 && K.split_hi < 0) {
+    if (split > 1) {
         const int nb = (int)std::min<int64_t>((K.ni + 255) / 256, 4 * num_sms());
         sum_partials_kernel<<<nb, 256, 0, stream>>>(partial, img, K.ni, split);
         KGB_CUDA_TRY(cudaGetLastError());
@@ -1947,35 +1935,6 @@ int prepare_kernels(const KirchDev& K0, int L) {
     return KGB_OK;
 }
 
-int launch_wavelet_block(const float* x, float* y, int ns, int nr, int r0, int r1, int nt, const float* g, int L,
-                         int interleave, cudaStream_t stream) {
-    const int64_t nb = r1 - r0, ntr = (int64_t)ns * nb;
-    if (ntr <= 0 || nt <= 0) return KGB_OK;
-    const size_t smem = wavelet_smem(L, nt);
-    if (smem > 227 * 1024)
-        return set_error(KGB_ERR_NOT_IMPLEMENTED, "wavelet: nt=%d too long for shared memory", nt);
-    const int threads = wavelet_threads(g, nt);
-    const int64_t blocks = std::min<int64_t>(ntr, (int64_t)wavelet_blocks_per_sm(threads, smem) * num_sms());
-    wavelet_kernel<<<(unsigned)blocks, threads, smem, stream>>>(x, y, ntr, nt, g, L, interleave, nb, nr, r0);
-    KGB_CUDA_TRY(cudaGetLastError());
-    return KGB_OK;
-}
-
-int launch_sum_partials(const float* partial, float* img, int64_t ni, int nsplit, cudaStream_t stream) {
-    const int nb = (int)std::min<int64_t>((ni + 255) / 256, 4 * num_sms());
-    sum_partials_kernel<<<nb, 256, 0, stream>>>(partial, img, ni, nsplit);
-    KGB_CUDA_TRY(cudaGetLastError());
-    return KGB_OK;
-}
-
-int gather_split_receivers(const KirchDev& K, bool dynamic, bool gate, int* r_per_split) {
-    const int split = gather_nsplit(K, dynamic, gate);
-    const int nchunks = (K.nr + kGatherRC - 1) / kGatherRC;
-    const int c_per = (nchunks + split - 1) / split;
-    *r_per_split = c_per * kGatherRC;
-    return split;
-}
-
 int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g, int L, int interleave,
                    cudaStream_t stream) {
     if (ntr <= 0 || nt <= 0) return KGB_OK;
@@ -1986,7 +1945,7 @@ int launch_wavelet(const float* x, float* y, int64_t ntr, int nt, const float* g
     // blocks: as many as stay resident (one wave of the grid-stride loop)
     const int threads = wavelet_threads(g, nt);
     const int64_t blocks = std::min<int64_t>(ntr, (int64_t)wavelet_blocks_per_sm(threads, smem) * num_sms());
-    wavelet_kernel<<<(unsigned)blocks, threads, smem, stream>>>(x, y, ntr, nt, g, L, interleave, ntr, ntr, 0);
+    wavelet_kernel<<<(unsigned)blocks, threads, smem, stream>>>(x, y, ntr, nt, g, L, interleave);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
