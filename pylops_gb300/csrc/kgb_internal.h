@@ -154,8 +154,15 @@ struct TableGeom {
 };
 int launch_analytic_rows(const TableGeom& g, const double* yax, const double* xax, const double* zax,
                          const double* pts, int np, double vel, double* trav, double* dist, cudaStream_t s);
-int launch_eikonal_rows(const TableGeom& g, const double* speed, const int* pts, int np, double* out, unsigned* err,
-                        cudaStream_t s);
+// 2-D eikonal traveltime rows of ns sources and nr receivers (pts: grid
+// coordinates (ix, iz) of the sources, then of the receivers) into trav_s
+// and trav_r, in one launch with the unit-speed table of a point at the
+// grid's corner into `corner` (ni values); rhs: ni floats of scratch.
+int launch_eikonal_tables(const TableGeom& g, const double* speed, float* rhs, const int* pts, int ns, int nr,
+                          double* trav_s, double* trav_r, double* corner, unsigned* err, cudaStream_t s);
+// Distance (unit-speed eikonal) rows of the same points from the corner table.
+int launch_distance_rows(const TableGeom& g, const double* corner, const int* pts, int ns, int nr, double* dist_s,
+                         double* dist_r, cudaStream_t s);
 int launch_angle_rows(const TableGeom& g, const double* trav, const double* sign_rows, int np, double* ang,
                       cudaStream_t s);
 int launch_fold_rows(int ndim, double maxdist, double amin, double amax, const double* taper21,

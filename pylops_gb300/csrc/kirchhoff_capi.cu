@@ -740,23 +740,24 @@ int kgb_kirchhoff_build_tables(kgb_kirchhoff* op, int mode, int ndim, const doub
             return rc;
     } else {
         // grid coordinates of the points: round((p - origin) / spacing) (kirchhoff.py:615, 627)
-        std::vector<int> is_(2 * (size_t)ns), ir_(2 * (size_t)nr);
-        auto coords = [&](const double* pts, int np, std::vector<int>& out) {
+        // sources, then receivers
+        std::vector<int> pts(2 * ((size_t)ns + nr));
+        auto coords = [&](const double* p, int np, int* out) {
             for (int k = 0; k < np; ++k) {
-                const double cx = nearbyint((pts[k] - xax[0]) / g.hx);
-                const double cz = nearbyint((pts[np + k] - zax[0]) / g.hz);
+                const double cx = nearbyint((p[k] - xax[0]) / g.hx);
+                const double cz = nearbyint((p[np + k] - zax[0]) / g.hz);
                 if (!(cx >= 0 && cx < nx && cz >= 0 && cz < nz)) return false;
                 out[2 * k] = (int)cx;
                 out[2 * k + 1] = (int)cz;
             }
             return true;
         };
-        if (!coords(srcs, ns, is_) || !coords(recs, nr, ir_))
+        if (!coords(srcs, ns, pts.data()) || !coords(recs, nr, pts.data() + 2 * (size_t)ns))
             return set_error(KGB_ERR_VALUE, "build_tables: a source or receiver lies outside the grid");
-        DevBuf<int> ds, dr;
-        DevBuf<double> sp;
-        if ((rc = upload(ds, is_.data(), is_.size(), "upload source points"))) return rc;
-        if ((rc = upload(dr, ir_.data(), ir_.size(), "upload receiver points"))) return rc;
+        DevBuf<int> dp;
+        DevBuf<double> sp, corner;
+        DevBuf<float> rhs;
+        if ((rc = upload(dp, pts.data(), pts.size(), "upload table points"))) return rc;
         std::vector<double> vfull;
         const double* vp = vel;
         if (nvel == 1) {
@@ -764,11 +765,13 @@ int kgb_kirchhoff_build_tables(kgb_kirchhoff* op, int mode, int ndim, const doub
             vp = vfull.data();
         }
         if ((rc = upload(sp, vp, (size_t)ni, "upload velocity"))) return rc;
+        if ((rc = dev_alloc(&rhs.p, (size_t)ni, "alloc eikonal right-hand side"))) return rc;
+        if ((rc = dev_alloc(&corner.p, (size_t)ni, "alloc corner distance table"))) return rc;
         KGB_CUDA_TRY(cudaMemset(op->err, 0, sizeof(unsigned)));
-        if ((rc = launch_eikonal_rows(g, sp.p, ds.p, ns, op->trav64_s, op->err, nullptr))) return rc;
-        if ((rc = launch_eikonal_rows(g, sp.p, dr.p, nr, op->trav64_r, op->err, nullptr))) return rc;
-        if ((rc = launch_eikonal_rows(g, nullptr, ds.p, ns, op->dist64_s, op->err, nullptr))) return rc;
-        if ((rc = launch_eikonal_rows(g, nullptr, dr.p, nr, op->dist64_r, op->err, nullptr))) return rc;
+        if ((rc = launch_eikonal_tables(g, sp.p, rhs.p, dp.p, ns, nr, op->trav64_s, op->trav64_r, corner.p, op->err,
+                                        nullptr)))
+            return rc;
+        if ((rc = launch_distance_rows(g, corner.p, dp.p, ns, nr, op->dist64_s, op->dist64_r, nullptr))) return rc;
         unsigned err = 0;
         KGB_CUDA_TRY(cudaMemcpy(&err, op->err, sizeof(unsigned), cudaMemcpyDeviceToHost));
         if (err) return set_error(KGB_ERR_CUDA, "build_tables: the eikonal sweeps did not converge");

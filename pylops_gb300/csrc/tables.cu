@@ -13,7 +13,8 @@
 //    Gauss-Seidel sweeps in the four diagonal orders until no value
 //    changes: one CTA per table, anti-diagonals of the sweep in parallel
 //    (their points do not neighbour one another), the same upwind
-//    second-order local solver;
+//    second-order local solver; distances (unit speed) from one table of a
+//    point at the grid's corner, shifted to each point;
 //  * gradients: numpy.gradient with the sample spacing (central differences
 //    inside, one-sided at the ends, kirchhoff.py:642-648);
 //  * angles with the vertical: atan2(dT/dx, dT/dz) in 2-D;
@@ -64,120 +65,127 @@ __global__ void analytic_kernel(const double* __restrict__ yax, const double* __
 // ---------------------------------------------------------------------------
 // 2-D eikonal by diagonal Gauss-Seidel sweeps
 // ---------------------------------------------------------------------------
-// larger root of sum_i c[i] (T - b[i])^2 = rhs if it is not below any b[i]
-__device__ __forceinline__ bool ek_root(int m, const double* c, const double* b, double rhs, double* T) {
-    double A = 0.0, B = 0.0, C = -rhs, bmax = -INFINITY;
-    for (int i = 0; i < m; ++i) {
-        A += c[i];
-        B += -2.0 * c[i] * b[i];
-        C += c[i] * b[i] * b[i];
-        bmax = fmax(bmax, b[i]);
-    }
-    const double disc = B * B - 4.0 * A * C;
-    if (disc < 0.0) return false;
-    const double t = (-B + sqrt(disc)) / (2.0 * A);
-    if (t < bmax) return false;
-    *T = t;
-    return true;
+// Times are non-negative doubles or +inf, whose order is the order of their
+// bit patterns as signed 64-bit integers: the comparisons run on the integer
+// pipe (the float64 pipe of this GPU runs at 1/64 of the float32 rate).
+__device__ __forceinline__ bool t_less(double a, double b) {
+    return __double_as_longlong(a) < __double_as_longlong(b);
 }
+__device__ __forceinline__ bool t_finite(double a) { return __double_as_longlong(a) < 0x7ff0000000000000LL; }
 
-// The host solver's local update (eikonal.cpp, update()) on a set of m
-// axes: second order on every axis that has it, else first order dropping
-// the latest axes.  `drop2` first retries second order on the earliest axis
-// alone: in a marching order that axis would have been the only one known.
-__device__ double ek_solve(int m, const double* a2o, const double* b2o, const double* a1, const double* b1,
-                           double slow2, bool drop2) {
-    double t;
-    if (ek_root(m, a2o, b2o, slow2, &t)) return t;
-    const int o0 = (m == 2 && b1[1] < b1[0]) ? 1 : 0, o1 = 1 - o0;
-    if (m == 2 && drop2) {
-        const double aa[1] = {a2o[o0]}, bb[1] = {b2o[o0]};
-        if (ek_root(1, aa, bb, slow2, &t)) return t;
+// Upwind neighbours of node k along one axis (coordinate c of n, stride st):
+// the smaller finite neighbour `best`, and `second`, the node beyond it on
+// the same side, when that is finite and not larger (the second-order
+// stencil of the host solver, eikonal.cpp).  The negative side is taken
+// first; the positive side replaces it only when strictly smaller.
+__device__ __forceinline__ void ek_axis(const double* T, int64_t k, int c, int n, int64_t st, double* best,
+                                        double* second, bool* have2) {
+    const double vm1 = c >= 1 ? T[k - st] : INFINITY;
+    const double vp1 = c + 1 < n ? T[k + st] : INFINITY;
+    const double vm2 = c >= 2 ? T[k - 2 * st] : INFINITY;
+    const double vp2 = c + 2 < n ? T[k + 2 * st] : INFINITY;
+    *best = INFINITY;
+    *have2 = false;
+    if (t_finite(vm1)) {
+        *best = vm1;
+        if (t_finite(vm2) && !t_less(vm1, vm2)) {
+            *have2 = true;
+            *second = vm2;
+        }
     }
-    if (m == 2) {
-        const double aa[2] = {a1[o0], a1[o1]}, bb[2] = {b1[o0], b1[o1]};
-        if (ek_root(2, aa, bb, slow2, &t)) return t;
+    if (t_finite(vp1) && t_less(vp1, *best)) {
+        *best = vp1;
+        *have2 = false;
+        if (t_finite(vp2) && !t_less(vp1, vp2)) {
+            *have2 = true;
+            *second = vp2;
+        }
     }
-    {
-        const double aa[1] = {a1[o0]}, bb[1] = {b1[o0]};
-        if (ek_root(1, aa, bb, slow2, &t)) return t;
-    }
-    return b1[o0] + sqrt(slow2 / a1[o0]);
 }
 
 // Tentative time of node (i0, i1) from its finite neighbours, reproducing
 // what fast marching computes for it: marching accepts nodes in increasing
 // time, so a node's neighbours become known in increasing order and its
 // value is the smaller of the update with the earliest axis alone and the
-// update with both axes (each with the host solver's stencil rules).  With
-// every finite neighbour taken as known, this keeps a later (larger)
-// neighbour from turning a valid second-order solve into a first-order
-// one.  +inf when no neighbour is finite.
-__device__ double ek_update(const double* T, int n0, int n1, double h0, double h1, int i0, int i1,
-                            double slow2) {
+// update with both axes (second order on every axis whose stencil allows
+// it; the two-axis root counts when it is not below either axis' value).
+// With every finite neighbour taken as known, this keeps a later (larger)
+// neighbour from turning a valid second-order solve into a first-order one.
+// +inf when no neighbour is finite.
+//
+// Each axis contributes c (T - b)^2 with c = 1/h^2, b = t1, or, second
+// order, c = 9/(4 h^2), b = (4 t1 - t2)/3.  The equation is solved for
+// d = T - r, r the smaller axis value, in float: d and the b - r are of
+// the size of one cell's traveltime, whatever the time itself, so float
+// keeps T to ~5e-8 of its size (measured against the same update in
+// float64 on the 800 x 300 workload: 4.9e-8 of the largest time), and the
+// float64 pipe only forms the differences b - r and the final r + d.
+// Single axis: the larger root of c (d - b)^2 = rhs, b + sqrt(rhs/c).
+// Two axes: A d^2 - 2 B d + C = 0 with A = c0 + c1, B = c0 b0 + c1 b1,
+// C = c0 b0^2 + c1 b1^2 - rhs.
+__device__ double ek_update(const double* T, int n0, int n1, float ih0, float ih1, int i0, int i1, float rhs) {
     const int64_t k = (int64_t)i0 * n1 + i1;
-    double a2o[2], b2o[2], a1[2], b1[2];
-    int m = 0;
-    for (int a = 0; a < 2; ++a) {
-        const int c = a == 0 ? i0 : i1;
-        const int n = a == 0 ? n0 : n1;
-        const int64_t st = a == 0 ? n1 : 1;
-        const double h = a == 0 ? h0 : h1;
-        double best = INFINITY, second = INFINITY;
-        bool have2 = false;
-        for (int dir = -1; dir <= 1; dir += 2) {
-            const int c1 = c + dir;
-            if (c1 < 0 || c1 >= n) continue;
-            const double v1 = T[k + dir * st];
-            if (!(v1 < INFINITY)) continue;
-            if (v1 < best) {
-                best = v1;
-                have2 = false;
-                const int c2 = c + 2 * dir;
-                if (c2 >= 0 && c2 < n) {
-                    const double v2 = T[k + 2 * dir * st];
-                    if (v2 < INFINITY && v2 <= v1) {
-                        have2 = true;
-                        second = v2;
-                    }
-                }
-            }
-        }
-        if (best < INFINITY) {
-            a1[m] = 1.0 / (h * h);
-            b1[m] = best;
-            if (have2) {
-                a2o[m] = 9.0 / (4.0 * h * h);
-                b2o[m] = (4.0 * best - second) / 3.0;
-            } else {
-                a2o[m] = a1[m];
-                b2o[m] = best;
-            }
-            ++m;
+    double bx, sx = 0.0, bz, sz = 0.0;
+    bool hx, hz;
+    ek_axis(T, k, i0, n0, n1, &bx, &sx, &hx);
+    ek_axis(T, k, i1, n1, 1, &bz, &sz, &hz);
+    const bool fx = t_finite(bx), fz = t_finite(bz);
+    if (!fx && !fz) return INFINITY;
+    // axis "e" (earliest: the smaller value; axis 0 on ties) and axis "l"
+    const bool zfirst = fz && (!fx || t_less(bz, bx));
+    const double r = zfirst ? bz : bx;
+    const double se = zfirst ? sz : sx;
+    const bool he = zfirst ? hz : hx;
+    const float ihe = zfirst ? ih1 : ih0;
+    const float ce = he ? 2.25f * ihe : ihe;
+    const float be = he ? (float)(r - se) * (1.f / 3.f) : 0.f;
+    float d = be + sqrtf(rhs / ce);  // earliest axis alone
+    if (fx && fz) {
+        const double bl = zfirst ? bx : bz, sl = zfirst ? sx : sz;
+        const bool hl = zfirst ? hx : hz;
+        const float ihl = zfirst ? ih0 : ih1;
+        const float dl = (float)(bl - r);
+        const float cl = hl ? 2.25f * ihl : ihl;
+        const float b2 = hl ? (4.f * dl - (float)(sl - r)) * (1.f / 3.f) : dl;
+        const float A = ce + cl;
+        const float B = ce * be + cl * b2;
+        const float C = ce * be * be + cl * b2 * b2 - rhs;
+        const float disc = B * B - A * C;
+        if (disc >= 0.f) {
+            const float t = (B + sqrtf(disc)) / A;
+            if (t >= fmaxf(be, b2) && t < d) d = t;
         }
     }
-    if (m == 0) return INFINITY;
-    const double both = ek_solve(m, a2o, b2o, a1, b1, slow2, true);
-    if (m == 1) return both;
-    const int o = b1[1] < b1[0] ? 1 : 0;
-    const double one = ek_solve(1, a2o + o, b2o + o, a1 + o, b1 + o, slow2, false);
-    return one < both ? one : both;
+    return r + (double)d;
 }
 
 constexpr int kEikThreads = 320;
 constexpr int kEikMaxSets = 64;  // sweep sets before giving up (each set is 4 sweeps)
 
-// One CTA per table: blockIdx.x = point (traveltimes with `speed`, or
-// distances with speed 1 when speed == nullptr).
-__global__ void __launch_bounds__(kEikThreads)
+// rhs of the eikonal equation, 1/speed^2, rounded once to float
+__global__ void ek_rhs_kernel(const double* __restrict__ speed, int64_t n, float* __restrict__ rhs) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = speed[i];
+        rhs[i] = (float)(1.0 / (v * v));
+    }
+}
+
+// One CTA per table.  CTAs [0, ns) solve the traveltimes of the sources,
+// [ns, ns + nr) those of the receivers (grid points pts[2b], pts[2b + 1]),
+// and CTA ns + nr the unit-speed table of a point at the grid's corner.
+__global__ void __launch_bounds__(kEikThreads, 4)
 eikonal_sweep_kernel(int n0, int n1, double h0, double h1, const double* __restrict__ speed,
-                     const int* __restrict__ pts, int np, double* out, unsigned* __restrict__ err) {
-    const int p = blockIdx.x;
-    double* T = out + (size_t)p * n0 * n1;  // read and written by all threads between barriers
-    const int s0 = pts[2 * p], s1 = pts[2 * p + 1];
+                     const float* __restrict__ rhs, const int* __restrict__ pts, int ns, int nr, double* trav_s,
+                     double* trav_r, double* corner, unsigned* __restrict__ err) {
+    const int b = blockIdx.x;
+    const bool unit = b >= ns + nr;
+    double* T = unit ? corner : b < ns ? trav_s + (size_t)b * n0 * n1 : trav_r + (size_t)(b - ns) * n0 * n1;
+    // T is read and written by all threads between barriers
+    const int s0 = unit ? 0 : pts[2 * b], s1 = unit ? 0 : pts[2 * b + 1];
     const int64_t N = (int64_t)n0 * n1;
     const double r0 = 0.5 / sqrt(1.0 / (h0 * h0) + 1.0 / (h1 * h1));
-    auto spd = [&](int64_t i) { return speed ? speed[i] : 1.0; };
+    const float ih0 = (float)(1.0 / (h0 * h0)), ih1 = (float)(1.0 / (h1 * h1));
+    auto spd = [&](int64_t i) { return unit ? 1.0 : speed[i]; };
     // the point and its axis neighbours start on the level set (half a cell
     // from the point); they never change
     auto frozen = [&](int i0, int i1) { return abs(i0 - s0) + abs(i1 - s1) <= 1; };
@@ -205,9 +213,8 @@ eikonal_sweep_kernel(int n0, int n1, double h0, double h1, const double* __restr
                     const int i1 = f1 ? u1 : n1 - 1 - u1;
                     if (frozen(i0, i1)) continue;
                     const int64_t k = (int64_t)i0 * n1 + i1;
-                    const double sp = spd(k);
-                    const double t = ek_update(T, n0, n1, h0, h1, i0, i1, 1.0 / (sp * sp));
-                    if (t < T[k]) {
+                    const double t = ek_update(T, n0, n1, ih0, ih1, i0, i1, unit ? 1.f : rhs[k]);
+                    if (t_less(t, T[k])) {
                         T[k] = t;
                         changed = 1;
                     }
@@ -222,6 +229,24 @@ eikonal_sweep_kernel(int n0, int n1, double h0, double h1, const double* __restr
             if (threadIdx.x == 0) atomicExch(err, 3u);
             break;
         }
+    }
+}
+
+// Unit-speed (distance) rows: with unit speed the sweeps' solution depends
+// only on the offset from the point (every update reads the upwind side,
+// which lies between the node and the point, inside the grid), so row p at
+// (i0, i1) is the corner table at (|i0 - p0|, |i1 - p1|).  The same holds
+// for the host fast-marching solver; both were checked bit for bit against
+// per-point solves on the 800 x 300 grid.
+__global__ void distance_rows_kernel(int n0, int n1, const double* __restrict__ corner, const int* __restrict__ pts,
+                                     int ns, double* __restrict__ dist_s, double* __restrict__ dist_r) {
+    const int p = blockIdx.y;
+    const int p0 = pts[2 * p], p1 = pts[2 * p + 1];
+    const int64_t N = (int64_t)n0 * n1;
+    double* out = p < ns ? dist_s + (size_t)p * N : dist_r + (size_t)(p - ns) * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int i0 = (int)(i / n1), i1 = (int)(i - (int64_t)i0 * n1);
+        out[i] = corner[(int64_t)abs(i0 - p0) * n1 + abs(i1 - p1)];
     }
 }
 
@@ -416,10 +441,22 @@ int launch_analytic_rows(const TableGeom& g, const double* yax, const double* xa
     return KGB_OK;
 }
 
-int launch_eikonal_rows(const TableGeom& g, const double* speed, const int* pts, int np, double* out, unsigned* err,
-                        cudaStream_t s) {
+int launch_eikonal_tables(const TableGeom& g, const double* speed, float* rhs, const int* pts, int ns, int nr,
+                          double* trav_s, double* trav_r, double* corner, unsigned* err, cudaStream_t s) {
     if (g.ndim != 2) return set_error(KGB_ERR_NOT_IMPLEMENTED, "device eikonal tables: 2-D only");
-    eikonal_sweep_kernel<<<np, kEikThreads, 0, s>>>(g.nx, g.nz, g.hx, g.hz, speed, pts, np, out, err);
+    ek_rhs_kernel<<<grid_for(g.ni), 256, 0, s>>>(speed, g.ni, rhs);
+    KGB_CUDA_TRY(cudaGetLastError());
+    eikonal_sweep_kernel<<<ns + nr + 1, kEikThreads, 0, s>>>(g.nx, g.nz, g.hx, g.hz, speed, rhs, pts, ns, nr,
+                                                              trav_s, trav_r, corner, err);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int launch_distance_rows(const TableGeom& g, const double* corner, const int* pts, int ns, int nr, double* dist_s,
+                         double* dist_r, cudaStream_t s) {
+    if (g.ndim != 2) return set_error(KGB_ERR_NOT_IMPLEMENTED, "device eikonal tables: 2-D only");
+    dim3 grid((unsigned)std::max(1, grid_for(g.ni) / std::max(1, (ns + nr) / 8 + 1)), (unsigned)(ns + nr));
+    distance_rows_kernel<<<grid, 256, 0, s>>>(g.nx, g.nz, corner, pts, ns, dist_s, dist_r);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
