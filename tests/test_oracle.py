@@ -210,3 +210,24 @@ def test_eikonal_oracle_matches_analytic_and_the_package_solver():
     b = Kirchhoff._traveltime_table(z, x, s3, r3, v3, y=y, mode="eikonal")
     for i in range(4):
         np.testing.assert_allclose(a[i], b[i], rtol=1e-12, atol=0)
+
+
+def test_unit_speed_fast_marching_tables_are_shifts_of_one_corner_table():
+    """The premise of the device distance rows: with unit speed a point's
+    fast-marching table depends only on the offset from the point, so every
+    distance row is the table of a point at the grid's corner read at
+    (|ix - px|, |iz - pz|).  Held bit for bit with the oracle's fast
+    marching (kirchhoff.py:609-638 computes the distances with
+    skfmm.distance) on an anisotropic grid, points on edges, corners and
+    inside."""
+    from oracle.kirch_oracle_c import eikonal_tables
+
+    nx, nz, hx, hz = 37, 23, 5.0, 4.0
+    pts = np.array([[0, 0], [36, 22], [18, 0], [0, 11], [7, 13], [36, 0], [20, 21]], np.int32)
+    _, own = eikonal_tables((nx, nz), (hx, hz), 1.0, pts, with_trav=False)
+    _, corner = eikonal_tables((nx, nz), (hx, hz), 1.0, np.array([[0, 0]], np.int32), with_trav=False)
+    corner = corner[:, 0].reshape(nx, nz)
+    I0, I1 = np.meshgrid(np.arange(nx), np.arange(nz), indexing="ij")
+    for k, (p0, p1) in enumerate(pts):
+        shifted = corner[np.abs(I0 - p0), np.abs(I1 - p1)].ravel()
+        assert np.array_equal(shifted, own[:, k]), (p0, p1)
