@@ -331,6 +331,19 @@ int kgb_gemm_bf16_tn_splitk(const void* A_dev, const void* B_dev, float* C_dev, 
 int kgb_conv3x3_bf16(const void* x_dev, const void* w_dev, void* y_dev, int B, int H, int W, int C, int N, int flip,
                      const float* bias_dev, int flags, int* err_dev, void* stream);
 
+/* Weight gradient of that convolution without an unfolded copy:
+ * dW[n][tap*C + c] = sum_p g[p][n] x[pixel(p) + (ky-1, kx-1)][c] (float32,
+ * row stride ldw >= 9 C), from gTr (bf16, B H x N x W: the output gradient
+ * transposed per image row) and xT3 (bf16, 3 x B H x C x W: the input
+ * transposed per image row, copy kx shifted by kx - 1 columns with zero
+ * fill), both as kgb_unet_row_transpose writes them.  A tensor-core GEMM
+ * with rows (tap, channel), reduction over pixels (64 per step, one image
+ * row segment; the row shift ky is the TMA box's zero fill), split over the
+ * pixels into `work` (at least 9 C x N floats) and summed in slice order
+ * (deterministic).  C % 32 == 0, W % 64 == 0.  No reference counterpart. */
+int kgb_conv3x3_wgrad_bf16(const void* xT3_dev, const void* gTr_dev, float* dW_dev, int B, int H, int W, int C, int N,
+                           int ldw, float* work_dev, int64_t work_elems, int* err_dev, void* stream);
+
 /* ---- U-Net helper kernels (NHWC bf16 activations) ------------------------
  * No reference counterpart (the learned preconditioner is new).  A ks x ks
  * convolution (ks 1 or 3, padding ks/2, stride 1 or 2) with weights
@@ -358,6 +371,11 @@ int kgb_conv3x3_bf16(const void* x_dev, const void* w_dev, void* y_dev, int B, i
  *               x into y, accumulate optional);
  *  to_bf16      y = x * scale[image] (scale may be NULL);
  *  image_rms    scale[b] = 1/rms of image b (B images of n floats; 0 if zero);
+ *  row_transpose  per image row r = b H + h of NHWC src (C, W multiples of
+ *               8): dst[s B H + r][c][w] = src[r][w + s - 1][c], s < 3
+ *               (shifts = 3, zero outside the row), or dst[r][c][w] =
+ *               src[r][w][c] (shifts = 1): the operands of
+ *               kgb_conv3x3_wgrad_bf16;
  *  mse          loss = mean (y - t)^2 (double, device), grad = 2 (y - t)/n
  *               (may be NULL), partials: 304 doubles of scratch;
  *  adam         Adam step `step` (1-based) on float32 weights. */
@@ -376,6 +394,7 @@ int kgb_unet_channels(const void* x, void* y, int64_t P, int C, int Ctot, int co
                       void* stream);
 int kgb_unet_to_bf16(const float* x, void* y, int64_t n, int B, const float* scale, void* stream);
 int kgb_unet_image_rms(const float* x, int64_t n, int B, float* scale, void* stream);
+int kgb_unet_row_transpose(const void* src, void* dst, int B, int H, int W, int C, int shifts, void* stream);
 int kgb_unet_mse(const float* y, const float* t, float* grad, int64_t n, double* partials, double* loss,
                  void* stream);
 int kgb_unet_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,

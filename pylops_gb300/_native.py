@@ -84,6 +84,7 @@ _SIGNATURES = {
     "kgb_gemm_bf16_tn_splitk": ([c_vp, c_vp, c_vp, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_vp, c_i64,
                                  c_vp, c_vp], c_int),
     "kgb_conv3x3_bf16": ([c_vp, c_vp, c_vp] + [c_int] * 6 + [c_vp, c_int, c_vp, c_vp], c_int),
+    "kgb_conv3x3_wgrad_bf16": ([c_vp, c_vp, c_vp] + [c_int] * 6 + [c_vp, c_i64, c_vp, c_vp], c_int),
     "kgb_unet_unfold": ([c_vp, c_vp] + [c_int] * 10 + [c_vp], c_int),
     "kgb_unet_unfold_t": ([c_vp, c_vp] + [c_int] * 6 + [c_vp], c_int),
     "kgb_unet_transpose": ([c_vp, c_vp, c_i64, c_int, c_i64, c_i64, c_int, c_vp], c_int),
@@ -95,6 +96,7 @@ _SIGNATURES = {
     "kgb_unet_channels": ([c_vp, c_vp, c_i64, c_int, c_int, c_int, c_int, c_int, c_vp], c_int),
     "kgb_unet_to_bf16": ([c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),
     "kgb_unet_image_rms": ([c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    "kgb_unet_row_transpose": ([c_vp, c_vp] + [c_int] * 5 + [c_vp], c_int),
     "kgb_unet_mse": ([c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
     "kgb_unet_adam": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_float, c_float, c_float, c_float, c_int, c_vp], c_int),
     "kgb_eikonal_tables": ([c_int, c_ip, c_dp, c_dp, c_int, c_ip, c_dp, c_dp, c_int, c_int], c_int),

@@ -5,19 +5,22 @@
 // the U-Net preconditioner: its convolutions (forward, data gradient, weight
 // gradient) are lowered to it through im2col / transposes.
 //
-// Structure (one 128 x BN output tile per CTA, 4 warps):
+// Structure (persistent: one CTA per SM walking 128 x BN output tiles, 6 warps):
 //  * warp 0, one lane: TMA producer -- 2-D tiled bulk-tensor loads of the A
 //    and B k-tiles (64 bf16 = 128 bytes along K) with 128-byte swizzle into a
-//    STAGES-deep shared-memory ring, completion counted on "full" mbarriers;
-//  * warp 1, one lane: MMA issuer -- four tcgen05.mma (K = 16 each) per
-//    k-tile on shared-memory descriptors, accumulating in tensor memory;
-//    tcgen05.commit releases the stage ("empty" mbarrier) and finally signals
-//    the epilogue;
-//  * warp 2 allocates and frees the tensor-memory accumulator (BN columns);
-//  * all four warps run the epilogue: tcgen05.ld of their 32 accumulator
-//    lanes, bias / ReLU, store.
+//    shared-memory ring of up to 8 stages, completion counted on "full"
+//    mbarriers, running ahead across tile boundaries;
+//  * warp 1: allocates and frees tensor memory (two BN-column accumulators);
+//    one lane issues the MMAs -- four tcgen05.mma (K = 16 each) per k-tile on
+//    shared-memory descriptors; tcgen05.commit releases the stage ("empty"
+//    mbarrier) and, after a tile's last k-tile, hands its accumulator to the
+//    epilogue;
+//  * warps 2-5: epilogue -- tcgen05.ld of their 32 accumulator lanes, bias /
+//    ReLU, store, then hand the accumulator back to the MMA warp, so that one
+//    tile's epilogue overlaps the next tile's MMAs.
 // Every mbarrier wait is bounded: after ~2^26 polls the CTA records an error
-// code in `err` and leaves (tensor memory is still freed).
+// code in `err`, waits (bounded) for its copies and MMAs in flight, frees
+// tensor memory and leaves.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -30,7 +33,6 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BK = 64;          // bf16 elements per k-tile row = 128 bytes (one swizzle atom)
-constexpr int STAGES = 4;
 constexpr uint32_t kSpinLimit = 1u << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -68,6 +70,14 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0, int c1,
+                                            int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
+        ::"r"(dst), "l"(map), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+        : "memory");
+}
+
 // 4-D tiled load (implicit convolution: channels, width, height, image).
 // Coordinates other than the innermost may be negative or past the end: the
 // box is zero-filled there (the convolution's padding).
@@ -83,10 +93,18 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map
 // an M tile of 128 output pixels is a box of bh rows x bw columns of one
 // image; k-tile g is (tap = g / cblk, channel block g % cblk) and reads the
 // input shifted by sgn * (ky - 1, kx - 1) (sgn = -1: the transposed
-// convolution of the data gradient).
+// convolution of the data gradient).  Weight gradient: cblk = channels per
+// tap (rows of A are (tap, channel)), k-tile = 64 pixels of one image row.
 struct ConvGeom {
     int H, W, cblk, sgn;
+    int nimg;  // weight gradient: images per shifted copy
 };
+
+// Operand modes of the GEMM kernel: plain 2-D A; implicit 3x3 convolution
+// (A from shifted 4-D boxes of NHWC activations); weight gradient of a 3x3
+// convolution (A from the column-shifted channel-major copies, see
+// kgb_conv3x3_wgrad_bf16).
+constexpr int kModePlain = 0, kModeConv = 1, kModeWgrad = 2;
 
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle.
 // start address >> 4 in bits [0,14); leading byte offset (unused for
@@ -115,11 +133,27 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-template <int BN, bool CONV>
-__global__ void __launch_bounds__(128, 1)
+// Shared-memory ring depth: as many stages as fit in ~192 KB (one CTA per SM).
+template <int BN>
+__host__ __device__ constexpr int gemm_stages() {
+    return (192 * 1024) / (BM * BK * 2 + BN * BK * 2) < 8 ? (192 * 1024) / (BM * BK * 2 + BN * BK * 2) : 8;
+}
+
+constexpr int kGemmThreads = 192;  // warp 0 producer, warp 1 MMA, warps 2-5 epilogue
+
+// Persistent GEMM: each CTA walks output tiles t = blockIdx.x, + gridDim.x,
+// ... (tile t: n tile t % tiles_n, m tile (t / tiles_n) % tiles_m, k split
+// t / (tiles_n tiles_m)), so the tiles that run together share their A rows
+// in L2.  The producer streams the k-tiles of consecutive tiles through one
+// ring without draining it between tiles; the accumulator is double-buffered
+// in tensor memory (2 x BN columns), so the MMAs of tile j + 1 run while the
+// epilogue warps read tile j.
+template <int BN, int MODE>
+__global__ void __launch_bounds__(kGemmThreads, 1)
 gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, void* __restrict__ C,
                int M, int N, int K, int ldc, const float* __restrict__ bias, int flags, int* __restrict__ err,
-               int kt_per, int64_t split_stride, const ConvGeom cg) {
+               int kt_per, int64_t split_stride, const ConvGeom cg, int tiles_m, int tiles_n, int splits) {
+    constexpr int S = gemm_stages<BN>();
     constexpr int A_BYTES = BM * BK * 2;
     constexpr int B_BYTES = BN * BK * 2;
     extern __shared__ uint8_t smem_dyn[];
@@ -128,35 +162,38 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
     uint8_t* smem = smem_dyn + pad;
     const uint32_t sA = smem_u32(smem);
-    const uint32_t sB = sA + STAGES * A_BYTES;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * (A_BYTES + B_BYTES));
-    // bars[0..S) full, bars[S..2S) empty, bars[2S] done; then the tmem slot and an abort flag
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+    const uint32_t sB = sA + S * A_BYTES;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * (A_BYTES + B_BYTES));
+    // bars: [0, S) full, [S, 2S) empty, then accumulator full x2, accumulator
+    // empty x2, drain; then the tmem slot and an abort flag
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 5);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     const uint32_t bar_full = smem_u32(bars);
-    const uint32_t bar_empty = bar_full + 8 * STAGES;
-    const uint32_t bar_done = bar_full + 16 * STAGES;
+    const uint32_t bar_empty = bar_full + 8 * S;
+    const uint32_t bar_tfull = bar_full + 16 * S;
+    const uint32_t bar_tempty = bar_tfull + 16;
+    const uint32_t bar_drain = bar_tempty + 16;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-    // split-K: this CTA reduces k-tiles [kt0, kt0 + ktiles) into its own
-    // slice of C (the host makes every slice non-empty)
-    const int kt0 = blockIdx.z * kt_per;
-    const int ktiles = min((K + BK - 1) / BK - kt0, kt_per);
-    if (blockIdx.z) C = reinterpret_cast<float*>(C) + blockIdx.z * split_stride;
+    const int ktiles_total = (K + BK - 1) / BK;
+    const int ntiles = tiles_m * tiles_n * splits;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(bar_full + 8 * s, 1);
             mbar_init(bar_empty + 8 * s, 1);
         }
-        mbar_init(bar_done, 1);
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(bar_tfull + 8 * a, 1);
+            mbar_init(bar_tempty + 8 * a, 4);  // one arrival per epilogue warp
+        }
+        mbar_init(bar_drain, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 2) {
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"((uint32_t)BN));
+                     "r"((uint32_t)(2 * BN)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -164,127 +201,209 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0 && lane == 0) {
-        // producer
-        int img = 0, h0 = 0, w0 = 0;
-        if (CONV) {
-            const int hw = cg.H * cg.W;
-            img = m0 / hw;
-            const int r = m0 - img * hw;
-            h0 = r / cg.W;
-            w0 = r - h0 * cg.W;
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: k-tiles of this CTA's tiles in order, `it` counting them
+            uint32_t it = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int tn = t % tiles_n, rest = t / tiles_n;
+                const int m0 = (rest % tiles_m) * BM, n0 = tn * BN, z = rest / tiles_m;
+                const int kt0 = z * kt_per;
+                const int nkt = min(ktiles_total - kt0, kt_per);
+                int img = 0, h0 = 0, w0 = 0;
+                if (MODE == kModeConv) {
+                    const int hw = cg.H * cg.W;
+                    img = m0 / hw;
+                    const int r = m0 - img * hw;
+                    h0 = r / cg.W;
+                    w0 = r - h0 * cg.W;
+                }
+                for (int kt = 0; kt < nkt; ++kt, ++it) {
+                    const int s = (int)(it % S);
+                    if ((it >= (uint32_t)S && !mbar_wait(bar_empty + 8 * s, ((it / S) - 1) & 1)) || *abort_flag) {
+                        ok = false;
+                        break;
+                    }
+                    if (MODE == kModeWgrad) {
+                        // 64 pixels of one image row; A rows m0.. in boxes of
+                        // 32 (tap, channel) rows, each from the copy shifted by
+                        // its kx, at row h + ky - 1 (zero fill outside)
+                        const int p0 = (kt0 + kt) * BK;
+                        const int hw = cg.H * cg.W;
+                        const int b = p0 / hw, r = p0 - b * hw;
+                        const int h = r / cg.W, wp = r - h * cg.W;
+                        const int nbox = min(4, (M - m0) >> 5);
+                        mbar_expect_tx(bar_full + 8 * s, (uint32_t)(nbox * (A_BYTES / 4) + B_BYTES));
+                        for (int i = 0; i < nbox; ++i) {
+                            const int row = m0 + 32 * i;
+                            const int tap = row / cg.cblk, c = row - tap * cg.cblk;
+                            const int ky = tap / 3, kx = tap - ky * 3;
+                            tma_load_4d(sA + s * A_BYTES + i * (A_BYTES / 4), &tmA, bar_full + 8 * s, wp, c, h + ky - 1,
+                                        kx * cg.nimg + b);
+                        }
+                        tma_load_3d(sB + s * B_BYTES, &tmB, bar_full + 8 * s, wp, n0, b * cg.H + h);
+                        continue;
+                    }
+                    mbar_expect_tx(bar_full + 8 * s, A_BYTES + B_BYTES);
+                    if (MODE == kModeConv) {
+                        const int g = kt0 + kt;
+                        const int tap = g / cg.cblk, cb = g - tap * cg.cblk;
+                        const int ky = tap / 3, kx = tap - ky * 3;
+                        tma_load_4d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, cb * BK, w0 + cg.sgn * (kx - 1),
+                                    h0 + cg.sgn * (ky - 1), img);
+                    } else {
+                        tma_load_2d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, (kt0 + kt) * BK, m0);
+                    }
+                    tma_load_2d(sB + s * B_BYTES, &tmB, bar_full + 8 * s, (kt0 + kt) * BK, n0);
+                }
+            }
+            if (!ok) *abort_flag = 1;
+            // the copies issued last (at most S stages) land before the CTA
+            // can leave: wait for their full phases (already complete on the
+            // normal path)
+            for (uint32_t j = it > (uint32_t)S ? it - S : 0u; j < it; ++j)
+                mbar_wait(bar_full + 8 * (j % S), (j / S) & 1);
         }
-        for (int kt = 0; kt < ktiles; ++kt) {
-            const int s = kt % STAGES;
-            if (kt >= STAGES && !mbar_wait(bar_empty + 8 * s, ((kt / STAGES) - 1) & 1)) {
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer
+            constexpr uint32_t idesc = idesc_bf16(BM, BN);
+            uint32_t it = 0;
+            bool ok = true;
+            int j = 0;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++j) {
+                const int a = j & 1, u = j >> 1;
+                // accumulator a is free once the epilogue has read tile j - 2
+                if (j >= 2 && !mbar_wait(bar_tempty + 8 * a, (u - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const int z = (t / tiles_n) / tiles_m;
+                const int nkt = min(ktiles_total - z * kt_per, kt_per);
+                const uint32_t dacc = tmem + (uint32_t)(a * BN);
+                for (int kt = 0; kt < nkt; ++kt, ++it) {
+                    const int s = (int)(it % S);
+                    if (!mbar_wait(bar_full + 8 * s, (it / S) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+                    for (int k = 0; k < BK / 16; ++k) {
+                        const uint64_t da = sw128_desc(sA + s * A_BYTES + k * 32);
+                        const uint64_t db = sw128_desc(sB + s * B_BYTES + k * 32);
+                        const uint32_t acc = (kt > 0 || k > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                            ::"r"(dacc), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                    }
+                    // release the stage when these MMAs have read it
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                                 ::"r"(bar_empty + 8 * s) : "memory");
+                }
+                if (!ok) break;
+                // accumulator a holds tile t when these MMAs complete
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             ::"r"(bar_tfull + 8 * a) : "memory");
+            }
+            if (!ok) *abort_flag = 1;
+            // every MMA issued completes before tensor memory is freed
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(bar_drain) : "memory");
+            mbar_wait(bar_drain, 0);
+        }
+    } else {
+        // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31,
+        // i.e. rows m0 + 32 (w % 4) + lane of each tile
+        const int q = warp & 3;
+        int j = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
+            const int a = j & 1, u = j >> 1;
+            const bool ready = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * a, u & 1));
+            if (!ready || *abort_flag) {
                 *abort_flag = 1;
                 break;
             }
-            mbar_expect_tx(bar_full + 8 * s, A_BYTES + B_BYTES);
-            if (CONV) {
-                const int g = kt0 + kt;
-                const int tap = g / cg.cblk, cb = g - tap * cg.cblk;
-                const int ky = tap / 3, kx = tap - ky * 3;
-                tma_load_4d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, cb * BK, w0 + cg.sgn * (kx - 1),
-                            h0 + cg.sgn * (ky - 1), img);
-            } else {
-                tma_load_2d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, (kt0 + kt) * BK, m0);
-            }
-            tma_load_2d(sB + s * B_BYTES, &tmB, bar_full + 8 * s, (kt0 + kt) * BK, n0);
-        }
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer
-        constexpr uint32_t idesc = idesc_bf16(BM, BN);
-        bool ok = true;
-        for (int kt = 0; kt < ktiles; ++kt) {
-            const int s = kt % STAGES;
-            if (!mbar_wait(bar_full + 8 * s, (kt / STAGES) & 1)) {
-                ok = false;
-                break;
-            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-            for (int k = 0; k < BK / 16; ++k) {
-                const uint64_t da = sw128_desc(sA + s * A_BYTES + k * 32);
-                const uint64_t db = sw128_desc(sB + s * B_BYTES + k * 32);
-                const uint32_t acc = (kt > 0 || k > 0) ? 1u : 0u;
+            const int tn = t % tiles_n, rest = t / tiles_n;
+            const int m0 = (rest % tiles_m) * BM, n0 = tn * BN, z = rest / tiles_m;
+            void* Cz = z ? reinterpret_cast<void*>(reinterpret_cast<float*>(C) + z * split_stride) : C;
+            const int row = m0 + q * 32 + lane;
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t r[32];
+                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN + c0);
                 asm volatile(
-                    "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-                    ::"r"(tmem), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                      "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                      "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (row < M && (flags & 4) && n0 + c0 + 32 <= N) {
+                    // whole 32-column chunk, 16-byte aligned row segment
+                    float v[32];
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) {
+                        v[jj] = __uint_as_float(r[jj]);
+                        if (bias) v[jj] += __ldg(bias + n0 + c0 + jj);
+                        if (flags & 1) v[jj] = fmaxf(v[jj], 0.f);
+                    }
+                    if (flags & 2) {
+                        uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(Cz) + (size_t)row * ldc +
+                                                              n0 + c0);
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq) {
+                            uint4 w4;
+                            w4.x = pack_bf16(v[8 * qq + 0], v[8 * qq + 1]);
+                            w4.y = pack_bf16(v[8 * qq + 2], v[8 * qq + 3]);
+                            w4.z = pack_bf16(v[8 * qq + 4], v[8 * qq + 5]);
+                            w4.w = pack_bf16(v[8 * qq + 6], v[8 * qq + 7]);
+                            dst[qq] = w4;
+                        }
+                    } else {
+                        float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(Cz) + (size_t)row * ldc + n0 +
+                                                                c0);
+#pragma unroll
+                        for (int qq = 0; qq < 8; ++qq)
+                            dst[qq] = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
+                    }
+                } else if (row < M) {
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) {
+                        const int col = n0 + c0 + jj;
+                        if (col < N) {
+                            float v = __uint_as_float(r[jj]);
+                            if (bias) v += __ldg(bias + col);
+                            if (flags & 1) v = fmaxf(v, 0.f);
+                            if (flags & 2)
+                                reinterpret_cast<__nv_bfloat16*>(Cz)[(size_t)row * ldc + col] = __float2bfloat16(v);
+                            else
+                                reinterpret_cast<float*>(Cz)[(size_t)row * ldc + col] = v;
+                        }
+                    }
+                }
             }
-            // release the stage when these MMAs have read it
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                         ::"r"(bar_empty + 8 * s) : "memory");
+            // this warp's lanes of accumulator a are read: hand it back
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_tempty + 8 * a) : "memory");
         }
-        if (!ok) *abort_flag = 1;
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                     ::"r"(bar_done) : "memory");
     }
     __syncwarp();
-    // epilogue: every warp reads its 32 accumulator lanes
-    const bool done = mbar_wait(bar_done, 0);
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool good = done && !*abort_flag;
-    const int row = m0 + warp * 32 + lane;
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t r[32];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-              "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-            : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (good && row < M && (flags & 4) && n0 + c0 + 32 <= N) {
-            // whole 32-column chunk, 16-byte aligned row segment
-            float v[32];
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                v[j] = __uint_as_float(r[j]);
-                if (bias) v[j] += __ldg(bias + n0 + c0 + j);
-                if (flags & 1) v[j] = fmaxf(v[j], 0.f);
-            }
-            if (flags & 2) {
-                uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(C) + (size_t)row * ldc + n0 + c0);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    uint4 u;
-                    u.x = pack_bf16(v[8 * q + 0], v[8 * q + 1]);
-                    u.y = pack_bf16(v[8 * q + 2], v[8 * q + 3]);
-                    u.z = pack_bf16(v[8 * q + 4], v[8 * q + 5]);
-                    u.w = pack_bf16(v[8 * q + 6], v[8 * q + 7]);
-                    dst[q] = u;
-                }
-            } else {
-                float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(C) + (size_t)row * ldc + n0 + c0);
-#pragma unroll
-                for (int q = 0; q < 8; ++q) dst[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-            }
-        } else if (good && row < M) {
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int col = n0 + c0 + j;
-                if (col < N) {
-                    float v = __uint_as_float(r[j]);
-                    if (bias) v += __ldg(bias + col);
-                    if (flags & 1) v = fmaxf(v, 0.f);
-                    if (flags & 2)
-                        reinterpret_cast<__nv_bfloat16*>(C)[(size_t)row * ldc + col] = __float2bfloat16(v);
-                    else
-                        reinterpret_cast<float*>(C)[(size_t)row * ldc + col] = v;
-                }
-            }
-        }
-    }
-    if (!good && threadIdx.x == 0 && err) atomicExch(err, 1);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 2) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN));
+    if (threadIdx.x == 0 && *abort_flag && err) atomicExch(err, 1);
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN)));
+    }
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -336,25 +455,87 @@ int make_map_nhwc(CUtensorMap* map, const void* base, int B, int H, int W, int C
     return KGB_OK;
 }
 
-template <int BN>
-size_t gemm_smem() {
-    return 1024 + (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * STAGES + 1) + 16;
+// Column-shifted row-blocked copies xT3[kx][b][h][c][w] (bf16) as a 4-D
+// tensor {W, C, H, 3B}; box {64 columns, 32 channels, 1, 1} = 32 rows of 128
+// bytes (512-byte apart in memory), a quarter of the 128-row A tile.
+int make_map_wgrad(CUtensorMap* map, const void* base, int B, int H, int W, int C) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_error(KGB_ERR_CUDA, "wgrad: cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[4] = {(cuuint64_t)W, (cuuint64_t)C, (cuuint64_t)H, (cuuint64_t)3 * B};
+    cuuint64_t strides[3] = {(cuuint64_t)W * 2, (cuuint64_t)C * W * 2, (cuuint64_t)H * C * W * 2};
+    cuuint32_t box[4] = {(cuuint32_t)BK, 32, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(KGB_ERR_VALUE, "wgrad: tensor map rejected (CUresult %d)", (int)r);
+    return KGB_OK;
 }
 
-template <int BN, bool CONV = false>
+// Row-blocked output gradient gTr[r][n][w] (bf16, r = b H + h) as a 3-D
+// tensor {W, N, B H}; box {64 columns, box_rows gradients, 1}.
+int make_map_rows(CUtensorMap* map, const void* base, int64_t R, int W, int N, int box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_error(KGB_ERR_CUDA, "wgrad: cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[3] = {(cuuint64_t)W, (cuuint64_t)N, (cuuint64_t)R};
+    cuuint64_t strides[2] = {(cuuint64_t)W * 2, (cuuint64_t)N * W * 2};
+    cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(KGB_ERR_VALUE, "wgrad: tensor map rejected (CUresult %d)", (int)r);
+    return KGB_OK;
+}
+
+// dW[n][q] = sum over z of work[z][q][n], q = tap * C + c < M, in order z = 0, 1, ...
+__global__ void wgrad_sum_kernel(const float* __restrict__ work, float* __restrict__ dW, int M, int N, int splits,
+                                 int ldw) {
+    const int64_t total = (int64_t)M * N, mn = (int64_t)M * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int n = (int)(i / M), q = (int)(i - (int64_t)n * M);
+        float acc = 0.f;
+        for (int z = 0; z < splits; ++z) acc += work[z * mn + (int64_t)q * N + n];
+        dW[(int64_t)n * ldw + q] = acc;
+    }
+}
+
+template <int BN>
+size_t gemm_smem() {
+    return 1024 + (size_t)gemm_stages<BN>() * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * gemm_stages<BN>() + 5) + 16;
+}
+
+int sm_count() {
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 148;
+    if (!sms[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev] = v > 0 ? v : 148;
+    }
+    return sms[dev];
+}
+
+template <int BN, int MODE = kModePlain>
 int gemm_launch(const CUtensorMap& ma, const CUtensorMap& mb, void* C, int M, int N, int K, int ldc, const float* bias,
                 int flags, int* err, int splits, int kt_per, int64_t split_stride, cudaStream_t s,
-                ConvGeom cg = ConvGeom{1, 1, 1, 1}) {
+                ConvGeom cg = ConvGeom{1, 1, 1, 1, 1}) {
     static bool attr = false;
     const size_t smem = gemm_smem<BN>();
     if (!attr) {
-        KGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tn_kernel<BN, CONV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        KGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tn_kernel<BN, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
         attr = true;
     }
-    dim3 grid((unsigned)((M + BM - 1) / BM), (unsigned)((N + BN - 1) / BN), (unsigned)splits);
-    gemm_tn_kernel<BN, CONV><<<grid, 128, smem, s>>>(ma, mb, C, M, N, K, ldc, bias, flags, err, kt_per, split_stride,
-                                                     cg);
+    const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+    const int64_t ntiles = (int64_t)tiles_m * tiles_n * splits;
+    if (ntiles > 0x7fffffff) return set_error(KGB_ERR_VALUE, "gemm: too many tiles");
+    // one persistent CTA per SM (at most one per tile)
+    const int grid = (int)std::min<int64_t>(ntiles, sm_count());
+    gemm_tn_kernel<BN, MODE><<<grid, kGemmThreads, smem, s>>>(ma, mb, C, M, N, K, ldc, bias, flags, err, kt_per,
+                                                              split_stride, cg, tiles_m, tiles_n, splits);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -419,7 +600,7 @@ extern "C" int kgb_gemm_bf16_tn_splitk(const void* A, const void* B, float* C, i
     const int ktiles = (K + BK - 1) / BK;
     const int BN = N <= 64 ? 64 : 128;
     const int64_t tiles = (int64_t)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
-    if (splits <= 0) splits = (int)std::max<int64_t>(1, (2 * 152 + tiles - 1) / tiles);
+    if (splits <= 0) splits = (int)std::max<int64_t>(1, (2 * sm_count() + tiles - 1) / tiles);
     const int64_t mn = (int64_t)M * N;
     if (work && ((uintptr_t)work & 15) == 0) splits = (int)std::min<int64_t>(splits, work_elems / mn);
     else splits = 1;
@@ -430,7 +611,7 @@ extern "C" int kgb_gemm_bf16_tn_splitk(const void* A, const void* B, float* C, i
     cudaStream_t s = (cudaStream_t)stream;
     if (splits == 1) return run_gemm(A, B, C, M, N, K, lda, ldb, ldc, nullptr, 0, err_dev, 1, ktiles, 0, s);
     if ((rc = run_gemm(A, B, work, M, N, K, lda, ldb, N, nullptr, 0, err_dev, splits, kt_per, mn, s))) return rc;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4 * 152));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4 * sm_count()));
     splitk_sum_kernel<<<grid, 256, 0, s>>>(work, C, M, N, ldc, splits);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
@@ -464,10 +645,50 @@ extern "C" int kgb_conv3x3_bf16(const void* x, const void* w, void* y, int B, in
     if ((rc = make_map_nhwc(&ma, x, B, H, W, C, bw, bh))) return rc;
     if ((rc = make_map(&mb, w, N, K, K, BN))) return rc;
     flags = (flags & 3) | vector_flag(y, N, flags);
-    const ConvGeom cg{H, W, cblk, flip ? -1 : 1};
+    const ConvGeom cg{H, W, cblk, flip ? -1 : 1, B};
     cudaStream_t s = (cudaStream_t)stream;
     const int ktiles = K / BK;
     if (BN == 64)
-        return gemm_launch<64, true>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
-    return gemm_launch<128, true>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
+        return gemm_launch<64, kModeConv>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
+    return gemm_launch<128, kModeConv>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
+}
+
+extern "C" int kgb_conv3x3_wgrad_bf16(const void* xT3, const void* gTr, float* dW, int B, int H, int W, int C, int N,
+                                      int ldw, float* work, int64_t work_elems, int* err_dev, void* stream) {
+    if (!xT3 || !gTr || !dW || !work) return set_error(KGB_ERR_VALUE, "wgrad: null pointer");
+    if (B <= 0 || H <= 0 || W <= 0 || C <= 0 || N <= 0) return set_error(KGB_ERR_VALUE, "wgrad: sizes must be positive");
+    if (C % 32) return set_error(KGB_ERR_VALUE, "wgrad: channels must be a multiple of 32");
+    if (W % BK) return set_error(KGB_ERR_VALUE, "wgrad: width %d is not a multiple of %d", W, BK);
+    if (ldw < 9 * C) return set_error(KGB_ERR_VALUE, "wgrad: ldw < 9 C");
+    if ((((uintptr_t)xT3 | (uintptr_t)gTr | (uintptr_t)work) & 15) != 0)
+        return set_error(KGB_ERR_VALUE, "wgrad: operands must be 16-byte aligned");
+    const int64_t P = (int64_t)B * H * W;
+    if (P > 0x7fffffffLL || (int64_t)3 * B > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "wgrad: too many pixels");
+    const int M = 9 * C;
+    const int BN = N <= 64 ? 64 : 128;
+    const int64_t tiles = (int64_t)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int ktiles = (int)(P / BK);
+    const int64_t mn = (int64_t)M * N;
+    if (work_elems < mn) return set_error(KGB_ERR_VALUE, "wgrad: work buffer smaller than 9 C x N");
+    int splits = (int)std::max<int64_t>(1, (2 * sm_count() + tiles - 1) / tiles);
+    splits = (int)std::min<int64_t>(splits, work_elems / mn);
+    splits = std::max(1, std::min(splits, ktiles));
+    const int kt_per = (ktiles + splits - 1) / splits;
+    splits = (ktiles + kt_per - 1) / kt_per;
+    CUtensorMap ma, mb;
+    int rc;
+    if ((rc = make_map_wgrad(&ma, xT3, B, H, W, C))) return rc;
+    if ((rc = make_map_rows(&mb, gTr, (int64_t)B * H, W, N, BN))) return rc;
+    const ConvGeom cg{H, W, C, 1, B};
+    cudaStream_t s = (cudaStream_t)stream;
+    const int flags = vector_flag(work, N, 0);
+    if (BN == 64) rc = gemm_launch<64, kModeWgrad>(ma, mb, work, M, N, (int)P, N, nullptr, flags, err_dev, splits, kt_per,
+                                                   mn, s, cg);
+    else rc = gemm_launch<128, kModeWgrad>(ma, mb, work, M, N, (int)P, N, nullptr, flags, err_dev, splits, kt_per, mn,
+                                           s, cg);
+    if (rc) return rc;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4 * sm_count()));
+    wgrad_sum_kernel<<<grid, 256, 0, s>>>(work, dW, M, N, splits, ldw);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
 }

@@ -45,20 +45,20 @@ __device__ __forceinline__ bool src_pixel(int hd, int wd, int ky, int kx, int s,
 
 // out[pd][(ky*ks+kx)*C + c] for pd over B x Hd x Wd, columns padded to Kpad.
 // VEC: C % 8 == 0 and 8 channels (16 bytes) per thread.
-template <bool TRANS, bool VEC>
+template <bool TRANS, bool VEC, typename I>
 __global__ void unfold_kernel(const bf16* __restrict__ src, bf16* __restrict__ out, int B, int Hs, int Ws, int C,
                               int Hd, int Wd, int ks, int s, int Kpad) {
     const int pad = ks >> 1;
     const int G = VEC ? 8 : 1;
-    const int kunits = Kpad / G;
-    const int64_t total = (int64_t)B * Hd * Wd * kunits;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const I kunits = (I)(Kpad / G);
+    const I total = (I)B * Hd * Wd * kunits;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x) {
         const int k = (int)(i % kunits) * G;
-        const int64_t p = i / kunits;
-        const int wd = (int)(p % Wd);
-        const int64_t t = p / Wd;
-        const int hd = (int)(t % Hd);
-        const int b = (int)(t / Hd);
+        const I p = i / kunits;
+        const int wd = (int)(p % (I)Wd);
+        const I t = p / (I)Wd;
+        const int hd = (int)(t % (I)Hd);
+        const int b = (int)(t / (I)Hd);
         const bf16* sp = nullptr;
         if (k < ks * ks * C) {
             const int tap = k / C, c = k - tap * C;
@@ -115,28 +115,42 @@ __global__ void unfold_t_kernel(const bf16* __restrict__ x, bf16* __restrict__ c
 // transpose of 16-bit values in registers, eight 16-byte stores).
 // Consecutive threads take the channel groups of consecutive pixel groups,
 // so a warp's loads cover whole pixels and its stores runs of 8 pixels.
+template <typename I>
 __global__ void unfold_t_vec_kernel(const bf16* __restrict__ x, bf16* __restrict__ colT, int H, int W, int C, int Ho,
                                     int Wo, int ks, int s, int64_t P) {
     const int pad = ks >> 1;
-    const int cgn = C >> 3;
-    const int64_t pgn = P >> 3;
-    const int64_t total = (int64_t)ks * ks * cgn * pgn;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const I cgn = (I)(C >> 3);
+    const I pgn = (I)(P >> 3);
+    const I total = (I)(ks * ks) * cgn * pgn;
+    // the 8 pixels of a group lie in one output row when Wo % 8 == 0
+    const bool row8 = (Wo & 7) == 0;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x) {
         // channel group fastest: a warp loads whole pixels (contiguous
         // channel groups) and stores 8 runs of consecutive pixels per row
         const int cg = (int)(i % cgn);
-        const int64_t rest = i / cgn;
-        const int64_t pg = rest % pgn;
+        const I rest = i / cgn;
+        const I pg = rest % pgn;
         const int tap = (int)(rest / pgn);
         const int ky = tap / ks, kx = tap - ky * ks;
+        int wo0 = 0, ho0 = 0, b0 = 0;
+        if (row8) {
+            const I p0 = pg * 8;
+            wo0 = (int)(p0 % (I)Wo);
+            const I t = p0 / (I)Wo;
+            ho0 = (int)(t % (I)Ho);
+            b0 = (int)(t / (I)Ho);
+        }
         uint32_t v[8][4];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const int64_t p = pg * 8 + j;
-            const int wo = (int)(p % Wo);
-            const int64_t t = p / Wo;
-            const int ho = (int)(t % Ho);
-            const int b = (int)(t / Ho);
+            int wo = wo0 + j, ho = ho0, b = b0;
+            if (!row8) {
+                const I p = pg * 8 + j;
+                wo = (int)(p % (I)Wo);
+                const I t = p / (I)Wo;
+                ho = (int)(t % (I)Ho);
+                b = (int)(t / (I)Ho);
+            }
             const int h = ho * s + ky - pad, w = wo * s + kx - pad;
             uint4 u = make_uint4(0, 0, 0, 0);
             if (h >= 0 && h < H && w >= 0 && w < W)
@@ -147,7 +161,7 @@ __global__ void unfold_t_vec_kernel(const bf16* __restrict__ x, bf16* __restrict
             v[j][3] = u.w;
         }
         // channel k of pixel j is the (k & 1) half of word k >> 1 of v[j]
-        bf16* dst = colT + ((int64_t)tap * C + cg * 8) * P + pg * 8;
+        bf16* dst = colT + ((int64_t)tap * C + cg * 8) * P + (int64_t)pg * 8;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             const uint32_t sel = (k & 1) ? 0x7632u : 0x5410u;  // high or low halves of two words
@@ -163,22 +177,73 @@ __global__ void unfold_t_vec_kernel(const bf16* __restrict__ x, bf16* __restrict
 
 // unfold_t for narrow inputs (C < 32, where a 32 x 32 tile would leave
 // most lanes idle): one thread per output element, pixels fastest.
+template <typename I>
 __global__ void unfold_t_small_kernel(const bf16* __restrict__ x, bf16* __restrict__ colT, int H, int W, int C, int Ho,
                                       int Wo, int ks, int s, int64_t P) {
     const int pad = ks >> 1;
-    const int64_t total = (int64_t)ks * ks * C * P;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t p = i % P;
-        const int k = (int)(i / P);
+    const I total = (I)(ks * ks * C) * (I)P;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x) {
+        const I p = i % (I)P;
+        const int k = (int)(i / (I)P);
         const int tap = k / C, c = k - tap * C;
         const int ky = tap / ks, kx = tap - ky * ks;
-        const int wo = (int)(p % Wo);
-        const int64_t t = p / Wo;
-        const int ho = (int)(t % Ho);
-        const int b = (int)(t / Ho);
+        const int wo = (int)(p % (I)Wo);
+        const I t = p / (I)Wo;
+        const int ho = (int)(t % (I)Ho);
+        const int b = (int)(t / (I)Ho);
         const int h = ho * s + ky - pad, w = wo * s + kx - pad;
         colT[i] = (h >= 0 && h < H && w >= 0 && w < W) ? x[(((int64_t)b * H + h) * W + w) * C + c]
                                                        : __float2bfloat16(0.f);
+    }
+}
+
+// Per-image-row transposes for the implicit weight gradient: for each of
+// the R = B H image rows r, the W x C block src[r][w][c] (NHWC, C % 8 == 0)
+// becomes dst[s R + r][c][w] = src[r][w + s - 1][c] for s < 3 (shifts = 3:
+// three copies shifted by -1, 0, +1 columns, zero outside the row) or
+// dst[r][c][w] = src[r][w][c] (shifts = 1).  One block per (row, 64
+// columns, 32 channels): the strip (with its one-column halo) is staged in
+// shared memory by 16-byte loads along channels and written by 16-byte
+// stores along columns.
+__global__ void row_transpose_kernel(const bf16* __restrict__ src, bf16* __restrict__ dst, int64_t R, int W, int C,
+                                     int shifts) {
+    __shared__ __align__(16) unsigned short tile[66][40];  // [w - w0 + 1][c - c0], rows of 80 bytes
+    const int wb = (W + 63) / 64, cb = (C + 31) / 32;
+    const int64_t items = R * wb * cb;
+    const int lo = shifts == 3 ? -1 : 0;
+    const int span = shifts == 3 ? 66 : 64;
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    for (int64_t it = blockIdx.x; it < items; it += gridDim.x) {
+        const int c0 = (int)(it % cb) * 32;
+        const int64_t r1 = it / cb;
+        const int w0 = (int)(r1 % wb) * 64;
+        const int64_t r = r1 / wb;
+        __syncthreads();
+        // 8 channels (16 bytes) per load
+        for (int e = threadIdx.x; e < span * 4; e += blockDim.x) {
+            const int j = e >> 2, q = e & 3;
+            const int w = w0 + lo + j, c = c0 + 8 * q;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (w >= 0 && w < W && c < C) v = __ldg(s4 + ((r * W + w) * C + c) / 8);
+            *reinterpret_cast<uint4*>(&tile[j][8 * q]) = v;
+        }
+        __syncthreads();
+        // 8 columns (16 bytes) per store; channels fastest across a warp, so
+        // the shared-memory reads of a warp fall in one tile row
+        for (int e = threadIdx.x; e < shifts * 32 * 8; e += blockDim.x) {
+            const int sh = e >> 8, cc = e & 31, w8 = (e >> 5) & 7;
+            const int c = c0 + cc, w = w0 + 8 * w8;
+            if (c >= C || w >= W) continue;
+            // tile row of output column w + k: (w + k + sh - 1) - (w0 - 1) = 8 w8 + k + sh
+            // (shifts = 3), (w + k) - w0 = 8 w8 + k (shifts = 1); W % 8 == 0, so w + 8 <= W
+            const int jb = shifts == 3 ? 8 * w8 + sh : 8 * w8;
+            uint4 o;
+            o.x = (uint32_t)tile[jb + 0][cc] | ((uint32_t)tile[jb + 1][cc] << 16);
+            o.y = (uint32_t)tile[jb + 2][cc] | ((uint32_t)tile[jb + 3][cc] << 16);
+            o.z = (uint32_t)tile[jb + 4][cc] | ((uint32_t)tile[jb + 5][cc] << 16);
+            o.w = (uint32_t)tile[jb + 6][cc] | ((uint32_t)tile[jb + 7][cc] << 16);
+            *reinterpret_cast<uint4*>(dst + (((int64_t)sh * R + r) * C + c) * W + w) = o;
+        }
     }
 }
 
@@ -305,32 +370,34 @@ __global__ void upsample_kernel(const bf16* __restrict__ x, bf16* __restrict__ y
 
 // vector form (C, Ctot, coff multiples of 8, 16-byte aligned): 8 channels
 // (16 bytes) per thread
+template <typename I>
 __global__ void upsample_vec_kernel(const uint4* __restrict__ x, uint4* __restrict__ y, int B, int H, int W, int C8,
                                     int Ctot8, int coff8) {
-    const int64_t total = (int64_t)B * 2 * H * 2 * W * C8;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C8);
-        int64_t t = i / C8;
-        const int w = (int)(t % (2 * W));
-        t /= 2 * W;
-        const int h = (int)(t % (2 * H));
-        const int b = (int)(t / (2 * H));
+    const I total = (I)B * 2 * H * 2 * W * C8;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x) {
+        const int c = (int)(i % (I)C8);
+        I t = i / (I)C8;
+        const int w = (int)(t % (I)(2 * W));
+        t /= (I)(2 * W);
+        const int h = (int)(t % (I)(2 * H));
+        const int b = (int)(t / (I)(2 * H));
         y[(((int64_t)b * 2 * H + h) * 2 * W + w) * Ctot8 + coff8 + c] =
             __ldg(x + (((int64_t)b * H + h / 2) * W + w / 2) * C8 + c);
     }
 }
 
 // its gradient: dx[b,h,w,c] = sum of the 2x2 block of dy[..., coff + c]
+template <typename I>
 __global__ void upsample_grad_kernel(const float* __restrict__ dy, float* __restrict__ dx, int B, int H, int W, int C,
                                      int Ctot, int coff) {
-    const int64_t total = (int64_t)B * H * W * C;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        int64_t t = i / C;
-        const int w = (int)(t % W);
-        t /= W;
-        const int h = (int)(t % H);
-        const int b = (int)(t / H);
+    const I total = (I)B * H * W * C;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x) {
+        const int c = (int)(i % (I)C);
+        I t = i / (I)C;
+        const int w = (int)(t % (I)W);
+        t /= (I)W;
+        const int h = (int)(t % (I)H);
+        const int b = (int)(t / (I)H);
         const int64_t r0 = (((int64_t)b * 2 * H + 2 * h) * 2 * W + 2 * w) * Ctot + coff + c;
         const int64_t rs = (int64_t)2 * W * Ctot;
         dx[i] = (dy[r0] + dy[r0 + Ctot]) + (dy[r0 + rs] + dy[r0 + rs + Ctot]);
@@ -338,17 +405,21 @@ __global__ void upsample_grad_kernel(const float* __restrict__ dy, float* __rest
 }
 
 // y[p][coff + c] = x[p][c]  (skip connection into the concatenation)
+template <typename I>
 __global__ void put_channels_kernel(const bf16* __restrict__ x, bf16* __restrict__ y, int64_t P, int C, int Ctot,
                                     int coff) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P * C; i += (int64_t)gridDim.x * blockDim.x)
-        y[(i / C) * Ctot + coff + (i % C)] = x[i];
+    const I total = (I)P * (I)C;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x)
+        y[(int64_t)(i / (I)C) * Ctot + coff + (int)(i % (I)C)] = x[i];
 }
 
 // y[p][c] (+)= x[p][coff + c]  (gradient of the skip connection)
+template <typename I>
 __global__ void take_channels_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t P, int C, int Ctot,
                                      int coff, int accumulate) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < P * C; i += (int64_t)gridDim.x * blockDim.x) {
-        const float v = x[(i / C) * Ctot + coff + (i % C)];
+    const I total = (I)P * (I)C;
+    for (I i = (I)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (I)gridDim.x * blockDim.x) {
+        const float v = x[(int64_t)(i / (I)C) * Ctot + coff + (int)(i % (I)C)];
         y[i] = accumulate ? y[i] + v : v;
     }
 }
@@ -392,13 +463,22 @@ __global__ void mse_final_kernel(const double* __restrict__ partials, int np, in
 }
 
 // scale[b] = 1 / sqrt(mean over image b of x^2) (0 for an all-zero image);
-// one block per image, fixed reduction order
+// one block per image, fixed reduction order.  Each thread keeps a
+// compensated (Kahan) float32 sum of its strided elements -- the float64
+// pipe of this GPU runs at 1/64 of the float32 rate -- and the block adds
+// the 512 per-thread sums in float64.
 __global__ void image_rms_kernel(const float* __restrict__ x, int64_t n, float* __restrict__ scale) {
     const float* xb = x + (int64_t)blockIdx.x * n;
-    double acc = 0.0;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += (double)xb[i] * xb[i];
+    float sum = 0.f, comp = 0.f;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const float v = xb[i];
+        const float y = __fmul_rn(v, v) - comp;
+        const float t = __fadd_rn(sum, y);
+        comp = __fsub_rn(__fsub_rn(t, sum), y);
+        sum = t;
+    }
     __shared__ double sh[512];
-    sh[threadIdx.x] = acc;
+    sh[threadIdx.x] = (double)sum - (double)comp;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
@@ -439,13 +519,19 @@ int kgb_unet_unfold(const void* src, void* out, int B, int Hs, int Ws, int C, in
     cudaStream_t s = (cudaStream_t)stream;
     const bf16* x = (const bf16*)src;
     bf16* y = (bf16*)out;
+    // 32-bit index arithmetic whenever the element count allows it
+    const bool i32 = n < (int64_t)1 << 31;
+#define KGB_UNFOLD(T, V)                                                                                    \
+    (i32 ? unfold_kernel<T, V, uint32_t><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad) \
+         : unfold_kernel<T, V, int64_t><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad))
     if (transposed) {
-        if (vec) unfold_kernel<true, true><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
-        else unfold_kernel<true, false><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
+        if (vec) KGB_UNFOLD(true, true);
+        else KGB_UNFOLD(true, false);
     } else {
-        if (vec) unfold_kernel<false, true><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
-        else unfold_kernel<false, false><<<grid_for(n), 256, 0, s>>>(x, y, B, Hs, Ws, C, Hd, Wd, ks, stride, Kpad);
+        if (vec) KGB_UNFOLD(false, true);
+        else KGB_UNFOLD(false, false);
     }
+#undef KGB_UNFOLD
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -459,12 +545,20 @@ int kgb_unet_unfold_t(const void* x, void* colT, int B, int H, int W, int C, int
     if ((P + 31) / 32 > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "unet_unfold_t: too many pixels");
     if (C % 8 == 0 && P % 8 == 0 && ((uintptr_t)x & 15) == 0 && ((uintptr_t)colT & 15) == 0) {
         const int64_t n = (int64_t)ks * ks * (C / 8) * (P / 8);
-        unfold_t_vec_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, H, W, C, Ho,
-                                                                            Wo, ks, stride, P);
+        if (n < (int64_t)1 << 31)
+            unfold_t_vec_kernel<uint32_t><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, H,
+                                                                                        W, C, Ho, Wo, ks, stride, P);
+        else
+            unfold_t_vec_kernel<int64_t><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, H,
+                                                                                       W, C, Ho, Wo, ks, stride, P);
     } else if (C < 32) {
         const int64_t n = (int64_t)ks * ks * C * P;
-        unfold_t_small_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, H, W, C, Ho,
-                                                                             Wo, ks, stride, P);
+        if (n < (int64_t)1 << 31)
+            unfold_t_small_kernel<uint32_t><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(
+                (const bf16*)x, (bf16*)colT, H, W, C, Ho, Wo, ks, stride, P);
+        else
+            unfold_t_small_kernel<int64_t><<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(
+                (const bf16*)x, (bf16*)colT, H, W, C, Ho, Wo, ks, stride, P);
     } else {
         dim3 grid((unsigned)((P + 31) / 32), (unsigned)((C + 31) / 32), (unsigned)(ks * ks)), block(32, 8);
         unfold_t_kernel<<<grid, block, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)colT, B, H, W, C, Ho, Wo,
@@ -534,12 +628,19 @@ int kgb_unet_upsample(const void* x, void* y, int B, int H, int W, int C, int Ct
     cudaStream_t s = (cudaStream_t)stream;
     if (grad) {
         const int64_t n = (int64_t)B * H * W * C;
-        upsample_grad_kernel<<<grid_for(n), 256, 0, s>>>((const float*)x, (float*)y, B, H, W, C, Ctot, coff);
+        if (n < (int64_t)1 << 31)
+            upsample_grad_kernel<uint32_t><<<grid_for(n), 256, 0, s>>>((const float*)x, (float*)y, B, H, W, C, Ctot, coff);
+        else
+            upsample_grad_kernel<int64_t><<<grid_for(n), 256, 0, s>>>((const float*)x, (float*)y, B, H, W, C, Ctot, coff);
     } else {
         if (C % 8 == 0 && Ctot % 8 == 0 && coff % 8 == 0 && (((uintptr_t)x | (uintptr_t)y) & 15) == 0) {
             const int64_t n = (int64_t)B * 4 * H * W * (C / 8);
-            upsample_vec_kernel<<<grid_for(n), 256, 0, s>>>((const uint4*)x, (uint4*)y, B, H, W, C / 8, Ctot / 8,
-                                                            coff / 8);
+            if (n < (int64_t)1 << 31)
+                upsample_vec_kernel<uint32_t><<<grid_for(n), 256, 0, s>>>((const uint4*)x, (uint4*)y, B, H, W, C / 8,
+                                                                          Ctot / 8, coff / 8);
+            else
+                upsample_vec_kernel<int64_t><<<grid_for(n), 256, 0, s>>>((const uint4*)x, (uint4*)y, B, H, W, C / 8,
+                                                                         Ctot / 8, coff / 8);
         } else {
             const int64_t n = (int64_t)B * 4 * H * W * C;
             upsample_kernel<<<grid_for(n), 256, 0, s>>>((const bf16*)x, (bf16*)y, B, H, W, C, Ctot, coff);
@@ -554,10 +655,17 @@ int kgb_unet_channels(const void* x, void* y, int64_t P, int C, int Ctot, int co
     if (!x || !y || P <= 0 || C <= 0 || coff < 0 || coff + C > Ctot)
         return set_error(KGB_ERR_VALUE, "unet_channels: bad arguments");
     cudaStream_t s = (cudaStream_t)stream;
-    if (take)
-        take_channels_kernel<<<grid_for(P * C), 256, 0, s>>>((const float*)x, (float*)y, P, C, Ctot, coff, accumulate);
+    const bool i32 = P * C < (int64_t)1 << 31;
+    if (take && i32)
+        take_channels_kernel<uint32_t><<<grid_for(P * C), 256, 0, s>>>((const float*)x, (float*)y, P, C, Ctot, coff,
+                                                                       accumulate);
+    else if (take)
+        take_channels_kernel<int64_t><<<grid_for(P * C), 256, 0, s>>>((const float*)x, (float*)y, P, C, Ctot, coff,
+                                                                      accumulate);
+    else if (i32)
+        put_channels_kernel<uint32_t><<<grid_for(P * C), 256, 0, s>>>((const bf16*)x, (bf16*)y, P, C, Ctot, coff);
     else
-        put_channels_kernel<<<grid_for(P * C), 256, 0, s>>>((const bf16*)x, (bf16*)y, P, C, Ctot, coff);
+        put_channels_kernel<int64_t><<<grid_for(P * C), 256, 0, s>>>((const bf16*)x, (bf16*)y, P, C, Ctot, coff);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -565,6 +673,18 @@ int kgb_unet_channels(const void* x, void* y, int64_t P, int C, int Ctot, int co
 int kgb_unet_to_bf16(const float* x, void* y, int64_t n, int B, const float* scale, void* stream) {
     if (!x || !y || n <= 0 || B <= 0) return set_error(KGB_ERR_VALUE, "unet_to_bf16: bad arguments");
     to_bf16_kernel<<<grid_for(n * B), 256, 0, (cudaStream_t)stream>>>(x, (bf16*)y, n, B, scale);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_row_transpose(const void* src, void* dst, int B, int H, int W, int C, int shifts, void* stream) {
+    if (!src || !dst || B <= 0 || H <= 0 || W <= 0 || C <= 0 || C % 8 || W % 8 || (shifts != 1 && shifts != 3) ||
+        (((uintptr_t)src | (uintptr_t)dst) & 15))
+        return set_error(KGB_ERR_VALUE, "unet_row_transpose: bad arguments (C and W multiples of 8, 16-byte aligned)");
+    const int64_t R = (int64_t)B * H;
+    const int64_t items = R * ((W + 63) / 64) * ((C + 31) / 32);
+    const int grid = (int)std::min<int64_t>(items, 16 * 152);
+    row_transpose_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const bf16*)src, (bf16*)dst, R, W, C, shifts);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

@@ -75,7 +75,7 @@ class _CountingLib:
     launches (two for the split-K GEMM, the row sums and the MSE, one for
     the others)."""
 
-    _KERNELS = {"kgb_gemm_bf16_tn_splitk": 2, "kgb_unet_rowsum": 2, "kgb_unet_mse": 2}
+    _KERNELS = {"kgb_gemm_bf16_tn_splitk": 2, "kgb_unet_rowsum": 2, "kgb_unet_mse": 2, "kgb_conv3x3_wgrad_bf16": 2}
 
     def __init__(self, owner):
         self._owner = owner
@@ -293,6 +293,7 @@ class UNet:
         ws["col"] = torch.empty(col, dtype=bf, device=dev)
         ws["g"] = torch.empty(gmax, dtype=bf, device=dev)
         ws["gT"] = torch.empty(gmax, dtype=bf, device=dev)
+        ws["gTr"] = torch.empty(gmax, dtype=bf, device=dev)
         ws["work_elems"] = 1 << 23
         ws["work"] = torch.empty(ws["work_elems"], dtype=f32, device=dev)
         self._ws, self._ws_key = ws, key
@@ -356,10 +357,20 @@ class UNet:
             _native.check(L.kgb_unet_transpose(g.data_ptr(), gT.data_ptr(), P_out, c.cout, c.cout, P_out, 0, s))
         _native.check(L.kgb_unet_rowsum(gT.data_ptr(), self._db(c).data_ptr(), c.cout, P_out, ws["work"].data_ptr(),
                                          s))
-        _native.check(L.kgb_unet_unfold_t(x.data_ptr(), col.data_ptr(), B, H, W, c.cin, c.ks, c.stride, s))
-        _native.check(L.kgb_gemm_bf16_tn_splitk(gT.data_ptr(), col.data_ptr(), self._dw(c).data_ptr(), c.cout, c.kc,
-                                                P_out, P_out, P_out, c.kpad, 0, ws["work"].data_ptr(),
-                                                ws["work_elems"], self._err.data_ptr(), s))
+        if self.implicit and c.ks == 3 and c.stride == 1 and c.cin % 32 == 0 and c.cout % 8 == 0 and W % 64 == 0:
+            # implicit weight gradient: x and g transposed per image row (x in
+            # three column-shifted copies) instead of the nine-tap unfolded copy
+            gTr = ws["gTr"]
+            _native.check(L.kgb_unet_row_transpose(x.data_ptr(), col.data_ptr(), B, H, W, c.cin, 3, s))
+            _native.check(L.kgb_unet_row_transpose(g.data_ptr(), gTr.data_ptr(), B, H, W, c.cout, 1, s))
+            _native.check(L.kgb_conv3x3_wgrad_bf16(col.data_ptr(), gTr.data_ptr(), self._dw(c).data_ptr(), B, H, W,
+                                                   c.cin, c.cout, c.kpad, ws["work"].data_ptr(), ws["work_elems"],
+                                                   self._err.data_ptr(), s))
+        else:
+            _native.check(L.kgb_unet_unfold_t(x.data_ptr(), col.data_ptr(), B, H, W, c.cin, c.ks, c.stride, s))
+            _native.check(L.kgb_gemm_bf16_tn_splitk(gT.data_ptr(), col.data_ptr(), self._dw(c).data_ptr(), c.cout,
+                                                    c.kc, P_out, P_out, P_out, c.kpad, 0, ws["work"].data_ptr(),
+                                                    ws["work_elems"], self._err.data_ptr(), s))
         if dx is None:
             return
         if self.implicit and c.implicit_dx and _tileable(H, W):

@@ -158,3 +158,45 @@ def test_unet_implicit_and_explicit_paths_agree():
         assert _rel(wa, wb) < 3e-2 and _rel(ba, bb) < 3e-2
     a.check_errors()
     b.check_errors()
+
+
+@pytest.mark.parametrize("B,H,W,C,N", [(2, 8, 64, 32, 32), (1, 4, 128, 96, 64), (2, 6, 64, 64, 136),
+                                       (1, 3, 64, 256, 16)])
+def test_implicit_weight_gradient_matches_conv2d_weight(B, H, W, C, N):
+    """kgb_unet_row_transpose + kgb_conv3x3_wgrad_bf16 (operands transposed
+    per image row, x in three column-shifted copies; rows (tap, channel),
+    split over pixels) against the weight gradient of torch conv2d (padding
+    1) on the same bf16-rounded operands:
+    dW[n][(ky*3 + kx)*C + c] = sum over pixels of g[p][n] x[p + (ky-1, kx-1)][c]."""
+    from pylops_gb300 import _native
+
+    g = torch.Generator().manual_seed(B * 100 + C + N)
+    x = _bf(torch.randn(B, H, W, C, generator=g))
+    gy = _bf(torch.randn(B, H, W, N, generator=g))
+    ref = torch.nn.grad.conv2d_weight(x.permute(0, 3, 1, 2).double(), (N, C, 3, 3),
+                                      gy.permute(0, 3, 1, 2).double(), padding=1)
+    ref = ref.permute(0, 2, 3, 1).reshape(N, 9 * C).float()  # [n][(ky*3+kx)*C + c]
+    P = B * H * W
+    xd = x.to(torch.bfloat16).cuda().contiguous()
+    gd = gy.to(torch.bfloat16).cuda().contiguous()
+    xT3 = torch.empty(3 * P * C, dtype=torch.bfloat16, device="cuda")
+    gTr = torch.empty(P * N, dtype=torch.bfloat16, device="cuda")
+    ldw = 9 * C + 8
+    dW = torch.full((N, ldw), 5.0, device="cuda")
+    work = torch.empty(1 << 22, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    L, s = _native.lib(), torch.cuda.current_stream().cuda_stream
+    _native.check(L.kgb_unet_row_transpose(xd.data_ptr(), xT3.data_ptr(), B, H, W, C, 3, s))
+    _native.check(L.kgb_unet_row_transpose(gd.data_ptr(), gTr.data_ptr(), B, H, W, N, 1, s))
+    # the transposed operands themselves: [shift][b][h][c][w] and [b][h][n][w]
+    x3 = xT3.view(3, B, H, C, W).float().cpu()
+    xp = torch.nn.functional.pad(x.permute(0, 1, 3, 2), (1, 1))  # (B, H, C, W + 2)
+    for kx in range(3):
+        assert torch.equal(x3[kx], xp[..., kx:kx + W])
+    assert torch.equal(gTr.view(B, H, N, W).float().cpu(), gy.permute(0, 1, 3, 2))
+    _native.check(L.kgb_conv3x3_wgrad_bf16(xT3.data_ptr(), gTr.data_ptr(), dW.data_ptr(), B, H, W, C, N, ldw,
+                                           work.data_ptr(), work.numel(), err.data_ptr(), s))
+    got = dW.cpu()
+    assert int(err.item()) == 0
+    assert _rel(got[:, :9 * C].numpy(), ref.numpy()) < 1e-5
+    assert torch.all(got[:, 9 * C:] == 5.0)
