@@ -334,13 +334,15 @@ int kgb_conv3x3_bf16(const void* x_dev, const void* w_dev, void* y_dev, int B, i
 /* Weight gradient of that convolution without an unfolded copy:
  * dW[n][tap*C + c] = sum_p g[p][n] x[pixel(p) + (ky-1, kx-1)][c] (float32,
  * row stride ldw >= 9 C), from gTr (bf16, B H x N x W: the output gradient
- * transposed per image row) and xT3 (bf16, 3 x B H x C x W: the input
- * transposed per image row, copy kx shifted by kx - 1 columns with zero
- * fill), both as kgb_unet_row_transpose writes them.  A tensor-core GEMM
- * with rows (tap, channel), reduction over pixels (64 per step, one image
- * row segment; the row shift ky is the TMA box's zero fill), split over the
- * pixels into `work` (at least 9 C x N floats) and summed in slice order
- * (deterministic).  C % 32 == 0, W % 64 == 0.  No reference counterpart. */
+ * transposed per image row) and xT3 (bf16, B H x 3 x C x W: the input
+ * transposed per image row in three copies, copy kx shifted by kx - 1
+ * columns with zero fill), both as kgb_unet_row_transpose writes them.  A
+ * tensor-core GEMM whose 128-row A tiles are rows (kx, c) of one image row
+ * of xT3 (one TMA box each; the row shift ky is the box's zero fill at the
+ * image edges), reduction over pixels (64 per step, one image row segment),
+ * split over the pixels into `work` (at least 3 ceil(3 C / 128) 128 x N
+ * floats) and summed in slice order (deterministic).  C % 32 == 0,
+ * W % 64 == 0.  No reference counterpart. */
 int kgb_conv3x3_wgrad_bf16(const void* xT3_dev, const void* gTr_dev, float* dW_dev, int B, int H, int W, int C, int N,
                            int ldw, float* work_dev, int64_t work_elems, int* err_dev, void* stream);
 
@@ -372,7 +374,7 @@ int kgb_conv3x3_wgrad_bf16(const void* xT3_dev, const void* gTr_dev, float* dW_d
  *  to_bf16      y = x * scale[image] (scale may be NULL);
  *  image_rms    scale[b] = 1/rms of image b (B images of n floats; 0 if zero);
  *  row_transpose  per image row r = b H + h of NHWC src (C, W multiples of
- *               8): dst[s B H + r][c][w] = src[r][w + s - 1][c], s < 3
+ *               8): dst[r][s][c][w] = src[r][w + s - 1][c], s < 3
  *               (shifts = 3, zero outside the row), or dst[r][c][w] =
  *               src[r][w][c] (shifts = 1): the operands of
  *               kgb_conv3x3_wgrad_bf16;

@@ -93,8 +93,9 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map
 // an M tile of 128 output pixels is a box of bh rows x bw columns of one
 // image; k-tile g is (tap = g / cblk, channel block g % cblk) and reads the
 // input shifted by sgn * (ky - 1, kx - 1) (sgn = -1: the transposed
-// convolution of the data gradient).  Weight gradient: cblk = channels per
-// tap (rows of A are (tap, channel)), k-tile = 64 pixels of one image row.
+// convolution of the data gradient).  Weight gradient: cblk = 128-row tiles
+// per ky (rows of A are (ky, kx, channel)), k-tile = 64 pixels of one image
+// row.
 struct ConvGeom {
     int H, W, cblk, sgn;
     int nimg;  // weight gradient: images per shifted copy
@@ -226,22 +227,17 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
                         break;
                     }
                     if (MODE == kModeWgrad) {
-                        // 64 pixels of one image row; A rows m0.. in boxes of
-                        // 32 (tap, channel) rows, each from the copy shifted by
-                        // its kx, at row h + ky - 1 (zero fill outside)
+                        // 64 pixels of one image row; the A tile is rows
+                        // j0 .. j0 + 127 of the 3 C rows (kx, c) of image row
+                        // h + ky - 1 (zero fill outside the image and past 3 C)
                         const int p0 = (kt0 + kt) * BK;
                         const int hw = cg.H * cg.W;
                         const int b = p0 / hw, r = p0 - b * hw;
                         const int h = r / cg.W, wp = r - h * cg.W;
-                        const int nbox = min(4, (M - m0) >> 5);
-                        mbar_expect_tx(bar_full + 8 * s, (uint32_t)(nbox * (A_BYTES / 4) + B_BYTES));
-                        for (int i = 0; i < nbox; ++i) {
-                            const int row = m0 + 32 * i;
-                            const int tap = row / cg.cblk, c = row - tap * cg.cblk;
-                            const int ky = tap / 3, kx = tap - ky * 3;
-                            tma_load_4d(sA + s * A_BYTES + i * (A_BYTES / 4), &tmA, bar_full + 8 * s, wp, c, h + ky - 1,
-                                        kx * cg.nimg + b);
-                        }
+                        const int tm = m0 / BM;
+                        const int ky = tm / cg.cblk, j0 = (tm - ky * cg.cblk) * BM;
+                        mbar_expect_tx(bar_full + 8 * s, A_BYTES + B_BYTES);
+                        tma_load_4d(sA + s * A_BYTES, &tmA, bar_full + 8 * s, wp, j0, h + ky - 1, b);
                         tma_load_3d(sB + s * B_BYTES, &tmB, bar_full + 8 * s, wp, n0, b * cg.H + h);
                         continue;
                     }
@@ -455,15 +451,15 @@ int make_map_nhwc(CUtensorMap* map, const void* base, int B, int H, int W, int C
     return KGB_OK;
 }
 
-// Column-shifted row-blocked copies xT3[kx][b][h][c][w] (bf16) as a 4-D
-// tensor {W, C, H, 3B}; box {64 columns, 32 channels, 1, 1} = 32 rows of 128
-// bytes (512-byte apart in memory), a quarter of the 128-row A tile.
+// Column-shifted copies stacked per image row, xT3[b][h][kx][c][w] (bf16),
+// as a 4-D tensor {W, 3C, H, B}; box {64 columns, 128 rows (kx, c), 1, 1} =
+// one 128-row A tile (rows past 3 C are zero fill).
 int make_map_wgrad(CUtensorMap* map, const void* base, int B, int H, int W, int C) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return set_error(KGB_ERR_CUDA, "wgrad: cuTensorMapEncodeTiled unavailable");
-    cuuint64_t dims[4] = {(cuuint64_t)W, (cuuint64_t)C, (cuuint64_t)H, (cuuint64_t)3 * B};
-    cuuint64_t strides[3] = {(cuuint64_t)W * 2, (cuuint64_t)C * W * 2, (cuuint64_t)H * C * W * 2};
-    cuuint32_t box[4] = {(cuuint32_t)BK, 32, 1, 1};
+    cuuint64_t dims[4] = {(cuuint64_t)W, (cuuint64_t)3 * C, (cuuint64_t)H, (cuuint64_t)B};
+    cuuint64_t strides[3] = {(cuuint64_t)W * 2, (cuuint64_t)3 * C * W * 2, (cuuint64_t)H * 3 * C * W * 2};
+    cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)BM, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -488,14 +484,19 @@ int make_map_rows(CUtensorMap* map, const void* base, int64_t R, int W, int N, i
     return KGB_OK;
 }
 
-// dW[n][q] = sum over z of work[z][q][n], q = tap * C + c < M, in order z = 0, 1, ...
+// dW[n][tap C + c] = sum over z of work[z][ky Mky + kx C + c][n] (tap = 3 ky
+// + kx; Mky rows per ky), in order z = 0, 1, ...
 __global__ void wgrad_sum_kernel(const float* __restrict__ work, float* __restrict__ dW, int M, int N, int splits,
-                                 int ldw) {
-    const int64_t total = (int64_t)M * N, mn = (int64_t)M * N;
+                                 int C, int Mky, int ldw) {
+    const int Q = 9 * C;
+    const int64_t total = (int64_t)Q * N, mn = (int64_t)M * N;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-        const int n = (int)(i / M), q = (int)(i - (int64_t)n * M);
+        const int n = (int)(i / Q), q = (int)(i - (int64_t)n * Q);
+        const int tap = q / C, c = q - tap * C;
+        const int ky = tap / 3, kx = tap - ky * 3;
+        const int64_t row = (int64_t)ky * Mky + kx * C + c;
         float acc = 0.f;
-        for (int z = 0; z < splits; ++z) acc += work[z * mn + (int64_t)q * N + n];
+        for (int z = 0; z < splits; ++z) acc += work[z * mn + row * N + n];
         dW[(int64_t)n * ldw + q] = acc;
     }
 }
@@ -664,13 +665,18 @@ extern "C" int kgb_conv3x3_wgrad_bf16(const void* xT3, const void* gTr, float* d
         return set_error(KGB_ERR_VALUE, "wgrad: operands must be 16-byte aligned");
     const int64_t P = (int64_t)B * H * W;
     if (P > 0x7fffffffLL || (int64_t)3 * B > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "wgrad: too many pixels");
-    const int M = 9 * C;
+    // rows of A: per ky, the 3 C rows (kx, c) of the shifted copies, in
+    // 128-row tiles (the last one zero-filled past 3 C)
+    const int mt_ky = (3 * C + BM - 1) / BM;
+    const int Mky = mt_ky * BM;
+    const int M = 3 * Mky;
     const int BN = N <= 64 ? 64 : 128;
-    const int64_t tiles = (int64_t)((M + BM - 1) / BM) * ((N + BN - 1) / BN);
+    const int64_t tiles = (int64_t)(M / BM) * ((N + BN - 1) / BN);
     const int ktiles = (int)(P / BK);
     const int64_t mn = (int64_t)M * N;
-    if (work_elems < mn) return set_error(KGB_ERR_VALUE, "wgrad: work buffer smaller than 9 C x N");
-    int splits = (int)std::max<int64_t>(1, (2 * sm_count() + tiles - 1) / tiles);
+    if (work_elems < mn) return set_error(KGB_ERR_VALUE, "wgrad: work buffer smaller than the padded 9 C x N");
+    // at most two tiles per SM: the persistent grid then ends evenly
+    int splits = (int)std::max<int64_t>(1, (2 * sm_count()) / tiles);
     splits = (int)std::min<int64_t>(splits, work_elems / mn);
     splits = std::max(1, std::min(splits, ktiles));
     const int kt_per = (ktiles + splits - 1) / splits;
@@ -679,7 +685,7 @@ extern "C" int kgb_conv3x3_wgrad_bf16(const void* xT3, const void* gTr, float* d
     int rc;
     if ((rc = make_map_wgrad(&ma, xT3, B, H, W, C))) return rc;
     if ((rc = make_map_rows(&mb, gTr, (int64_t)B * H, W, N, BN))) return rc;
-    const ConvGeom cg{H, W, C, 1, B};
+    const ConvGeom cg{H, W, mt_ky, 1, B};
     cudaStream_t s = (cudaStream_t)stream;
     const int flags = vector_flag(work, N, 0);
     if (BN == 64) rc = gemm_launch<64, kModeWgrad>(ma, mb, work, M, N, (int)P, N, nullptr, flags, err_dev, splits, kt_per,
@@ -688,7 +694,7 @@ extern "C" int kgb_conv3x3_wgrad_bf16(const void* xT3, const void* gTr, float* d
                                            s, cg);
     if (rc) return rc;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4 * sm_count()));
-    wgrad_sum_kernel<<<grid, 256, 0, s>>>(work, dW, M, N, splits, ldw);
+    wgrad_sum_kernel<<<grid, 256, 0, s>>>(work, dW, M, N, splits, C, Mky, ldw);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

@@ -199,8 +199,9 @@ __global__ void unfold_t_small_kernel(const bf16* __restrict__ x, bf16* __restri
 
 // Per-image-row transposes for the implicit weight gradient: for each of
 // the R = B H image rows r, the W x C block src[r][w][c] (NHWC, C % 8 == 0)
-// becomes dst[s R + r][c][w] = src[r][w + s - 1][c] for s < 3 (shifts = 3:
-// three copies shifted by -1, 0, +1 columns, zero outside the row) or
+// becomes dst[r][s][c][w] = src[r][w + s - 1][c] for s < 3 (shifts = 3:
+// three copies shifted by -1, 0, +1 columns, zero outside the row, stacked
+// per row so that the 3 C rows of one image row are contiguous) or
 // dst[r][c][w] = src[r][w][c] (shifts = 1).  One block per (row, 64
 // columns, 32 channels): the strip (with its one-column halo) is staged in
 // shared memory by 16-byte loads along channels and written by 16-byte
@@ -242,7 +243,7 @@ __global__ void row_transpose_kernel(const bf16* __restrict__ src, bf16* __restr
             o.y = (uint32_t)tile[jb + 2][cc] | ((uint32_t)tile[jb + 3][cc] << 16);
             o.z = (uint32_t)tile[jb + 4][cc] | ((uint32_t)tile[jb + 5][cc] << 16);
             o.w = (uint32_t)tile[jb + 6][cc] | ((uint32_t)tile[jb + 7][cc] << 16);
-            *reinterpret_cast<uint4*>(dst + (((int64_t)sh * R + r) * C + c) * W + w) = o;
+            *reinterpret_cast<uint4*>(dst + ((r * shifts + sh) * C + c) * W + w) = o;
         }
     }
 }

@@ -164,8 +164,8 @@ def test_unet_implicit_and_explicit_paths_agree():
                                        (1, 3, 64, 256, 16)])
 def test_implicit_weight_gradient_matches_conv2d_weight(B, H, W, C, N):
     """kgb_unet_row_transpose + kgb_conv3x3_wgrad_bf16 (operands transposed
-    per image row, x in three column-shifted copies; rows (tap, channel),
-    split over pixels) against the weight gradient of torch conv2d (padding
+    per image row, x in three column-shifted copies stacked per row; rows
+    (ky, kx, channel), split over pixels) against the weight gradient of torch conv2d (padding
     1) on the same bf16-rounded operands:
     dW[n][(ky*3 + kx)*C + c] = sum over pixels of g[p][n] x[p + (ky-1, kx-1)][c]."""
     from pylops_gb300 import _native
@@ -188,11 +188,11 @@ def test_implicit_weight_gradient_matches_conv2d_weight(B, H, W, C, N):
     L, s = _native.lib(), torch.cuda.current_stream().cuda_stream
     _native.check(L.kgb_unet_row_transpose(xd.data_ptr(), xT3.data_ptr(), B, H, W, C, 3, s))
     _native.check(L.kgb_unet_row_transpose(gd.data_ptr(), gTr.data_ptr(), B, H, W, N, 1, s))
-    # the transposed operands themselves: [shift][b][h][c][w] and [b][h][n][w]
-    x3 = xT3.view(3, B, H, C, W).float().cpu()
+    # the transposed operands themselves: [b][h][shift][c][w] and [b][h][n][w]
+    x3 = xT3.view(B, H, 3, C, W).float().cpu()
     xp = torch.nn.functional.pad(x.permute(0, 1, 3, 2), (1, 1))  # (B, H, C, W + 2)
     for kx in range(3):
-        assert torch.equal(x3[kx], xp[..., kx:kx + W])
+        assert torch.equal(x3[:, :, kx], xp[..., kx:kx + W])
     assert torch.equal(gTr.view(B, H, N, W).float().cpu(), gy.permute(0, 1, 3, 2))
     _native.check(L.kgb_conv3x3_wgrad_bf16(xT3.data_ptr(), gTr.data_ptr(), dW.data_ptr(), B, H, W, C, N, ldw,
                                            work.data_ptr(), work.numel(), err.data_ptr(), s))
