@@ -373,6 +373,19 @@ int kgb_conv3x3_wgrad_bf16(const void* xT3_dev, const void* gTr_dev, float* dW_d
  *               x into y, accumulate optional);
  *  to_bf16      y = x * scale[image] (scale may be NULL);
  *  image_rms    scale[b] = 1/rms of image b (B images of n floats; 0 if zero);
+ *  colsum       out[c] = sum_r wt[r] g[r][c] (bf16 g, rows x cols, cols a
+ *               multiple of 8 up to 256; wt bf16 or NULL for 1: bias
+ *               gradients from the NHWC gradient, or the weight gradient of a
+ *               1x1 convolution to one channel; work: 1024 x cols floats;
+ *               fixed summation order);
+ *  head_forward y[p] = bias[0] + sum_c w[c] x[p][c]: the 1x1 convolution to
+ *               one channel (x bf16 NHWC, C % 8 == 0, float32 y);
+ *  head_dx      its data gradient dx[p][c] = g[p] w[c] (float32, C % 4 == 0);
+ *  conv3x3_c1   3x3 convolution (padding 1) of a one-channel image: y[p][n] =
+ *               act(bias[n] + sum_t w[n * kpad + t] x[p + off(t)]), bf16 y,
+ *               N % 8 == 0, N <= 128, ReLU if relu;
+ *  conv3x3_c1_wgrad  its weight gradient dW[n * kpad + t] = sum_p g[p][n]
+ *               x[p + off(t)] (work: 1024 x 9 N floats, fixed order);
  *  row_transpose  per image row r = b H + h of NHWC src (C, W multiples of
  *               8): dst[r][s][c][w] = src[r][w + s - 1][c], s < 3
  *               (shifts = 3, zero outside the row), or dst[r][c][w] =
@@ -397,6 +410,13 @@ int kgb_unet_channels(const void* x, void* y, int64_t P, int C, int Ctot, int co
 int kgb_unet_to_bf16(const float* x, void* y, int64_t n, int B, const float* scale, void* stream);
 int kgb_unet_image_rms(const float* x, int64_t n, int B, float* scale, void* stream);
 int kgb_unet_row_transpose(const void* src, void* dst, int B, int H, int W, int C, int shifts, void* stream);
+int kgb_unet_colsum(const void* g, const void* wt, float* out, int64_t rows, int cols, float* work, void* stream);
+int kgb_unet_head_forward(const void* x, const void* w, const float* bias, float* y, int64_t P, int C, void* stream);
+int kgb_unet_head_dx(const void* g, const void* w, float* dx, int64_t P, int C, void* stream);
+int kgb_unet_conv3x3_c1(const void* x, const void* w, const void* bias, void* y, int B, int H, int W, int N, int kpad,
+                        int relu, void* stream);
+int kgb_unet_conv3x3_c1_wgrad(const void* x, const void* g, float* dW, int B, int H, int W, int N, int kpad,
+                              float* work, void* stream);
 int kgb_unet_mse(const float* y, const float* t, float* grad, int64_t n, double* partials, double* loss,
                  void* stream);
 int kgb_unet_adam(float* w, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2, float eps,

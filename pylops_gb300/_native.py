@@ -97,6 +97,11 @@ _SIGNATURES = {
     "kgb_unet_to_bf16": ([c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),
     "kgb_unet_image_rms": ([c_vp, c_i64, c_int, c_vp, c_vp], c_int),
     "kgb_unet_row_transpose": ([c_vp, c_vp] + [c_int] * 5 + [c_vp], c_int),
+    "kgb_unet_colsum": ([c_vp, c_vp, c_vp, c_i64, c_int, c_vp, c_vp], c_int),
+    "kgb_unet_head_forward": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_int, c_vp], c_int),
+    "kgb_unet_head_dx": ([c_vp, c_vp, c_vp, c_i64, c_int, c_vp], c_int),
+    "kgb_unet_conv3x3_c1": ([c_vp, c_vp, c_vp, c_vp] + [c_int] * 6 + [c_vp], c_int),
+    "kgb_unet_conv3x3_c1_wgrad": ([c_vp, c_vp, c_vp] + [c_int] * 5 + [c_vp, c_vp], c_int),
     "kgb_unet_mse": ([c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp], c_int),
     "kgb_unet_adam": ([c_vp, c_vp, c_vp, c_vp, c_i64, c_float, c_float, c_float, c_float, c_int, c_vp], c_int),
     "kgb_eikonal_tables": ([c_int, c_ip, c_dp, c_dp, c_int, c_ip, c_dp, c_dp, c_int, c_int], c_int),

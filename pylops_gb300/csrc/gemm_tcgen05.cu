@@ -142,6 +142,74 @@ __host__ __device__ constexpr int gemm_stages() {
 
 constexpr int kGemmThreads = 192;  // warp 0 producer, warp 1 MMA, warps 2-5 epilogue
 
+// Epilogue of one 128 x BN tile: the calling warp reads tensor-memory lanes
+// 32 q .. 32 q + 31 of accumulator a (rows m0 + 32 q + lane), adds the bias,
+// applies ReLU (flags & 1) and stores float32 or bf16 (flags & 2; 16-byte
+// vector stores when flags & 4).
+template <int BN>
+__device__ __forceinline__ void epilogue_store(uint32_t tmem, int q, int a, int lane, int m0, int n0, int M, int N,
+                                               int ldc, void* Cz, const float* __restrict__ bias, int flags) {
+    const int row = m0 + q * 32 + lane;
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN + c0);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+              "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+              "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+              "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row < M && (flags & 4) && n0 + c0 + 32 <= N) {
+            // whole 32-column chunk, 16-byte aligned row segment
+            float v[32];
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) {
+                v[jj] = __uint_as_float(r[jj]);
+                if (bias) v[jj] += __ldg(bias + n0 + c0 + jj);
+                if (flags & 1) v[jj] = fmaxf(v[jj], 0.f);
+            }
+            if (flags & 2) {
+                uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(Cz) + (size_t)row * ldc +
+                                                      n0 + c0);
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    uint4 w4;
+                    w4.x = pack_bf16(v[8 * qq + 0], v[8 * qq + 1]);
+                    w4.y = pack_bf16(v[8 * qq + 2], v[8 * qq + 3]);
+                    w4.z = pack_bf16(v[8 * qq + 4], v[8 * qq + 5]);
+                    w4.w = pack_bf16(v[8 * qq + 6], v[8 * qq + 7]);
+                    dst[qq] = w4;
+                }
+            } else {
+                float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(Cz) + (size_t)row * ldc + n0 +
+                                                        c0);
+#pragma unroll
+                for (int qq = 0; qq < 8; ++qq)
+                    dst[qq] = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
+            }
+        } else if (row < M) {
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) {
+                const int col = n0 + c0 + jj;
+                if (col < N) {
+                    float v = __uint_as_float(r[jj]);
+                    if (bias) v += __ldg(bias + col);
+                    if (flags & 1) v = fmaxf(v, 0.f);
+                    if (flags & 2)
+                        reinterpret_cast<__nv_bfloat16*>(Cz)[(size_t)row * ldc + col] = __float2bfloat16(v);
+                    else
+                        reinterpret_cast<float*>(Cz)[(size_t)row * ldc + col] = v;
+                }
+            }
+        }
+    }
+}
+
 // Persistent GEMM: each CTA walks output tiles t = blockIdx.x, + gridDim.x,
 // ... (tile t: n tile t % tiles_n, m tile (t / tiles_n) % tiles_m, k split
 // t / (tiles_n tiles_m)), so the tiles that run together share their A rows
@@ -327,66 +395,184 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
             const int tn = t % tiles_n, rest = t / tiles_n;
             const int m0 = (rest % tiles_m) * BM, n0 = tn * BN, z = rest / tiles_m;
             void* Cz = z ? reinterpret_cast<void*>(reinterpret_cast<float*>(C) + z * split_stride) : C;
-            const int row = m0 + q * 32 + lane;
-            for (int c0 = 0; c0 < BN; c0 += 32) {
-                uint32_t r[32];
-                const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * BN + c0);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-                    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                      "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                      "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                      "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                    : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (row < M && (flags & 4) && n0 + c0 + 32 <= N) {
-                    // whole 32-column chunk, 16-byte aligned row segment
-                    float v[32];
-#pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) {
-                        v[jj] = __uint_as_float(r[jj]);
-                        if (bias) v[jj] += __ldg(bias + n0 + c0 + jj);
-                        if (flags & 1) v[jj] = fmaxf(v[jj], 0.f);
+            epilogue_store<BN>(tmem, q, a, lane, m0, n0, M, N, ldc, Cz, bias, flags);
+            // this warp's lanes of accumulator a are read: hand it back
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_tempty + 8 * a) : "memory");
+        }
+    }
+    __syncwarp();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && *abort_flag && err) atomicExch(err, 1);
+    if (warp == 1) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN)));
+    }
+}
+
+// Implicit 3x3 convolution with the input read once per image row of a
+// tile: tiles are 128 consecutive output pixels of one image row (W % 128
+// == 0).  For each channel block cb and each ky the producer loads one halo
+// row -- input pixels w0 - 1 .. w0 + 134 of image row h + sgn (ky - 1), 64
+// channels each (a 136-row, 128-byte-row tile, zero fill outside the image)
+// -- and the MMA warp issues the three kx taps on it: the A operand of tap
+// kx is the same tile starting kx rows in (2 - kx for the transposed
+// convolution; the descriptor's 128-byte swizzle follows the absolute
+// shared-memory address, so a start offset by whole rows reads the rows
+// the TMA wrote there).  The weights of all 9 taps (N <= BN rows) stay in
+// shared memory for the whole kernel.  Same persistence, accumulator
+// double-buffering, epilogue and bounded waits as gemm_tn_kernel.
+constexpr int kHaloRows = 136;                  // 130 needed, 8-row multiple
+constexpr int kHaloBytes = 18 * 1024;           // 136 x 128 B, rounded to 1 KB
+constexpr int kHaloMaxStages = 8;
+
+template <int BN>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW, void* __restrict__ C,
+                 int M, int N, const float* __restrict__ bias, int flags, int* __restrict__ err, const ConvGeom cg,
+                 int stages) {
+    constexpr int W_TILE = BN * BK * 2;  // one (tap, channel block) weight tile
+    const int S = stages;
+    const int nw = 9 * cg.cblk;          // resident weight tiles
+    extern __shared__ uint8_t smem_dyn[];
+    const uint32_t base_s = smem_u32(smem_dyn);
+    const uint32_t pad = (1024 - (base_s & 1023)) & 1023;
+    uint8_t* smem = smem_dyn + pad;
+    const uint32_t sW = smem_u32(smem);
+    const uint32_t sR = sW + nw * W_TILE;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + nw * W_TILE + S * kHaloBytes);
+    // bars: [0, S) full, [S, 2S) empty, accumulator full x2, empty x2,
+    // drain, weights; then the tmem slot and an abort flag
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * S + 6);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const uint32_t bar_full = smem_u32(bars);
+    const uint32_t bar_empty = bar_full + 8 * S;
+    const uint32_t bar_tfull = bar_full + 16 * S;
+    const uint32_t bar_tempty = bar_tfull + 16;
+    const uint32_t bar_drain = bar_tempty + 16;
+    const uint32_t bar_w = bar_drain + 8;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = M / BM;
+    const int steps = 3 * cg.cblk;  // halo rows per tile
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            mbar_init(bar_full + 8 * s, 1);
+            mbar_init(bar_empty + 8 * s, 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(bar_tfull + 8 * a, 1);
+            mbar_init(bar_tempty + 8 * a, 4);
+        }
+        mbar_init(bar_drain, 1);
+        mbar_init(bar_w, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)(2 * BN)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // the weights: tile g = tap * cblk + cb is columns g * 64 .. + 63
+            mbar_expect_tx(bar_w, (uint32_t)(nw * W_TILE));
+            for (int g = 0; g < nw; ++g) tma_load_2d(sW + g * W_TILE, &tmW, bar_w, g * BK, 0);
+            uint32_t it = 0;
+            bool ok = true;
+            const int hw = cg.H * cg.W;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+                const int m0 = t * BM;
+                const int img = m0 / hw, r = m0 - img * hw;
+                const int h = r / cg.W, w0 = r - h * cg.W;
+                for (int st = 0; st < steps; ++st, ++it) {
+                    const int s = (int)(it % S);
+                    if ((it >= (uint32_t)S && !mbar_wait(bar_empty + 8 * s, ((it / S) - 1) & 1)) || *abort_flag) {
+                        ok = false;
+                        break;
                     }
-                    if (flags & 2) {
-                        uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(Cz) + (size_t)row * ldc +
-                                                              n0 + c0);
-#pragma unroll
-                        for (int qq = 0; qq < 4; ++qq) {
-                            uint4 w4;
-                            w4.x = pack_bf16(v[8 * qq + 0], v[8 * qq + 1]);
-                            w4.y = pack_bf16(v[8 * qq + 2], v[8 * qq + 3]);
-                            w4.z = pack_bf16(v[8 * qq + 4], v[8 * qq + 5]);
-                            w4.w = pack_bf16(v[8 * qq + 6], v[8 * qq + 7]);
-                            dst[qq] = w4;
-                        }
-                    } else {
-                        float4* dst = reinterpret_cast<float4*>(reinterpret_cast<float*>(Cz) + (size_t)row * ldc + n0 +
-                                                                c0);
-#pragma unroll
-                        for (int qq = 0; qq < 8; ++qq)
-                            dst[qq] = make_float4(v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3]);
-                    }
-                } else if (row < M) {
-#pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) {
-                        const int col = n0 + c0 + jj;
-                        if (col < N) {
-                            float v = __uint_as_float(r[jj]);
-                            if (bias) v += __ldg(bias + col);
-                            if (flags & 1) v = fmaxf(v, 0.f);
-                            if (flags & 2)
-                                reinterpret_cast<__nv_bfloat16*>(Cz)[(size_t)row * ldc + col] = __float2bfloat16(v);
-                            else
-                                reinterpret_cast<float*>(Cz)[(size_t)row * ldc + col] = v;
-                        }
-                    }
+                    const int cb = st / 3, ky = st - cb * 3;
+                    mbar_expect_tx(bar_full + 8 * s, kHaloRows * BK * 2);
+                    tma_load_4d(sR + s * kHaloBytes, &tmX, bar_full + 8 * s, cb * BK, w0 - 1, h + cg.sgn * (ky - 1),
+                                img);
                 }
             }
-            // this warp's lanes of accumulator a are read: hand it back
+            if (!ok) *abort_flag = 1;
+            for (uint32_t j = it > (uint32_t)S ? it - S : 0u; j < it; ++j)
+                mbar_wait(bar_full + 8 * (j % S), (j / S) & 1);
+            mbar_wait(bar_w, 0);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(BM, BN);
+            bool ok = mbar_wait(bar_w, 0);
+            uint32_t it = 0;
+            int j = 0;
+            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++j) {
+                const int a = j & 1, u = j >> 1;
+                if (j >= 2 && !mbar_wait(bar_tempty + 8 * a, (u - 1) & 1)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t dacc = tmem + (uint32_t)(a * BN);
+                for (int st = 0; st < steps; ++st, ++it) {
+                    const int s = (int)(it % S);
+                    if (!mbar_wait(bar_full + 8 * s, (it / S) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const int cb = st / 3, ky = st - cb * 3;
+                    const uint32_t halo = sR + s * kHaloBytes;
+#pragma unroll
+                    for (int kx = 0; kx < 3; ++kx) {
+                        const int off = cg.sgn > 0 ? kx : 2 - kx;
+                        const uint32_t wt = sW + ((ky * 3 + kx) * cg.cblk + cb) * W_TILE;
+#pragma unroll
+                        for (int k = 0; k < BK / 16; ++k) {
+                            const uint64_t da = sw128_desc(halo + off * 128 + k * 32);
+                            const uint64_t db = sw128_desc(wt + k * 32);
+                            const uint32_t acc = (st > 0 || kx > 0 || k > 0) ? 1u : 0u;
+                            asm volatile(
+                                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                                ::"r"(dacc), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                        }
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                                 ::"r"(bar_empty + 8 * s) : "memory");
+                }
+                if (!ok) break;
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                             ::"r"(bar_tfull + 8 * a) : "memory");
+            }
+            if (!ok) *abort_flag = 1;
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                         ::"r"(bar_drain) : "memory");
+            mbar_wait(bar_drain, 0);
+        }
+    } else {
+        const int q = warp & 3;
+        int j = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++j) {
+            const int a = j & 1, u = j >> 1;
+            const bool ready = __all_sync(0xffffffffu, mbar_wait(bar_tfull + 8 * a, u & 1));
+            if (!ready || *abort_flag) {
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            epilogue_store<BN>(tmem, q, a, lane, t * BM, 0, M, N, N, C, bias, flags);
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_tempty + 8 * a) : "memory");
@@ -499,6 +685,50 @@ __global__ void wgrad_sum_kernel(const float* __restrict__ work, float* __restri
         for (int z = 0; z < splits; ++z) acc += work[z * mn + row * N + n];
         dW[(int64_t)n * ldw + q] = acc;
     }
+}
+
+// NHWC activations as the 4-D tensor {C, W, H, B} with a halo box {64
+// channels, 136 pixels, 1, 1}.
+int make_map_halo(CUtensorMap* map, const void* base, int B, int H, int W, int C) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_error(KGB_ERR_CUDA, "conv: cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)kHaloRows, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(KGB_ERR_VALUE, "conv: tensor map rejected (CUresult %d)", (int)r);
+    return KGB_OK;
+}
+
+int sm_count();
+
+constexpr size_t kSmemLimit = 227 * 1024;
+
+// shared memory of conv_halo_kernel with `stages` halo rows
+size_t halo_smem(int BN, int cblk, int stages) {
+    return 1024 + (size_t)9 * cblk * BN * BK * 2 + (size_t)stages * kHaloBytes + 8 * (2 * stages + 6) + 16;
+}
+
+// halo rows that fit next to the resident weights (0 if fewer than 3)
+int halo_stages(int BN, int cblk) {
+    for (int st = kHaloMaxStages; st >= 3; --st)
+        if (halo_smem(BN, cblk, st) <= kSmemLimit) return st;
+    return 0;
+}
+
+template <int BN>
+int halo_launch(const CUtensorMap& mx, const CUtensorMap& mw, void* y, int M, int N, const float* bias, int flags,
+                int* err, const ConvGeom& cg, int stages, cudaStream_t s) {
+    const size_t smem = halo_smem(BN, cg.cblk, stages);
+    KGB_CUDA_TRY(cudaFuncSetAttribute(conv_halo_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int ntiles = M / BM;
+    const int grid = std::min(ntiles, sm_count());
+    conv_halo_kernel<BN><<<grid, kGemmThreads, smem, s>>>(mx, mw, y, M, N, bias, flags, err, cg, stages);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
 }
 
 template <int BN>
@@ -643,6 +873,18 @@ extern "C" int kgb_conv3x3_bf16(const void* x, const void* w, void* y, int B, in
     const int BN = N <= 64 ? 64 : 128;
     CUtensorMap ma, mb;
     int rc;
+    // rows of whole 128-pixel segments, one N tile, weights resident: read
+    // each input row once per tile (conv_halo_kernel)
+    const int hstages = W % BM == 0 && N <= 128 ? halo_stages(BN, cblk) : 0;
+    if (hstages) {
+        if ((rc = make_map_halo(&ma, x, B, H, W, C))) return rc;
+        if ((rc = make_map(&mb, w, N, K, K, BN))) return rc;
+        flags = (flags & 3) | vector_flag(y, N, flags);
+        const ConvGeom hg{H, W, cblk, flip ? -1 : 1, B};
+        cudaStream_t hs = (cudaStream_t)stream;
+        if (BN == 64) return halo_launch<64>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, hstages, hs);
+        return halo_launch<128>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, hstages, hs);
+    }
     if ((rc = make_map_nhwc(&ma, x, B, H, W, C, bw, bh))) return rc;
     if ((rc = make_map(&mb, w, N, K, K, BN))) return rc;
     flags = (flags & 3) | vector_flag(y, N, flags);

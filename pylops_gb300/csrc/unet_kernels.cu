@@ -25,6 +25,12 @@ typedef __nv_bfloat16 bf16;
 
 int grid_for(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 16 * 152)); }
 
+// two floats rounded to bf16 (round to nearest even), low half first
+__device__ __forceinline__ uint32_t pack_bf16_pair(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
 // Source pixel of destination pixel (hd, wd) for tap (ky, kx).  Forward
 // unfold: hs = hd*s + ky - pad.  Transposed unfold: hd = hs*s + ky - pad.
 template <bool TRANS>
@@ -208,7 +214,10 @@ __global__ void unfold_t_small_kernel(const bf16* __restrict__ x, bf16* __restri
 // stores along columns.
 __global__ void row_transpose_kernel(const bf16* __restrict__ src, bf16* __restrict__ dst, int64_t R, int W, int C,
                                      int shifts) {
-    __shared__ __align__(16) unsigned short tile[66][40];  // [w - w0 + 1][c - c0], rows of 80 bytes
+    // channel-major staging [c - c0][w - (w0 + lo)], 33 words per row: the
+    // scalar writes of the load phase and the reads of the store phase fall
+    // in distinct banks across a warp
+    __shared__ unsigned short tile[32][66];
     const int wb = (W + 63) / 64, cb = (C + 31) / 32;
     const int64_t items = R * wb * cb;
     const int lo = shifts == 3 ? -1 : 0;
@@ -226,26 +235,195 @@ __global__ void row_transpose_kernel(const bf16* __restrict__ src, bf16* __restr
             const int w = w0 + lo + j, c = c0 + 8 * q;
             uint4 v = make_uint4(0, 0, 0, 0);
             if (w >= 0 && w < W && c < C) v = __ldg(s4 + ((r * W + w) * C + c) / 8);
-            *reinterpret_cast<uint4*>(&tile[j][8 * q]) = v;
+            const uint32_t wd[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i) tile[8 * q + i][j] = (unsigned short)(wd[i >> 1] >> (16 * (i & 1)));
         }
         __syncthreads();
-        // 8 columns (16 bytes) per store; channels fastest across a warp, so
-        // the shared-memory reads of a warp fall in one tile row
+        // 8 columns (16 bytes) per store; a warp writes 4 channels x 64
+        // columns, i.e. four whole 128-byte row segments
         for (int e = threadIdx.x; e < shifts * 32 * 8; e += blockDim.x) {
-            const int sh = e >> 8, cc = e & 31, w8 = (e >> 5) & 7;
+            const int w8 = e & 7, cc = (e >> 3) & 31, sh = e >> 8;
             const int c = c0 + cc, w = w0 + 8 * w8;
             if (c >= C || w >= W) continue;
-            // tile row of output column w + k: (w + k + sh - 1) - (w0 - 1) = 8 w8 + k + sh
+            // staged column of output column w + k: (w + k + sh - 1) - (w0 - 1) = 8 w8 + k + sh
             // (shifts = 3), (w + k) - w0 = 8 w8 + k (shifts = 1); W % 8 == 0, so w + 8 <= W
-            const int jb = shifts == 3 ? 8 * w8 + sh : 8 * w8;
+            const unsigned short* t = &tile[cc][shifts == 3 ? 8 * w8 + sh : 8 * w8];
             uint4 o;
-            o.x = (uint32_t)tile[jb + 0][cc] | ((uint32_t)tile[jb + 1][cc] << 16);
-            o.y = (uint32_t)tile[jb + 2][cc] | ((uint32_t)tile[jb + 3][cc] << 16);
-            o.z = (uint32_t)tile[jb + 4][cc] | ((uint32_t)tile[jb + 5][cc] << 16);
-            o.w = (uint32_t)tile[jb + 6][cc] | ((uint32_t)tile[jb + 7][cc] << 16);
+            o.x = (uint32_t)t[0] | ((uint32_t)t[1] << 16);
+            o.y = (uint32_t)t[2] | ((uint32_t)t[3] << 16);
+            o.z = (uint32_t)t[4] | ((uint32_t)t[5] << 16);
+            o.w = (uint32_t)t[6] | ((uint32_t)t[7] << 16);
             *reinterpret_cast<uint4*>(dst + ((r * shifts + sh) * C + c) * W + w) = o;
         }
     }
+}
+
+// Column sums of a bf16 matrix g (rows x cols, cols % 8 == 0, cols <= 256),
+// each row optionally weighted by wt[r] (bf16): the bias gradient straight
+// from the NHWC output gradient, or (weighted) the weight gradient of a 1x1
+// convolution to one channel.  Block k sums
+// rows [k chunk, (k + 1) chunk): thread (phase, column group) adds 8
+// columns (one 16-byte load) of rows r0 + phase, r0 + phase + nph, ... in
+// order; the phases are added in order into work[k][c], and colsum_final
+// adds the blocks in order, so the sums are deterministic.
+constexpr int kColChunks = 1024;
+__device__ __forceinline__ float bf16_bits(uint32_t h) { return __uint_as_float(h << 16); }
+
+__global__ void __launch_bounds__(256) colsum_partial_kernel(const bf16* __restrict__ g, const bf16* __restrict__ wt,
+                                                             float* __restrict__ work, int64_t rows, int cols) {
+    __shared__ float part[8 * 256];
+    const int ng = cols >> 3;                 // 16-byte column groups
+    const int nph = blockDim.x / ng;          // row phases
+    const int ph = threadIdx.x / ng, cg = threadIdx.x - ph * ng;
+    const int64_t chunk = (rows + kColChunks - 1) / kColChunks;
+    const int64_t r0 = (int64_t)blockIdx.x * chunk, r1 = min(rows, r0 + chunk);
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (ph < nph) {
+        for (int64_t rr = r0 + ph; rr < r1; rr += nph) {
+            const uint4 u = __ldg(reinterpret_cast<const uint4*>(g + rr * cols) + cg);
+            const uint32_t wd[4] = {u.x, u.y, u.z, u.w};
+            const float f = wt ? __bfloat162float(wt[rr]) : 1.f;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] += f * bf16_bits((wd[i >> 1] >> (16 * (i & 1))) & 0xffffu);
+        }
+        for (int i = 0; i < 8; ++i) part[ph * cols + cg * 8 + i] = acc[i];
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < cols; c += blockDim.x) {
+        float sum = 0.f;
+        for (int k = 0; k < nph; ++k) sum += part[k * cols + c];
+        work[(int64_t)blockIdx.x * cols + c] = sum;
+    }
+}
+
+// one warp per column: lane l adds blocks l, l + 32, ... in order, then a
+// fixed butterfly over the lanes
+__global__ void colsum_final_kernel(const float* __restrict__ work, float* __restrict__ out, int cols) {
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (c >= cols) return;
+    float acc = 0.f;
+    for (int k = lane; k < kColChunks; k += 32) acc += work[(int64_t)k * cols + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[c] = acc;
+}
+
+// 1x1 convolution to one channel (the network's head): y[p] = b + sum_c
+// w[c] x[p][c], x NHWC bf16 with C % 8 == 0, w bf16, fp32 accumulation.
+__global__ void head_forward_kernel(const uint4* __restrict__ x, const bf16* __restrict__ w, const float* __restrict__ b,
+                                    float* __restrict__ y, int64_t P, int C) {
+    __shared__ float wsh[256];
+    for (int c = threadIdx.x; c < C; c += blockDim.x) wsh[c] = __bfloat162float(w[c]);
+    __syncthreads();
+    const float bias = b ? b[0] : 0.f;
+    const int G = C >> 3;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        for (int gI = 0; gI < G; ++gI) {
+            const uint4 u = __ldg(x + p * G + gI);
+            const uint32_t wd[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc += wsh[8 * gI + i] * bf16_bits((wd[i >> 1] >> (16 * (i & 1))) & 0xffffu);
+        }
+        y[p] = acc + bias;
+    }
+}
+
+// Its data gradient: dx[p][c] = g[p] w[c] (float32), 4 channels per thread.
+__global__ void head_dx_kernel(const bf16* __restrict__ g, const bf16* __restrict__ w, float4* __restrict__ dx,
+                               int64_t P, int C) {
+    __shared__ float wsh[256];
+    for (int c = threadIdx.x; c < C; c += blockDim.x) wsh[c] = __bfloat162float(w[c]);
+    __syncthreads();
+    const int Q = C >> 2;
+    const int64_t total = P * Q;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = i / Q;
+        const int q = (int)(i - p * Q);
+        const float gv = __bfloat162float(g[p]);
+        dx[i] = make_float4(gv * wsh[4 * q], gv * wsh[4 * q + 1], gv * wsh[4 * q + 2], gv * wsh[4 * q + 3]);
+    }
+}
+
+// 3x3 convolution of a one-channel image (the network's first layer), zero
+// padding 1: y[p][n] = act(b[n] + sum_t w[n][t] x[p + off(t)]) as bf16, w
+// bf16 with row stride kpad (tap t = 3 ky + kx), N % 8 == 0, N <= 128;
+// fp32 accumulation, one pixel per thread.
+__global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restrict__ w, const float* __restrict__ b,
+                               uint4* __restrict__ y, int B, int H, int W, int N, int kpad, int relu) {
+    __shared__ float wsh[128 * 9], bsh[128];
+    for (int k = threadIdx.x; k < N * 9; k += blockDim.x) wsh[k] = __bfloat162float(w[(k / 9) * kpad + k % 9]);
+    for (int k = threadIdx.x; k < N; k += blockDim.x) bsh[k] = b ? b[k] : 0.f;
+    __syncthreads();
+    const int64_t P = (int64_t)B * H * W;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+        const int wi = (int)(p % W);
+        const int64_t t = p / W;
+        const int hi = (int)(t % H);
+        float v[9];
+#pragma unroll
+        for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+            for (int kx = 0; kx < 3; ++kx) {
+                const int hh = hi + ky - 1, ww = wi + kx - 1;
+                v[ky * 3 + kx] = (hh >= 0 && hh < H && ww >= 0 && ww < W)
+                                     ? __bfloat162float(x[p + (int64_t)(ky - 1) * W + (kx - 1)])
+                                     : 0.f;
+            }
+        for (int n8 = 0; n8 < N; n8 += 8) {
+            float o[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float acc = bsh[n8 + j];
+#pragma unroll
+                for (int k = 0; k < 9; ++k) acc += wsh[(n8 + j) * 9 + k] * v[k];
+                o[j] = relu ? fmaxf(acc, 0.f) : acc;
+            }
+            uint4 u;
+            u.x = pack_bf16_pair(o[0], o[1]);
+            u.y = pack_bf16_pair(o[2], o[3]);
+            u.z = pack_bf16_pair(o[4], o[5]);
+            u.w = pack_bf16_pair(o[6], o[7]);
+            y[p * (N >> 3) + (n8 >> 3)] = u;
+        }
+    }
+}
+
+// Its weight gradient: dW[n][t] = sum_p g[p][n] x[p + off(t)].  Block k sums
+// a chunk of pixels in order per (n, t) into work[k][n * 9 + t];
+// conv_c1_wgrad_final adds the chunks in a fixed order (warp per output).
+__global__ void conv_c1_wgrad_partial_kernel(const bf16* __restrict__ x, const bf16* __restrict__ g,
+                                             float* __restrict__ work, int B, int H, int W, int N) {
+    const int64_t P = (int64_t)B * H * W;
+    const int64_t chunk = (P + kColChunks - 1) / kColChunks;
+    const int64_t p0 = (int64_t)blockIdx.x * chunk, p1 = min(P, p0 + chunk);
+    const int n = threadIdx.x / 9, tt = threadIdx.x - n * 9;
+    if (n >= N) return;
+    const int ky = tt / 3, kx = tt - ky * 3;
+    float acc = 0.f;
+    // pixel coordinates advanced incrementally (no division per pixel)
+    int wi = (int)(p0 % W), hi = (int)((p0 / W) % H);
+    for (int64_t p = p0; p < p1; ++p) {
+        const int hh = hi + ky - 1, ww = wi + kx - 1;
+        if (hh >= 0 && hh < H && ww >= 0 && ww < W)
+            acc += __bfloat162float(g[p * N + n]) * __bfloat162float(x[p + (int64_t)(ky - 1) * W + (kx - 1)]);
+        if (++wi == W) {
+            wi = 0;
+            if (++hi == H) hi = 0;
+        }
+    }
+    work[(int64_t)blockIdx.x * 9 * N + threadIdx.x] = acc;
+}
+
+__global__ void conv_c1_wgrad_final_kernel(const float* __restrict__ work, float* __restrict__ dW, int N, int kpad) {
+    const int o = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (o >= 9 * N) return;
+    float acc = 0.f;
+    for (int k = lane; k < kColChunks; k += 32) acc += work[(int64_t)k * 9 * N + o];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) dW[(o / 9) * kpad + o % 9] = acc;
 }
 
 // out[c][r] = in[r][c]; rows x cols, in leading dimension ldi, out ldo.
@@ -311,6 +489,28 @@ __global__ void weights_implicit_kernel(const float* __restrict__ Wm, bf16* __re
             if (co < Cout) v = Wm[(int64_t)co * Kpad + tap * Cin + ci];
             Wti[j] = __float2bfloat16(v);
         }
+    }
+}
+
+// vector form (n % 8 == 0, 16-byte aligned): 8 elements per iteration
+__global__ void relu_grad_vec_kernel(const float4* __restrict__ dy, const uint4* __restrict__ y, uint4* __restrict__ g,
+                                     int64_t n8, int relu) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += (int64_t)gridDim.x * blockDim.x) {
+        const float4 a = __ldg(dy + 2 * i), b = __ldg(dy + 2 * i + 1);
+        float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        if (relu) {
+            const uint4 u = __ldg(y + i);
+            const uint32_t wd[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (!(__uint_as_float((wd[k >> 1] >> (16 * (k & 1))) << 16) > 0.f)) v[k] = 0.f;
+        }
+        uint4 o;
+        o.x = pack_bf16_pair(v[0], v[1]);
+        o.y = pack_bf16_pair(v[2], v[3]);
+        o.z = pack_bf16_pair(v[4], v[5]);
+        o.w = pack_bf16_pair(v[6], v[7]);
+        g[i] = o;
     }
 }
 
@@ -609,7 +809,11 @@ int kgb_unet_weights_implicit(const float* Wm, void* Wi, void* Wti, int Cout, in
 
 int kgb_unet_relu_grad(const float* dy, const void* y, void* g, int64_t n, int relu, void* stream) {
     if (!dy || !g || (relu && !y) || n <= 0) return set_error(KGB_ERR_VALUE, "unet_relu_grad: bad arguments");
-    relu_grad_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(dy, (const bf16*)y, (bf16*)g, n, relu);
+    if (n % 8 == 0 && (((uintptr_t)dy | (uintptr_t)g | (relu ? (uintptr_t)y : 0)) & 15) == 0)
+        relu_grad_vec_kernel<<<grid_for(n / 8), 256, 0, (cudaStream_t)stream>>>(
+            (const float4*)dy, (const uint4*)y, (uint4*)g, n / 8, relu);
+    else
+        relu_grad_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(dy, (const bf16*)y, (bf16*)g, n, relu);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -686,6 +890,60 @@ int kgb_unet_row_transpose(const void* src, void* dst, int B, int H, int W, int 
     const int64_t items = R * ((W + 63) / 64) * ((C + 31) / 32);
     const int grid = (int)std::min<int64_t>(items, 16 * 152);
     row_transpose_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>((const bf16*)src, (bf16*)dst, R, W, C, shifts);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_colsum(const void* g, const void* wt, float* out, int64_t rows, int cols, float* work, void* stream) {
+    if (!g || !out || !work || rows <= 0 || cols <= 0 || cols > 256 || cols % 8 || ((uintptr_t)g & 15))
+        return set_error(KGB_ERR_VALUE, "unet_colsum: bad arguments (cols a multiple of 8 up to 256, g 16-byte aligned)");
+    cudaStream_t s = (cudaStream_t)stream;
+    // 256 threads: (256 / (cols / 8)) row phases x (cols / 8) column groups
+    const int threads = (256 / (cols / 8)) * (cols / 8);
+    colsum_partial_kernel<<<kColChunks, threads, 0, s>>>((const bf16*)g, (const bf16*)wt, work, rows, cols);
+    KGB_CUDA_TRY(cudaGetLastError());
+    colsum_final_kernel<<<(cols + 7) / 8, 256, 0, s>>>(work, out, cols);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_head_forward(const void* x, const void* w, const float* bias, float* y, int64_t P, int C, void* stream) {
+    if (!x || !w || !y || P <= 0 || C <= 0 || C % 8 || C > 256 || ((uintptr_t)x & 15))
+        return set_error(KGB_ERR_VALUE, "unet_head_forward: bad arguments");
+    head_forward_kernel<<<grid_for(P), 256, 0, (cudaStream_t)stream>>>((const uint4*)x, (const bf16*)w, bias, y, P, C);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_head_dx(const void* g, const void* w, float* dx, int64_t P, int C, void* stream) {
+    if (!g || !w || !dx || P <= 0 || C <= 0 || C % 4 || C > 256 || ((uintptr_t)dx & 15))
+        return set_error(KGB_ERR_VALUE, "unet_head_dx: bad arguments");
+    head_dx_kernel<<<grid_for(P * (C / 4)), 256, 0, (cudaStream_t)stream>>>((const bf16*)g, (const bf16*)w, (float4*)dx,
+                                                                           P, C);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_conv3x3_c1(const void* x, const void* w, const void* bias, void* y, int B, int H, int W, int N, int kpad,
+                        int relu, void* stream) {
+    if (!x || !w || !y || B <= 0 || H <= 0 || W <= 0 || N <= 0 || N % 8 || N > 128 || kpad < 9 ||
+        ((uintptr_t)y & 15))
+        return set_error(KGB_ERR_VALUE, "unet_conv3x3_c1: bad arguments");
+    const int64_t P = (int64_t)B * H * W;
+    conv_c1_kernel<<<grid_for(P), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)w, (const float*)bias,
+                                                                  (uint4*)y, B, H, W, N, kpad, relu);
+    KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+int kgb_unet_conv3x3_c1_wgrad(const void* x, const void* g, float* dW, int B, int H, int W, int N, int kpad,
+                              float* work, void* stream) {
+    if (!x || !g || !dW || !work || B <= 0 || H <= 0 || W <= 0 || N <= 0 || 9 * N > 1024 || kpad < 9)
+        return set_error(KGB_ERR_VALUE, "unet_conv3x3_c1_wgrad: bad arguments");
+    cudaStream_t s = (cudaStream_t)stream;
+    conv_c1_wgrad_partial_kernel<<<kColChunks, 9 * N, 0, s>>>((const bf16*)x, (const bf16*)g, work, B, H, W, N);
+    KGB_CUDA_TRY(cudaGetLastError());
+    conv_c1_wgrad_final_kernel<<<(9 * N + 7) / 8, 256, 0, s>>>(work, dW, N, kpad);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

@@ -1,10 +1,16 @@
 """BF16 U-Net image-domain network, trained and run by this package's kernels.
 
-Every convolution (forward, weight gradient, data gradient) is a tcgen05
-tensor-core GEMM (``kgb_gemm_bf16_tn`` / ``kgb_gemm_bf16_tn_splitk``) on
-operands unfolded by ``kgb_unet_unfold`` / ``kgb_unet_unfold_t``; ReLU
-masks, bias gradients, upsampling, skip concatenation, the MSE loss and Adam
-are the ``kgb_unet_*`` kernels.  PyTorch only allocates device memory and
+The convolutions (forward, weight gradient, data gradient) run on tcgen05
+tensor-core GEMMs: 3x3 stride-1 layers as implicit convolutions
+(``kgb_conv3x3_bf16``, one halo row per tap row for image rows of 128-pixel
+multiples) and implicit weight gradients (``kgb_conv3x3_wgrad_bf16`` on
+operands transposed per image row), the stride-2 layers as GEMMs
+(``kgb_gemm_bf16_tn`` / ``kgb_gemm_bf16_tn_splitk``) on operands unfolded by
+``kgb_unet_unfold`` / ``kgb_unet_unfold_t``.  The two layers with one
+channel on a side -- the first 3x3 convolution of the one-channel input and
+the 1x1 head to one channel -- are direct kernels (a GEMM would be 1/8 or
+1/64 occupied).  ReLU masks, bias gradients, upsampling, skip concatenation,
+the MSE loss and Adam are the ``kgb_unet_*`` kernels.  PyTorch only allocates device memory and
 provides the stream.  Activations are NHWC bf16 (an image of the Kirchhoff
 model, shape (nx, nz) with z fastest, is NHWC with H = nx, W = nz, C = 1);
 gradients between layers are float32, master weights and Adam moments
@@ -75,7 +81,8 @@ class _CountingLib:
     launches (two for the split-K GEMM, the row sums and the MSE, one for
     the others)."""
 
-    _KERNELS = {"kgb_gemm_bf16_tn_splitk": 2, "kgb_unet_rowsum": 2, "kgb_unet_mse": 2, "kgb_conv3x3_wgrad_bf16": 2}
+    _KERNELS = {"kgb_gemm_bf16_tn_splitk": 2, "kgb_unet_rowsum": 2, "kgb_unet_mse": 2, "kgb_conv3x3_wgrad_bf16": 2,
+                "kgb_unet_colsum": 2, "kgb_unet_conv3x3_c1_wgrad": 2}
 
     def __init__(self, owner):
         self._owner = owner
@@ -321,6 +328,16 @@ class UNet:
         lo = ws["lvl"][i]
         (H, W), (Ho, Wo) = ws["hw"][li], ws["hw"][lo]
         P_out = ws["P"][lo]
+        if self._is_head1(c):
+            # 1x1 convolution to one channel: a dot product per pixel
+            _native.check(L.kgb_unet_head_forward(x.data_ptr(), c.Wb.data_ptr(), self._b(c).data_ptr(),
+                                                  ws["y"][i].data_ptr(), P_out, c.cin, s))
+            return
+        if self._is_first1(c):
+            # 3x3 convolution of the one-channel input: nine taps per pixel
+            _native.check(L.kgb_unet_conv3x3_c1(x.data_ptr(), c.Wb.data_ptr(), self._b(c).data_ptr(),
+                                                ws["y"][i].data_ptr(), B, H, W, c.cout, c.kpad, int(c.relu), s))
+            return
         if c.ks == 1 and c.stride == 1 and c.cin % 8 == 0:
             A, lda = x, c.cin
         elif self.implicit and c.implicit and _tileable(Ho, Wo):
@@ -338,6 +355,14 @@ class UNet:
         _native.check(L.kgb_gemm_bf16_tn(A.data_ptr(), c.Wb.data_ptr(), y.data_ptr(), P_out, c.cout, c.kpad, lda,
                                          c.kpad, c.cout, self._b(c).data_ptr(), flags, self._err.data_ptr(), s))
 
+    @staticmethod
+    def _is_head1(c: _Conv) -> bool:
+        return c.ks == 1 and c.stride == 1 and c.cout == 1 and c.cin % 8 == 0 and c.cin <= 256
+
+    @staticmethod
+    def _is_first1(c: _Conv) -> bool:
+        return c.ks == 3 and c.stride == 1 and c.cin == 1 and c.cout % 8 == 0 and c.cout <= 128
+
     def _conv_backward(self, i: int, ws, B: int, dx: Optional[object]):
         """Weight/bias gradients of conv i from ws['dy'][i]; data gradient
         into dx (float32, input pixels x cin) unless dx is None."""
@@ -351,13 +376,35 @@ class UNet:
         n = P_out * c.cout
         _native.check(L.kgb_unet_relu_grad(ws["dy"][i].data_ptr(), ws["y"][i].data_ptr() if c.relu else None,
                                            g.data_ptr(), n, int(c.relu), s))
-        if c.cout == 1:
-            gT = g
+        if self._is_head1(c):
+            # head: bias = sum g, weights = g-weighted column sums of x,
+            # data gradient g w (no unfolded copies)
+            _native.check(L.kgb_unet_rowsum(g.data_ptr(), self._db(c).data_ptr(), 1, P_out, ws["work"].data_ptr(), s))
+            _native.check(L.kgb_unet_colsum(x.data_ptr(), g.data_ptr(), self._dw(c).data_ptr(), P_out, c.cin,
+                                            ws["work"].data_ptr(), s))
+            if dx is not None:
+                _native.check(L.kgb_unet_head_dx(g.data_ptr(), c.Wb.data_ptr(), dx.data_ptr(), P_out, c.cin, s))
+            return
+        if self._is_first1(c) and dx is None:
+            _native.check(L.kgb_unet_colsum(g.data_ptr(), None, self._db(c).data_ptr(), P_out, c.cout,
+                                            ws["work"].data_ptr(), s))
+            _native.check(L.kgb_unet_conv3x3_c1_wgrad(x.data_ptr(), g.data_ptr(), self._dw(c).data_ptr(), B, H, W,
+                                                      c.cout, c.kpad, ws["work"].data_ptr(), s))
+            return
+        implicit_wgrad = (self.implicit and c.ks == 3 and c.stride == 1 and c.cin % 32 == 0 and c.cout % 8 == 0
+                          and W % 64 == 0 and c.cout <= 256)
+        if implicit_wgrad:
+            # bias gradient as column sums of g (no transposed copy needed)
+            _native.check(L.kgb_unet_colsum(g.data_ptr(), None, self._db(c).data_ptr(), P_out, c.cout,
+                                            ws["work"].data_ptr(), s))
         else:
-            _native.check(L.kgb_unet_transpose(g.data_ptr(), gT.data_ptr(), P_out, c.cout, c.cout, P_out, 0, s))
-        _native.check(L.kgb_unet_rowsum(gT.data_ptr(), self._db(c).data_ptr(), c.cout, P_out, ws["work"].data_ptr(),
-                                         s))
-        if self.implicit and c.ks == 3 and c.stride == 1 and c.cin % 32 == 0 and c.cout % 8 == 0 and W % 64 == 0:
+            if c.cout == 1:
+                gT = g
+            else:
+                _native.check(L.kgb_unet_transpose(g.data_ptr(), gT.data_ptr(), P_out, c.cout, c.cout, P_out, 0, s))
+            _native.check(L.kgb_unet_rowsum(gT.data_ptr(), self._db(c).data_ptr(), c.cout, P_out,
+                                             ws["work"].data_ptr(), s))
+        if implicit_wgrad:
             # implicit weight gradient: x and g transposed per image row (x in
             # three column-shifted copies) instead of the nine-tap unfolded copy
             gTr = ws["gTr"]

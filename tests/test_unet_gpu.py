@@ -113,9 +113,11 @@ def test_splitk_gemm_matches_fp32_reference():
 
 
 @pytest.mark.parametrize("B,H,W,C,N,flip", [(2, 16, 32, 32, 32, 0), (1, 8, 256, 96, 64, 0), (2, 32, 64, 64, 96, 1),
-                                            (1, 64, 128, 40, 128, 1)])
+                                            (1, 64, 128, 40, 128, 1), (2, 6, 256, 32, 32, 1),
+                                            (3, 2, 128, 128, 64, 0)])
 def test_implicit_conv3x3_matches_conv2d(B, H, W, C, N, flip):
-    """kgb_conv3x3_bf16 (4-D TMA boxes shifted per tap, zero fill as padding)
+    """kgb_conv3x3_bf16 (4-D TMA boxes shifted per tap, zero fill as padding;
+    for W a multiple of 128 one halo row per ky shared by the three kx taps)
     against torch conv2d on the same bf16-rounded operands; flip = 1 is the
     transposed convolution (kernel flipped in both axes)."""
     import torch.nn.functional as F
