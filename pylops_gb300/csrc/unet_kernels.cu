@@ -390,30 +390,77 @@ __global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restric
     }
 }
 
-// Its weight gradient: dW[n][t] = sum_p g[p][n] x[p + off(t)].  Block k sums
-// a chunk of pixels in order per (n, t) into work[k][n * 9 + t];
-// conv_c1_wgrad_final adds the chunks in a fixed order (warp per output).
-__global__ void conv_c1_wgrad_partial_kernel(const bf16* __restrict__ x, const bf16* __restrict__ g,
-                                             float* __restrict__ work, int B, int H, int W, int N) {
-    const int64_t P = (int64_t)B * H * W;
-    const int64_t chunk = (P + kColChunks - 1) / kColChunks;
-    const int64_t p0 = (int64_t)blockIdx.x * chunk, p1 = min(P, p0 + chunk);
-    const int n = threadIdx.x / 9, tt = threadIdx.x - n * 9;
-    if (n >= N) return;
-    const int ky = tt / 3, kx = tt - ky * 3;
-    float acc = 0.f;
-    // pixel coordinates advanced incrementally (no division per pixel)
-    int wi = (int)(p0 % W), hi = (int)((p0 / W) % H);
-    for (int64_t p = p0; p < p1; ++p) {
-        const int hh = hi + ky - 1, ww = wi + kx - 1;
-        if (hh >= 0 && hh < H && ww >= 0 && ww < W)
-            acc += __bfloat162float(g[p * N + n]) * __bfloat162float(x[p + (int64_t)(ky - 1) * W + (kx - 1)]);
-        if (++wi == W) {
-            wi = 0;
-            if (++hi == H) hi = 0;
+// Its weight gradient: dW[n][t] = sum_p g[p][n] x[p + off(t)].  Block k
+// takes image rows [k rpb, (k + 1) rpb); warp w of the block the rows k rpb
+// + w, + 4, ...; lane l the output channels l, l + 32, ... (N <= 128) with
+// nine tap accumulators each, walking the row with a sliding 3 x 3 window
+// of x.  The warps' sums are added in warp order into work[k][n * 9 + t];
+// conv_c1_wgrad_final adds the blocks in a fixed order (warp per output).
+constexpr int kC1Warps = 4;
+__global__ void __launch_bounds__(32 * kC1Warps) conv_c1_wgrad_partial_kernel(const bf16* __restrict__ x,
+                                                                             const bf16* __restrict__ g,
+                                                                             float* __restrict__ work, int B, int H,
+                                                                             int W, int N) {
+    __shared__ float red[kC1Warps][128 * 9];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t R = (int64_t)B * H;
+    const int64_t rpb = (R + kColChunks - 1) / kColChunks;
+    const int64_t r0 = (int64_t)blockIdx.x * rpb, r1 = min(R, r0 + rpb);
+    const int ng = (N + 31) / 32;  // channel groups per lane (N <= 128)
+    float acc[4][9];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int t = 0; t < 9; ++t) acc[q][t] = 0.f;
+    for (int64_t r = r0 + warp; r < r1; r += kC1Warps) {
+        const int h = (int)(r % H);
+        const bf16* xr = x + r * W;  // row h of image r / H
+        const bool up = h > 0, dn = h + 1 < H;
+        auto xv = [&](int dy, int w) -> float {
+            if (w < 0 || w >= W || (dy < 0 && !up) || (dy > 0 && !dn)) return 0.f;
+            return __bfloat162float(xr[(int64_t)dy * W + w]);
+        };
+        // window v[dy][dx] = x at (h + dy - 1, w + dx - 1)
+        float v[3][3];
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy) {
+            v[dy][0] = 0.f;
+            v[dy][1] = xv(dy - 1, 0);
+            v[dy][2] = xv(dy - 1, 1);
+        }
+        for (int w = 0; w < W; ++w) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int n = lane + 32 * q;
+                if (q < ng && n < N) {
+                    const float gv = __bfloat162float(g[(r * W + w) * N + n]);
+#pragma unroll
+                    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                        for (int dx = 0; dx < 3; ++dx) acc[q][dy * 3 + dx] += gv * v[dy][dx];
+                }
+            }
+#pragma unroll
+            for (int dy = 0; dy < 3; ++dy) {
+                v[dy][0] = v[dy][1];
+                v[dy][1] = v[dy][2];
+                v[dy][2] = xv(dy - 1, w + 2);
+            }
         }
     }
-    work[(int64_t)blockIdx.x * 9 * N + threadIdx.x] = acc;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int n = lane + 32 * q;
+        if (q < ng && n < N)
+#pragma unroll
+            for (int t = 0; t < 9; ++t) red[warp][n * 9 + t] = acc[q][t];
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < 9 * N; o += blockDim.x) {
+        float sum = 0.f;
+        for (int k = 0; k < kC1Warps; ++k) sum += red[k][o];
+        work[(int64_t)blockIdx.x * 9 * N + o] = sum;
+    }
 }
 
 __global__ void conv_c1_wgrad_final_kernel(const float* __restrict__ work, float* __restrict__ dW, int N, int kpad) {
@@ -938,10 +985,10 @@ int kgb_unet_conv3x3_c1(const void* x, const void* w, const void* bias, void* y,
 
 int kgb_unet_conv3x3_c1_wgrad(const void* x, const void* g, float* dW, int B, int H, int W, int N, int kpad,
                               float* work, void* stream) {
-    if (!x || !g || !dW || !work || B <= 0 || H <= 0 || W <= 0 || N <= 0 || 9 * N > 1024 || kpad < 9)
-        return set_error(KGB_ERR_VALUE, "unet_conv3x3_c1_wgrad: bad arguments");
+    if (!x || !g || !dW || !work || B <= 0 || H <= 0 || W <= 0 || N <= 0 || N > 128 || kpad < 9)
+        return set_error(KGB_ERR_VALUE, "unet_conv3x3_c1_wgrad: bad arguments (N <= 128)");
     cudaStream_t s = (cudaStream_t)stream;
-    conv_c1_wgrad_partial_kernel<<<kColChunks, 9 * N, 0, s>>>((const bf16*)x, (const bf16*)g, work, B, H, W, N);
+    conv_c1_wgrad_partial_kernel<<<kColChunks, 32 * kC1Warps, 0, s>>>((const bf16*)x, (const bf16*)g, work, B, H, W, N);
     KGB_CUDA_TRY(cudaGetLastError());
     conv_c1_wgrad_final_kernel<<<(9 * N + 7) / 8, 256, 0, s>>>(work, dW, N, kpad);
     KGB_CUDA_TRY(cudaGetLastError());
