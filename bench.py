@@ -844,7 +844,7 @@ def run_unet(args):
         "config": {"workload": "unet4x32_train_batch8_512x256", "flops_per_step": flops,
                    "l2": "activations and unfold buffers larger than L2"},
         "images_per_s": round(B / step, 1), "inference_ms_per_image": round(inf_ms, 3),
-        "roofline": {"bound": "tensor", "kernel": "training step (tcgen05 GEMMs + unfold kernels)",
+        "roofline": {"bound": "tensor", "kernel": "training step (tcgen05 implicit convolutions, weight-gradient GEMMs and helper kernels)",
                      "achieved": round(ach, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(ach / peak, 4),
                      "traffic": None},
         "e2e": {"value": round(flops / e2e / 1e12, 2), "unit": "TFLOP/s", "h2d_bytes_per_step": 2 * x.numel() * 4,
@@ -1110,7 +1110,7 @@ def lsm_record(args, n_test, variants, with_cpu):
                                           "inference_ms")},
         "e2e": {"value": round(e2e, 4), "unit": "s", "h2d_bytes_per_step": int(op.shape[0] * 4),
                 "d2h_bytes_per_step": int(op.shape[1] * 4)},
-        "roofline": {"bound": "tensor", "kernel": "U-Net training step (tcgen05 GEMMs + unfold)",
+        "roofline": {"bound": "tensor", "kernel": "U-Net training step (tcgen05 implicit convolutions, weight-gradient GEMMs and helper kernels)",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "TFLOP/s",
                      "frac": round(achieved / peak, 4), "traffic": None},
         "gpu_launches": int(v["learned"]["gpu_launches_median"]),
