@@ -104,7 +104,7 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_srcs_host,
 
 /* Build the tables on the device instead of uploading them: mode 0 =
  * analytic (constant velocity *vel, nvel = 1; 2-D or 3-D), mode 1 = eikonal
- * (2-D; vel of ni values in the image order, or one constant), on the
+ * (2-D or 3-D; vel of ni values in the image order, or one constant), on the
  * operator's grid given by its axes (y of ny samples in 3-D, else NULL; x;
  * z) with sources and receivers (ndim, ns) / (ndim, nr) in the reference's
  * coordinate order ((x, z) or (y, x, z)).  Traveltimes, distances, their
@@ -114,8 +114,10 @@ int kgb_kirchhoff_set_dynamic(kgb_kirchhoff* op, const double* amp_srcs_host,
  * and six/rix as in kgb_kirchhoff_set_dynamic.  *maxdist_out receives
  * 1e-2 (max dist_s + max dist_r).  The float64 rows stay on the device for
  * kgb_kirchhoff_get_table.  Eikonal tables solve the fast-marching
- * equations of kgb_eikonal_tables by sweeping; they agree with it to
- * rounding where both converge to the same upwind solution.
+ * equations of kgb_eikonal_tables by sweeping (float32 local solves relative
+ * to the smallest neighbour); they agree with it to ~1e-7 of the largest
+ * time where marching and sweeping pick the same upwind stencils and to
+ * ~6e-5 elsewhere.
  * Replaces: Kirchhoff._traveltime_table and the table set-up of
  * Kirchhoff.__init__ (kirchhoff.py:303-393, 503-657); the eikonal solves
  * replace scikit-fmm's travel_time / distance (kirchhoff.py:609-638). */

@@ -700,7 +700,6 @@ int kgb_kirchhoff_build_tables(kgb_kirchhoff* op, int mode, int ndim, const doub
     if (nx < 1 || nz < 1 || ny < 1 || (int64_t)ny * nx * nz != op->ni || nz != op->nz)
         return set_error(KGB_ERR_VALUE, "build_tables: grid %d x %d x %d does not match the operator", ny, nx, nz);
     if (mode == 0 && nvel != 1) return set_error(KGB_ERR_VALUE, "vel must be scalar for mode=analytical");
-    if (mode == 1 && ndim != 2) return set_error(KGB_ERR_NOT_IMPLEMENTED, "build_tables: device eikonal tables are 2-D");
     if (mode == 1 && nvel != op->ni && nvel != 1) return set_error(KGB_ERR_VALUE, "build_tables: velocity size");
     if (nvel != 1 && nvel != op->ni) return set_error(KGB_ERR_VALUE, "build_tables: velocity size");
     for (int64_t k = 0; k < nvel; ++k)
@@ -739,20 +738,25 @@ int kgb_kirchhoff_build_tables(kgb_kirchhoff* op, int mode, int ndim, const doub
         if ((rc = launch_analytic_rows(g, dy.p, dx.p, dz.p, pr.p, nr, vel[0], op->trav64_r, op->dist64_r, nullptr)))
             return rc;
     } else {
-        // grid coordinates of the points: round((p - origin) / spacing) (kirchhoff.py:615, 627)
-        // sources, then receivers
-        std::vector<int> pts(2 * ((size_t)ns + nr));
+        // grid coordinates of the points, sources then receivers:
+        // round((p - origin) / spacing) (kirchhoff.py:615, 627); (x, z) in
+        // 2-D, (y, x, z) in 3-D
+        const int nd = ndim;
+        std::vector<int> pts((size_t)nd * ((size_t)ns + nr));
         auto coords = [&](const double* p, int np, int* out) {
             for (int k = 0; k < np; ++k) {
-                const double cx = nearbyint((p[k] - xax[0]) / g.hx);
-                const double cz = nearbyint((p[np + k] - zax[0]) / g.hz);
-                if (!(cx >= 0 && cx < nx && cz >= 0 && cz < nz)) return false;
-                out[2 * k] = (int)cx;
-                out[2 * k + 1] = (int)cz;
+                const double cx = nearbyint((p[(nd - 2) * (size_t)np + k] - xax[0]) / g.hx);
+                const double cz = nearbyint((p[(nd - 1) * (size_t)np + k] - zax[0]) / g.hz);
+                const double cy = nd == 3 ? nearbyint((p[k] - yax[0]) / g.hy) : 0.0;
+                if (!(cx >= 0 && cx < nx && cz >= 0 && cz < nz && cy >= 0 && cy < ny)) return false;
+                int* o = out + (size_t)nd * k;
+                if (nd == 3) *o++ = (int)cy;
+                o[0] = (int)cx;
+                o[1] = (int)cz;
             }
             return true;
         };
-        if (!coords(srcs, ns, pts.data()) || !coords(recs, nr, pts.data() + 2 * (size_t)ns))
+        if (!coords(srcs, ns, pts.data()) || !coords(recs, nr, pts.data() + (size_t)nd * ns))
             return set_error(KGB_ERR_VALUE, "build_tables: a source or receiver lies outside the grid");
         DevBuf<int> dp;
         DevBuf<double> sp, corner;

@@ -8,11 +8,11 @@
 //  * analytic: dist^2 = (X - px)^2 + (Z - pz)^2 (+ (Y - py)^2), trav =
 //    sqrt(dist^2)/v, dist = trav*v, in the reference's order of operations
 //    (kirchhoff.py:576-607), so the rows equal numpy's bit for bit;
-//  * eikonal (2-D): the fast-marching equations of the package's host
+//  * eikonal (2-D and 3-D): the fast-marching equations of the package's host
 //    solver (eikonal.cpp, the method scikit-fmm implements) solved by
-//    Gauss-Seidel sweeps in the four diagonal orders until no value
-//    changes: one CTA per table, anti-diagonals of the sweep in parallel
-//    (their points do not neighbour one another), the same upwind
+//    Gauss-Seidel sweeps in the 4 (2-D) or 8 (3-D) diagonal orders until no
+//    value changes: one CTA per table, anti-diagonal lines (planes) of the
+//    sweep in parallel (their points do not neighbour one another), the same upwind
 //    second-order local solver; distances (unit speed) from one table of a
 //    point at the grid's corner, shifted to each point;
 //  * gradients: numpy.gradient with the sample spacing (central differences
@@ -232,6 +232,141 @@ eikonal_sweep_kernel(int n0, int n1, double h0, double h1, const double* __restr
     }
 }
 
+// 3-D: the same emulation of fast marching with up to three axes, sorted by
+// their values e1 <= e2 <= e3 (ties: lower axis first): the smallest of the
+// updates with {e1}, {e1, e2} and {e1, e2, e3}, each second order where the
+// stencil allows it and counting when the root is not below any axis value
+// (what marching computes as those neighbours are accepted in turn).  Same
+// float form relative to r = the e1 value.
+__device__ double ek_update3(const double* T, const int* n, const int64_t* st, const float* ih, const int* c,
+                             float rhs) {
+    const int64_t k = c[0] * st[0] + c[1] * st[1] + c[2] * st[2];
+    double b[3], s2[3] = {0.0, 0.0, 0.0};
+    bool h2[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ek_axis(T, k, c[a], n[a], st[a], &b[a], &s2[a], &h2[a]);
+    int idx[3], m = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        if (t_finite(b[a])) idx[m++] = a;
+    if (m == 0) return INFINITY;
+    // insertion sort of the finite axes by value (stable: ties keep axis order)
+    for (int i = 1; i < m; ++i)
+        for (int j = i; j > 0 && t_less(b[idx[j]], b[idx[j - 1]]); --j) {
+            const int t = idx[j];
+            idx[j] = idx[j - 1];
+            idx[j - 1] = t;
+        }
+    const double r = b[idx[0]];
+    float cc[3], bb[3];
+    for (int i = 0; i < m; ++i) {
+        const int a = idx[i];
+        const float d1 = (float)(b[a] - r);
+        cc[i] = h2[a] ? 2.25f * ih[a] : ih[a];
+        bb[i] = h2[a] ? (4.f * d1 - (float)(s2[a] - r)) * (1.f / 3.f) : d1;
+    }
+    float d = bb[0] + sqrtf(rhs / cc[0]);
+    for (int q = 2; q <= m; ++q) {
+        float A = 0.f, B = 0.f, C = -rhs, bm = -INFINITY;
+        for (int i = 0; i < q; ++i) {
+            A += cc[i];
+            B += cc[i] * bb[i];
+            C += cc[i] * bb[i] * bb[i];
+            bm = fmaxf(bm, bb[i]);
+        }
+        const float disc = B * B - A * C;
+        if (disc >= 0.f) {
+            const float t = (B + sqrtf(disc)) / A;
+            if (t >= bm && t < d) d = t;
+        }
+    }
+    return r + (double)d;
+}
+
+constexpr int kEik3Threads = 512;
+
+// 3-D tables: CTAs as in the 2-D kernel (sources, receivers, unit-speed
+// corner); anti-diagonal planes u0 + u1 + u2 = d of the 8 sweep orders.
+__global__ void __launch_bounds__(kEik3Threads, 2)
+eikonal3_sweep_kernel(int n0, int n1, int n2, double h0, double h1, double h2, const double* __restrict__ speed,
+                      const float* __restrict__ rhs, const int* __restrict__ pts, int ns, int nr, double* trav_s,
+                      double* trav_r, double* corner, unsigned* __restrict__ err) {
+    const int bidx = blockIdx.x;
+    const bool unit = bidx >= ns + nr;
+    const int64_t N = (int64_t)n0 * n1 * n2;
+    double* T = unit ? corner : bidx < ns ? trav_s + (size_t)bidx * N : trav_r + (size_t)(bidx - ns) * N;
+    const int p0 = unit ? 0 : pts[3 * bidx], p1 = unit ? 0 : pts[3 * bidx + 1], p2 = unit ? 0 : pts[3 * bidx + 2];
+    const int n[3] = {n0, n1, n2};
+    const int64_t st[3] = {(int64_t)n1 * n2, n2, 1};
+    const double hh[3] = {h0, h1, h2};
+    const float ih[3] = {(float)(1.0 / (h0 * h0)), (float)(1.0 / (h1 * h1)), (float)(1.0 / (h2 * h2))};
+    const double r0 = 0.5 / sqrt(1.0 / (h0 * h0) + 1.0 / (h1 * h1) + 1.0 / (h2 * h2));
+    auto spd = [&](int64_t i) { return unit ? 1.0 : speed[i]; };
+    auto dist1 = [&](int c0, int c1, int c2) { return abs(c0 - p0) + abs(c1 - p1) + abs(c2 - p2); };
+    for (int64_t i = threadIdx.x; i < N; i += blockDim.x) {
+        const int c0 = (int)(i / st[0]);
+        const int64_t rem = i - (int64_t)c0 * st[0];
+        const int c1 = (int)(rem / n2), c2 = (int)(rem - (int64_t)c1 * n2);
+        const int dd = dist1(c0, c1, c2);
+        double v = INFINITY;
+        if (dd == 0) v = r0 / spd(i);
+        else if (dd == 1) v = 0.5 * (c0 != p0 ? hh[0] : c1 != p1 ? hh[1] : hh[2]) / spd(i);
+        T[i] = v;
+    }
+    __shared__ int changed;
+    int sets = 0;
+    for (;;) {
+        if (threadIdx.x == 0) changed = 0;
+        __syncthreads();
+        for (int dir = 0; dir < 8; ++dir) {
+            const bool f0 = dir & 1, f1 = (dir >> 1) & 1, f2 = (dir >> 2) & 1;
+            for (int d = 0; d <= n0 + n1 + n2 - 3; ++d) {
+                // points of the plane: u1 in [lo1, hi1], u2 over [0, n2), u0 = d - u1 - u2 in range
+                const int lo1 = max(0, d - (n0 - 1) - (n2 - 1)), hi1 = min(d, n1 - 1);
+                const int64_t cnt = (int64_t)(hi1 - lo1 + 1) * n2;
+                for (int64_t j = threadIdx.x; j < cnt; j += blockDim.x) {
+                    const int u1 = lo1 + (int)(j / n2), u2 = (int)(j - (int64_t)(u1 - lo1) * n2);
+                    const int u0 = d - u1 - u2;
+                    if (u0 < 0 || u0 >= n0) continue;
+                    int c[3] = {f0 ? u0 : n0 - 1 - u0, f1 ? u1 : n1 - 1 - u1, f2 ? u2 : n2 - 1 - u2};
+                    if (dist1(c[0], c[1], c[2]) <= 1) continue;
+                    const int64_t k = c[0] * st[0] + c[1] * st[1] + c[2];
+                    const double t = ek_update3(T, n, st, ih, c, unit ? 1.f : rhs[k]);
+                    if (t_less(t, T[k])) {
+                        T[k] = t;
+                        changed = 1;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        const int cflag = changed;
+        __syncthreads();
+        if (!cflag) break;
+        if (++sets >= kEikMaxSets) {
+            if (threadIdx.x == 0) atomicExch(err, 3u);
+            break;
+        }
+    }
+}
+
+// 3-D distance rows from the corner table: row p at (i0, i1, i2) is the
+// corner table at (|i0 - p0|, |i1 - p1|, |i2 - p2|).
+__global__ void distance3_rows_kernel(int n0, int n1, int n2, const double* __restrict__ corner,
+                                      const int* __restrict__ pts, int ns, double* __restrict__ dist_s,
+                                      double* __restrict__ dist_r) {
+    const int p = blockIdx.y;
+    const int q0 = pts[3 * p], q1 = pts[3 * p + 1], q2 = pts[3 * p + 2];
+    const int64_t N = (int64_t)n0 * n1 * n2, s0 = (int64_t)n1 * n2;
+    double* out = p < ns ? dist_s + (size_t)p * N : dist_r + (size_t)(p - ns) * N;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+        const int i0 = (int)(i / s0);
+        const int64_t rem = i - (int64_t)i0 * s0;
+        const int i1 = (int)(rem / n2), i2 = (int)(rem - (int64_t)i1 * n2);
+        out[i] = corner[(int64_t)abs(i0 - q0) * s0 + (int64_t)abs(i1 - q1) * n2 + abs(i2 - q2)];
+    }
+}
+
 // Unit-speed (distance) rows: with unit speed the sweeps' solution depends
 // only on the offset from the point (every update reads the upwind side,
 // which lies between the node and the point, inside the grid), so row p at
@@ -443,20 +578,24 @@ int launch_analytic_rows(const TableGeom& g, const double* yax, const double* xa
 
 int launch_eikonal_tables(const TableGeom& g, const double* speed, float* rhs, const int* pts, int ns, int nr,
                           double* trav_s, double* trav_r, double* corner, unsigned* err, cudaStream_t s) {
-    if (g.ndim != 2) return set_error(KGB_ERR_NOT_IMPLEMENTED, "device eikonal tables: 2-D only");
     ek_rhs_kernel<<<grid_for(g.ni), 256, 0, s>>>(speed, g.ni, rhs);
     KGB_CUDA_TRY(cudaGetLastError());
-    eikonal_sweep_kernel<<<ns + nr + 1, kEikThreads, 0, s>>>(g.nx, g.nz, g.hx, g.hz, speed, rhs, pts, ns, nr,
-                                                              trav_s, trav_r, corner, err);
+    if (g.ndim == 2) {
+        eikonal_sweep_kernel<<<ns + nr + 1, kEikThreads, 0, s>>>(g.nx, g.nz, g.hx, g.hz, speed, rhs, pts, ns, nr,
+                                                                  trav_s, trav_r, corner, err);
+    } else {
+        eikonal3_sweep_kernel<<<ns + nr + 1, kEik3Threads, 0, s>>>(g.ny, g.nx, g.nz, g.hy, g.hx, g.hz, speed, rhs, pts,
+                                                                    ns, nr, trav_s, trav_r, corner, err);
+    }
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
 
 int launch_distance_rows(const TableGeom& g, const double* corner, const int* pts, int ns, int nr, double* dist_s,
                          double* dist_r, cudaStream_t s) {
-    if (g.ndim != 2) return set_error(KGB_ERR_NOT_IMPLEMENTED, "device eikonal tables: 2-D only");
     dim3 grid((unsigned)std::max(1, grid_for(g.ni) / std::max(1, (ns + nr) / 8 + 1)), (unsigned)(ns + nr));
-    distance_rows_kernel<<<grid, 256, 0, s>>>(g.nx, g.nz, corner, pts, ns, dist_s, dist_r);
+    if (g.ndim == 2) distance_rows_kernel<<<grid, 256, 0, s>>>(g.nx, g.nz, corner, pts, ns, dist_s, dist_r);
+    else distance3_rows_kernel<<<grid, 256, 0, s>>>(g.ny, g.nx, g.nz, corner, pts, ns, dist_s, dist_r);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }

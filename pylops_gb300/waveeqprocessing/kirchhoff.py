@@ -162,9 +162,9 @@ class Kirchhoff(LinearOperator):
 
         # tables (kirchhoff.py:303-362)
         self.travsrcrec = True
-        # analytic tables and 2-D eikonal tables are built on the device
-        # (after the operator exists, below); 3-D eikonal tables on the host
-        device_tables = tables == "device" and (mode == "analytic" or (mode == "eikonal" and self.ndims == 2))
+        # analytic and eikonal tables are built on the device (after the
+        # operator exists, below)
+        device_tables = tables == "device" and mode in ("analytic", "eikonal")
         if device_tables and mode == "analytic" and not isinstance(vel, (float, int)):
             raise ValueError("vel must be scalar for mode=analytical")
         if mode in ["analytic", "eikonal", "byot"]:
