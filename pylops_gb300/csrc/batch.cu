@@ -30,7 +30,6 @@ namespace bt {
 
 constexpr int kRedThreads = 256;
 constexpr int kTile = 256;      // image points per adjoint item
-constexpr int kRC = 8;          // receivers in registers (adjoint)
 
 struct Prob {
     int ns, nr, nt, nz;

@@ -410,8 +410,8 @@ int ensure_cost(kgb_solver* s, int need) {
     return KGB_OK;
 }
 
-__global__ void diag_mul_kernel(float* __restrict__ out, const float* __restrict__ p, const float* __restrict__ v,
-                                int64_t n) {
+// out = p (.) v; out may be v (in-place scaling), so neither is restrict
+__global__ void diag_mul_kernel(float* out, const float* __restrict__ p, const float* v, int64_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = p[i] * v[i];
 }
