@@ -982,9 +982,19 @@ spread_binned_kernel(const KirchDev K, const FixedPoint<NONNEG> fp, float* __res
 // ---------------------------------------------------------------------------
 // 'same'-mode FIR along time: o[n] = sum_k g[k] x[n + c - k], c = (L-1)/2
 // (fir_same).  One block per trace (grid-stride); taps and the zero-padded
-// trace staged in shared memory.  interleave = 1 writes (o[n], o[n+1])
-// pairs for the gather; g == nullptr copies the trace (o = x).
+// trace staged in shared memory, two trace buffers: the next trace's
+// samples arrive by cp.async while the current one is filtered and
+// written.  interleave = 1 writes (o[n], o[n+1]) pairs for the gather;
+// g == nullptr copies the trace (o = x).
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 __global__ void __launch_bounds__(256)
 wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, int nt,
                const float* __restrict__ g, int L, int interleave) {
@@ -993,22 +1003,10 @@ wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, 
     const int span = fir_span(L, nt);
     const int q = fir_q(L);
     float* gs = smem;
-    float* xp = gs + Lp;
-    float* os = xp + span;
-    if (g) {
-        for (int k = threadIdx.x; k < Lp; k += blockDim.x) gs[k] = k < L ? g[k] : 0.f;
-        for (int i = threadIdx.x; i < span; i += blockDim.x) xp[i] = 0.f;
-    }
-    for (int64_t tr = blockIdx.x; tr < ntr; tr += gridDim.x) {
-        __syncthreads();
-        const float* xrow = x + tr * nt;
-        float* dst = g ? xp + q : os;
-        for (int n = threadIdx.x; n < nt; n += blockDim.x) dst[n] = __ldcs(xrow + n);
-        __syncthreads();
-        if (g) {
-            fir_same(gs, xp, os, L, nt, threadIdx.x, blockDim.x);
-            __syncthreads();
-        }
+    float* xb0 = gs + Lp;
+    float* xb1 = xb0 + span;
+    float* os = xb1 + span;
+    auto store = [&](int64_t tr) {
         if (interleave) {
             float2* yrow = reinterpret_cast<float2*>(y) + tr * nt;
             for (int n = threadIdx.x; n < nt; n += blockDim.x)
@@ -1017,7 +1015,41 @@ wavelet_kernel(const float* __restrict__ x, float* __restrict__ y, int64_t ntr, 
             float* yrow = y + tr * nt;
             for (int n = threadIdx.x; n < nt; n += blockDim.x) yrow[n] = os[n];
         }
+    };
+    if (!g) {
+        // copy (no filter)
+        for (int64_t tr = blockIdx.x; tr < ntr; tr += gridDim.x) {
+            __syncthreads();
+            const float* xrow = x + tr * nt;
+            for (int n = threadIdx.x; n < nt; n += blockDim.x) os[n] = __ldcs(xrow + n);
+            __syncthreads();
+            store(tr);
+        }
+        return;
     }
+    for (int k = threadIdx.x; k < Lp; k += blockDim.x) gs[k] = k < L ? g[k] : 0.f;
+    for (int i = threadIdx.x; i < 2 * span; i += blockDim.x) xb0[i] = 0.f;
+    __syncthreads();  // the zero padding is in place before the copies land
+    auto stage = [&](int64_t tr, float* dst) {
+        const float* xrow = x + tr * nt;
+        for (int n = threadIdx.x; n < nt; n += blockDim.x) cp_async4(dst + q + n, xrow + n);
+    };
+    int64_t tr = blockIdx.x;
+    if (tr < ntr) stage(tr, xb0);
+    cp_async_commit();
+    for (int it = 0; tr < ntr; ++it, tr += gridDim.x) {
+        float* cur = (it & 1) ? xb1 : xb0;
+        float* nxt = (it & 1) ? xb0 : xb1;
+        // the next trace into the buffer filtered one iteration ago
+        if (tr + gridDim.x < ntr) stage(tr + gridDim.x, nxt);
+        cp_async_commit();
+        cp_async_wait<1>();  // this thread's copies of the current trace landed
+        __syncthreads();     // ... and every thread's
+        fir_same(gs, cur, os, L, nt, threadIdx.x, blockDim.x);
+        __syncthreads();
+        store(tr);
+    }
+    cp_async_wait<0>();
 }
 
 // Dynamic-mode records {tq, wc, ws, 0}.
@@ -1758,8 +1790,9 @@ int gather1_launch_t(const KirchDev& K, const float2* d2, float* img, float* par
     return KGB_OK;
 }
 
+// taps, two padded trace buffers and the output trace
 size_t wavelet_smem(int L, int nt) {
-    return (size_t)(fir_lpad(L) + fir_span(L, nt) + fir_out(nt)) * sizeof(float);
+    return (size_t)(fir_lpad(L) + 2 * fir_span(L, nt) + fir_out(nt)) * sizeof(float);
 }
 
 int wavelet_threads(const float* g, int nt) {
