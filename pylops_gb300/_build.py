@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIBNAME = "libpylops_gb300.so"
 SOURCES = ["kirchhoff_kernels.cu", "kirchhoff_capi.cu", "solver.cu", "eikonal.cpp", "forward_static.cu", "batch.cu", "gemm_tcgen05.cu", "unet_kernels.cu", "nsconv2d.cu", "tables.cu"]
-HEADERS = ["kgb_internal.h", "fir.cuh", "fixed_acc.cuh", "tma.cuh", os.path.join("..", "..", "include", "kirchhoff_gb300.h")]
+HEADERS = ["kgb_internal.h", "fir.cuh", "fixed_acc.cuh", "tma.cuh", "dfacc.cuh", os.path.join("..", "..", "include", "kirchhoff_gb300.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fopenmp"]
 

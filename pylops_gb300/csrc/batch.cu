@@ -23,6 +23,7 @@
 
 #include "fir.cuh"
 #include "fixed_acc.cuh"
+#include "dfacc.cuh"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -294,7 +295,7 @@ seg_kernel(const SegItem* __restrict__ items, int op, float* __restrict__ u, con
            const CglsState* __restrict__ st, double* __restrict__ partials) {
     const SegItem it_ = items[blockIdx.x];
     const CglsState S = st[it_.p];
-    double acc = 0.0;
+    DFAcc dacc;
     if (S.active) {
         const float a = (float)S.a, b = (float)S.b, dsq = (float)S.dampsq;
         for (int64_t i = it_.begin + threadIdx.x; i < it_.end; i += blockDim.x) {
@@ -306,11 +307,11 @@ seg_kernel(const SegItem* __restrict__ items, int op, float* __restrict__ u, con
                 case OP_C: v = w[i] + b * v; u[i] = v; break;
                 default: break;
             }
-            acc = fma((double)v, (double)v, acc);
+            dacc.add_prod(v, v);
         }
     }
     if (op == OP_C) return;
-    acc = block_sum(acc);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 

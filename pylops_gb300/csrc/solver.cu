@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "dfacc.cuh"
 #include "kgb_internal.h"
 
 namespace kgb {
@@ -62,10 +63,10 @@ __device__ double block_sum(double v) {
 __global__ void __launch_bounds__(kRedThreads)
 dot_partial_kernel(const float* __restrict__ a, const float* __restrict__ b, int64_t n,
                    double* __restrict__ partials) {
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        acc = fma((double)a[i], (double)b[i], acc);
-    acc = block_sum(acc);
+        dacc.add_prod(a[i], b[i]);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -89,13 +90,13 @@ lsqr_u_kernel(float* __restrict__ u, const float* __restrict__ ub, int64_t n,
               const SolverState* __restrict__ st, double* __restrict__ partials) {
     if (!st->active) return;
     const float alfa = (float)st->alfa;
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float v = ub[i] - alfa * u[i];
         u[i] = v;
-        acc = fma((double)v, (double)v, acc);
+        dacc.add_prod(v, v);
     }
-    acc = block_sum(acc);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -134,13 +135,13 @@ lsqr_v_kernel(float* __restrict__ v, const float* __restrict__ vb, int64_t n,
               const SolverState* __restrict__ st, double* __restrict__ partials) {
     if (!st->active || !st->beta_pos) return;
     const float beta = (float)st->beta;
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = vb[i] - beta * v[i];
         v[i] = t;
-        acc = fma((double)t, (double)t, acc);
+        dacc.add_prod(t, t);
     }
-    acc = block_sum(acc);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -184,7 +185,7 @@ lsqr_xw_kernel(float* __restrict__ x, float* __restrict__ w, float* __restrict__
     const bool scale_v = st->beta_pos && st->alfa_pos;
     const float inv_alfa = (float)st->inv_alfa;
     const float t1 = (float)st->t1, t2 = (float)st->t2;
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float vi = v[i];
         if (scale_v) {
@@ -192,11 +193,11 @@ lsqr_xw_kernel(float* __restrict__ x, float* __restrict__ w, float* __restrict__
             v[i] = vi;
         }
         const float wi = w[i];
-        acc = fma((double)wi, (double)wi, acc);
+        dacc.add_prod(wi, wi);
         x[i] = x[i] + t1 * wi;
         w[i] = vi + t2 * wi;
     }
-    acc = block_sum(acc);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -260,10 +261,10 @@ __global__ void __launch_bounds__(kRedThreads)
 sq_partial_kernel(const float* __restrict__ a, int64_t n, const SolverState* __restrict__ st,
                   double* __restrict__ partials) {
     if (!st->active) return;
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        acc = fma((double)a[i], (double)a[i], acc);
-    acc = block_sum(acc);
+        dacc.add_prod(a[i], a[i]);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -273,13 +274,13 @@ cgls_x_kernel(float* __restrict__ x, const float* __restrict__ c, int64_t n,
               const SolverState* __restrict__ st, double* __restrict__ partials) {
     if (!st->active) return;
     const float a = (float)st->a;
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = x[i] + a * c[i];
         x[i] = t;
-        acc = fma((double)t, (double)t, acc);
+        dacc.add_prod(t, t);
     }
-    acc = block_sum(acc);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -289,13 +290,13 @@ cgls_s_kernel(float* __restrict__ s, const float* __restrict__ q, int64_t n,
               const SolverState* __restrict__ st, double* __restrict__ partials) {
     if (!st->active) return;
     const float a = (float)st->a;
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = s[i] - a * q[i];
         s[i] = t;
-        acc = fma((double)t, (double)t, acc);
+        dacc.add_prod(t, t);
     }
-    acc = block_sum(acc);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -305,13 +306,13 @@ cgls_r_kernel(float* __restrict__ r, const float* __restrict__ x, int64_t n,
               const SolverState* __restrict__ st, double* __restrict__ partials) {
     if (!st->active) return;
     const float damp = (float)st->dampsq;
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = r[i] - damp * x[i];
         r[i] = t;
-        acc = fma((double)t, (double)t, acc);
+        dacc.add_prod(t, t);
     }
-    acc = block_sum(acc);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
@@ -651,10 +652,10 @@ cgls_setup_kernel(SolverState* st, const double* __restrict__ pcc, int npc, cons
 
 __global__ void __launch_bounds__(kRedThreads)
 sq_partial_plain_kernel(const float* __restrict__ a, int64_t n, double* __restrict__ partials) {
-    double acc = 0.0;
+    DFAcc dacc;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        acc = fma((double)a[i], (double)a[i], acc);
-    acc = block_sum(acc);
+        dacc.add_prod(a[i], a[i]);
+    double acc = block_sum(dacc.value());
     if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
