@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(kRedThreads)
 dot_partial_kernel(const float* __restrict__ a, const float* __restrict__ b, int64_t n,
                    double* __restrict__ partials) {
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dacc.add_prod(a[i], b[i]);
     double acc = block_sum(dacc.value());
@@ -91,6 +92,7 @@ lsqr_u_kernel(float* __restrict__ u, const float* __restrict__ ub, int64_t n,
     if (!st->active) return;
     const float alfa = (float)st->alfa;
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float v = ub[i] - alfa * u[i];
         u[i] = v;
@@ -125,6 +127,7 @@ __global__ void scale_kernel(float* __restrict__ x, int64_t n, const SolverState
         if (!(st->beta_pos && st->alfa_pos)) return;
         f = (float)st->inv_alfa;
     }
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] *= f;
 }
@@ -136,6 +139,7 @@ lsqr_v_kernel(float* __restrict__ v, const float* __restrict__ vb, int64_t n,
     if (!st->active || !st->beta_pos) return;
     const float beta = (float)st->beta;
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = vb[i] - beta * v[i];
         v[i] = t;
@@ -186,6 +190,7 @@ lsqr_xw_kernel(float* __restrict__ x, float* __restrict__ w, float* __restrict__
     const float inv_alfa = (float)st->inv_alfa;
     const float t1 = (float)st->t1, t2 = (float)st->t2;
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float vi = v[i];
         if (scale_v) {
@@ -262,6 +267,7 @@ sq_partial_kernel(const float* __restrict__ a, int64_t n, const SolverState* __r
                   double* __restrict__ partials) {
     if (!st->active) return;
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dacc.add_prod(a[i], a[i]);
     double acc = block_sum(dacc.value());
@@ -275,6 +281,7 @@ cgls_x_kernel(float* __restrict__ x, const float* __restrict__ c, int64_t n,
     if (!st->active) return;
     const float a = (float)st->a;
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = x[i] + a * c[i];
         x[i] = t;
@@ -291,6 +298,7 @@ cgls_s_kernel(float* __restrict__ s, const float* __restrict__ q, int64_t n,
     if (!st->active) return;
     const float a = (float)st->a;
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = s[i] - a * q[i];
         s[i] = t;
@@ -307,6 +315,7 @@ cgls_r_kernel(float* __restrict__ r, const float* __restrict__ x, int64_t n,
     if (!st->active) return;
     const float damp = (float)st->dampsq;
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float t = r[i] - damp * x[i];
         r[i] = t;
@@ -321,6 +330,7 @@ __global__ void cgls_c_kernel(float* __restrict__ c, const float* __restrict__ r
                               const SolverState* __restrict__ st) {
     if (!st->active) return;
     const float b = (float)st->b;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         c[i] = r[i] + b * c[i];
 }
@@ -413,6 +423,7 @@ int ensure_cost(kgb_solver* s, int need) {
 
 // out = p (.) v; out may be v (in-place scaling), so neither is restrict
 __global__ void diag_mul_kernel(float* out, const float* __restrict__ p, const float* v, int64_t n) {
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = p[i] * v[i];
 }
@@ -614,6 +625,7 @@ __global__ void scale_by_kernel(float* __restrict__ x, int64_t n, const SolverSt
     float f;
     if (which == 0) { if (!st->beta_pos) return; f = (float)st->inv_beta; }
     else { if (!(st->beta_pos && st->alfa_pos)) return; f = (float)st->inv_alfa; }
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         x[i] *= f;
 }
@@ -621,16 +633,19 @@ __global__ void scale_by_kernel(float* __restrict__ x, int64_t n, const SolverSt
 __global__ void copy_if_beta_zero_kernel(float* __restrict__ v, const float* __restrict__ x, int64_t n,
                                          const SolverState* __restrict__ st) {
     if (st->beta_pos) return;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         v[i] = x[i];
 }
 
 __global__ void sub_kernel(float* __restrict__ out, const float* __restrict__ a, const float* __restrict__ b, int64_t n) {
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = a[i] - b[i];
 }
 
 __global__ void axpy_kernel(float* __restrict__ y, const float* __restrict__ x, float a, int64_t n) {
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         y[i] += a * x[i];
 }
@@ -653,6 +668,7 @@ cgls_setup_kernel(SolverState* st, const double* __restrict__ pcc, int npc, cons
 __global__ void __launch_bounds__(kRedThreads)
 sq_partial_plain_kernel(const float* __restrict__ a, int64_t n, double* __restrict__ partials) {
     DFAcc dacc;
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dacc.add_prod(a[i], a[i]);
     double acc = block_sum(dacc.value());
@@ -676,6 +692,7 @@ struct CombArgs {
 // out = c0 * base + sum_j c[j] v[j] (base may be NULL), summed in index order
 __global__ void lincomb_kernel(float* __restrict__ out, const float* __restrict__ base, float c0, CombArgs a, int k,
                                int64_t n) {
+    #pragma unroll 4
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float acc = base ? c0 * base[i] : 0.f;
         for (int j = 0; j < k; ++j) acc = fmaf(a.c[j], a.v[j][i], acc);
