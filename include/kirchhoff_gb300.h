@@ -345,6 +345,16 @@ int kgb_conv3x3_bf16(const void* x_dev, const void* w_dev, void* y_dev, int B, i
  * split over the pixels into `work` (at least 3 ceil(3 C / 128) 128 x N
  * floats) and summed in slice order (deterministic).  C % 32 == 0,
  * W % 64 == 0.  No reference counterpart. */
+/* Data gradient of a 3x3 stride-2 convolution (padding 1) of an input of
+ * 2 Hg x 2 Wg pixels: dx (float32, B x 2Hg x 2Wg x N) from the output
+ * gradient g (bf16 NHWC, B x Hg x Wg x C, C % 8 == 0) and the transposed
+ * weights wt (bf16, N x 9 Cp, as kgb_unet_weights_implicit writes Wti), as
+ * four stride-1 implicit convolutions on g, one per output pixel parity
+ * (1, 2, 2 and 4 taps), written 2 pixels apart: no unfolded copy.  Wg % 128
+ * == 0, N <= 128, N % 4 == 0.  No reference counterpart. */
+int kgb_conv3x3_s2_dgrad_bf16(const void* g_dev, const void* wt_dev, float* dx_dev, int B, int Hg, int Wg, int C,
+                              int N, int* err_dev, void* stream);
+
 int kgb_conv3x3_wgrad_bf16(const void* xT3_dev, const void* gTr_dev, float* dW_dev, int B, int H, int W, int C, int N,
                            int ldw, float* work_dev, int64_t work_elems, int* err_dev, void* stream);
 

@@ -85,6 +85,7 @@ _SIGNATURES = {
                                  c_vp, c_vp], c_int),
     "kgb_conv3x3_bf16": ([c_vp, c_vp, c_vp] + [c_int] * 6 + [c_vp, c_int, c_vp, c_vp], c_int),
     "kgb_conv3x3_wgrad_bf16": ([c_vp, c_vp, c_vp] + [c_int] * 6 + [c_vp, c_i64, c_vp, c_vp], c_int),
+    "kgb_conv3x3_s2_dgrad_bf16": ([c_vp, c_vp, c_vp] + [c_int] * 5 + [c_vp, c_vp], c_int),
     "kgb_unet_unfold": ([c_vp, c_vp] + [c_int] * 10 + [c_vp], c_int),
     "kgb_unet_unfold_t": ([c_vp, c_vp] + [c_int] * 6 + [c_vp], c_int),
     "kgb_unet_transpose": ([c_vp, c_vp, c_i64, c_int, c_i64, c_i64, c_int, c_vp], c_int),

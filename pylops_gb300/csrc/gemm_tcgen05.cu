@@ -412,27 +412,43 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
 }
 
-// Implicit 3x3 convolution with the input read once per image row of a
-// tile: tiles are 128 consecutive output pixels of one image row (W % 128
-// == 0).  For each channel block cb and each ky the producer loads one halo
-// row -- input pixels w0 - 1 .. w0 + 134 of image row h + sgn (ky - 1), 64
-// channels each (a 136-row, 128-byte-row tile, zero fill outside the image)
-// -- and the MMA warp issues the three kx taps on it: the A operand of tap
-// kx is the same tile starting kx rows in (2 - kx for the transposed
-// convolution; the descriptor's 128-byte swizzle follows the absolute
-// shared-memory address, so a start offset by whole rows reads the rows
-// the TMA wrote there).  The weights of all 9 taps (N <= BN rows) stay in
-// shared memory for the whole kernel.  Same persistence, accumulator
-// double-buffering, epilogue and bounded waits as gemm_tn_kernel.
+// Implicit convolutions with the input read once per image row of a tile:
+// tiles are 128 consecutive pixels of one row of the source grid (the
+// grid the A operand is read from; its width a multiple of 128).  A plan
+// lists, per channel block, up to three halo rows -- source row i +
+// row_dh[h], source columns w0 + col0 .. w0 + col0 + 135, 64 channels each
+// (a 136-row, 128-byte-row tile, zero fill outside the image) -- and per
+// halo row up to three taps: the A operand of a tap is that tile starting
+// `off` rows in (the descriptor's 128-byte swizzle follows the absolute
+// shared-memory address, so a start offset by whole rows reads the rows the
+// TMA wrote there), its B operand the weight tile of kernel tap `w`.  The
+// weights of all 9 taps (N <= BN rows) stay in shared memory for the whole
+// kernel.  Output pixel of source pixel (img, i, j): (img, out_rs i +
+// out_rb, out_cs j + out_cb) of an Hout x Wout image, so a tile's 128 output
+// rows are out_cs pixels apart.  Plans: the 3x3 stride-1 convolution and its
+// transposed form (3 halo rows, 3 taps each), and the four pixel-parity
+// classes of the data gradient of a 3x3 stride-2 convolution (1 or 2 halo
+// rows, 1, 2, 2 or 4 taps, outputs 2 pixels apart).  Same persistence,
+// accumulator double-buffering, epilogue and bounded waits as
+// gemm_tn_kernel.
 constexpr int kHaloRows = 136;                  // 130 needed, 8-row multiple
 constexpr int kHaloBytes = 18 * 1024;           // 136 x 128 B, rounded to 1 KB
 constexpr int kHaloMaxStages = 8;
+
+struct HaloPlan {
+    int nrows;                     // halo rows per channel block (1..3)
+    int row_dh[3];                 // source row offset of each halo row
+    int col0;                      // first source column of the halo, relative to the tile's
+    int row_ntaps[3];              // taps per halo row (1..3)
+    int tap_off[3][3], tap_w[3][3];  // per halo row and tap: row offset in the halo, kernel tap
+    int out_rs, out_rb, out_cs, out_cb, Hout, Wout;
+};
 
 template <int BN>
 __global__ void __launch_bounds__(kGemmThreads, 1)
 conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW, void* __restrict__ C,
                  int M, int N, const float* __restrict__ bias, int flags, int* __restrict__ err, const ConvGeom cg,
-                 int stages) {
+                 const __grid_constant__ HaloPlan plan, int stages) {
     constexpr int W_TILE = BN * BK * 2;  // one (tap, channel block) weight tile
     const int S = stages;
     const int nw = 9 * cg.cblk;          // resident weight tiles
@@ -456,7 +472,8 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ntiles = M / BM;
-    const int steps = 3 * cg.cblk;  // halo rows per tile
+    const int steps = plan.nrows * cg.cblk;  // halo rows per tile
+    const int hw = cg.H * cg.W;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
@@ -489,7 +506,6 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
             for (int g = 0; g < nw; ++g) tma_load_2d(sW + g * W_TILE, &tmW, bar_w, g * BK, 0);
             uint32_t it = 0;
             bool ok = true;
-            const int hw = cg.H * cg.W;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
                 const int m0 = t * BM;
                 const int img = m0 / hw, r = m0 - img * hw;
@@ -500,10 +516,10 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
                         ok = false;
                         break;
                     }
-                    const int cb = st / 3, ky = st - cb * 3;
+                    const int cb = st / plan.nrows, hr = st - cb * plan.nrows;
                     mbar_expect_tx(bar_full + 8 * s, kHaloRows * BK * 2);
-                    tma_load_4d(sR + s * kHaloBytes, &tmX, bar_full + 8 * s, cb * BK, w0 - 1, h + cg.sgn * (ky - 1),
-                                img);
+                    tma_load_4d(sR + s * kHaloBytes, &tmX, bar_full + 8 * s, cb * BK, w0 + plan.col0,
+                                h + plan.row_dh[hr], img);
                 }
             }
             if (!ok) *abort_flag = 1;
@@ -532,17 +548,16 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    const int cb = st / 3, ky = st - cb * 3;
+                    const int cb = st / plan.nrows, hr = st - cb * plan.nrows;
                     const uint32_t halo = sR + s * kHaloBytes;
-#pragma unroll
-                    for (int kx = 0; kx < 3; ++kx) {
-                        const int off = cg.sgn > 0 ? kx : 2 - kx;
-                        const uint32_t wt = sW + ((ky * 3 + kx) * cg.cblk + cb) * W_TILE;
+                    for (int q = 0; q < plan.row_ntaps[hr]; ++q) {
+                        const int off = plan.tap_off[hr][q];
+                        const uint32_t wt = sW + (plan.tap_w[hr][q] * cg.cblk + cb) * W_TILE;
 #pragma unroll
                         for (int k = 0; k < BK / 16; ++k) {
                             const uint64_t da = sw128_desc(halo + off * 128 + k * 32);
                             const uint64_t db = sw128_desc(wt + k * 32);
-                            const uint32_t acc = (st > 0 || kx > 0 || k > 0) ? 1u : 0u;
+                            const uint32_t acc = (st > 0 || q > 0 || k > 0) ? 1u : 0u;
                             asm volatile(
                                 "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
@@ -572,7 +587,15 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            epilogue_store<BN>(tmem, q, a, lane, t * BM, 0, M, N, N, C, bias, flags);
+            // output row segment of this tile: 128 pixels, out_cs apart
+            const int m0 = t * BM;
+            const int img = m0 / hw, r = m0 - img * hw;
+            const int h = r / cg.W, w0 = r - h * cg.W;
+            const int64_t opix = ((int64_t)img * plan.Hout + (int64_t)plan.out_rs * h + plan.out_rb) * plan.Wout +
+                                 (int64_t)plan.out_cs * w0 + plan.out_cb;
+            void* Ct = (flags & 2) ? static_cast<void*>(reinterpret_cast<__nv_bfloat16*>(C) + opix * N)
+                                   : static_cast<void*>(reinterpret_cast<float*>(C) + opix * N);
+            epilogue_store<BN>(tmem, q, a, lane, 0, 0, BM, N, plan.out_cs * N, Ct, bias, flags);
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar_tempty + 8 * a) : "memory");
@@ -721,14 +744,69 @@ int halo_stages(int BN, int cblk) {
 
 template <int BN>
 int halo_launch(const CUtensorMap& mx, const CUtensorMap& mw, void* y, int M, int N, const float* bias, int flags,
-                int* err, const ConvGeom& cg, int stages, cudaStream_t s) {
+                int* err, const ConvGeom& cg, const HaloPlan& plan, int stages, cudaStream_t s) {
     const size_t smem = halo_smem(BN, cg.cblk, stages);
     KGB_CUDA_TRY(cudaFuncSetAttribute(conv_halo_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int ntiles = M / BM;
     const int grid = std::min(ntiles, sm_count());
-    conv_halo_kernel<BN><<<grid, kGemmThreads, smem, s>>>(mx, mw, y, M, N, bias, flags, err, cg, stages);
+    conv_halo_kernel<BN><<<grid, kGemmThreads, smem, s>>>(mx, mw, y, M, N, bias, flags, err, cg, plan, stages);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
+}
+
+// The 3x3 stride-1 convolution (sgn = +1) or its transposed form (sgn = -1):
+// halo rows ky = 0, 1, 2 at source row offset sgn (ky - 1), columns from
+// w0 - 1, taps kx at halo row offset kx (2 - kx transposed).
+HaloPlan plan_conv3x3(int sgn, int Hout, int Wout) {
+    HaloPlan p{};
+    p.nrows = 3;
+    p.col0 = -1;
+    for (int ky = 0; ky < 3; ++ky) {
+        p.row_dh[ky] = sgn * (ky - 1);
+        p.row_ntaps[ky] = 3;
+        for (int kx = 0; kx < 3; ++kx) {
+            p.tap_off[ky][kx] = sgn > 0 ? kx : 2 - kx;
+            p.tap_w[ky][kx] = ky * 3 + kx;
+        }
+    }
+    p.out_rs = 1;
+    p.out_rb = 0;
+    p.out_cs = 1;
+    p.out_cb = 0;
+    p.Hout = Hout;
+    p.Wout = Wout;
+    return p;
+}
+
+// Data gradient of a 3x3 stride-2 convolution (padding 1), output pixels of
+// parity (a, b): dx[2i + a][2j + b] = sum over the taps (ky, kx) with
+// ky = 1 (a = 0) or ky in {0, 2} (a = 1), likewise kx, of W_tap^T g[i + di][j + dj],
+// di = 1 for ky = 0 and 0 otherwise (dj likewise): the halo rows are g rows
+// i + 1 and i, its columns start at j0, and a tap with dj = 1 starts one
+// row into the halo.
+HaloPlan plan_s2_dgrad(int a, int b, int Hout, int Wout) {
+    HaloPlan p{};
+    const int kys[2] = {a == 0 ? 1 : 0, 2}, nky = a == 0 ? 1 : 2;
+    const int kxs[2] = {b == 0 ? 1 : 0, 2}, nkx = b == 0 ? 1 : 2;
+    p.nrows = nky;
+    p.col0 = 0;
+    for (int r = 0; r < nky; ++r) {
+        const int ky = kys[r];
+        p.row_dh[r] = ky == 0 ? 1 : 0;
+        p.row_ntaps[r] = nkx;
+        for (int q = 0; q < nkx; ++q) {
+            const int kx = kxs[q];
+            p.tap_off[r][q] = kx == 0 ? 1 : 0;
+            p.tap_w[r][q] = ky * 3 + kx;
+        }
+    }
+    p.out_rs = 2;
+    p.out_rb = a;
+    p.out_cs = 2;
+    p.out_cb = b;
+    p.Hout = Hout;
+    p.Wout = Wout;
+    return p;
 }
 
 template <int BN>
@@ -881,9 +959,10 @@ extern "C" int kgb_conv3x3_bf16(const void* x, const void* w, void* y, int B, in
         if ((rc = make_map(&mb, w, N, K, K, BN))) return rc;
         flags = (flags & 3) | vector_flag(y, N, flags);
         const ConvGeom hg{H, W, cblk, flip ? -1 : 1, B};
+        const HaloPlan plan = plan_conv3x3(flip ? -1 : 1, H, W);
         cudaStream_t hs = (cudaStream_t)stream;
-        if (BN == 64) return halo_launch<64>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, hstages, hs);
-        return halo_launch<128>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, hstages, hs);
+        if (BN == 64) return halo_launch<64>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, plan, hstages, hs);
+        return halo_launch<128>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, plan, hstages, hs);
     }
     if ((rc = make_map_nhwc(&ma, x, B, H, W, C, bw, bh))) return rc;
     if ((rc = make_map(&mb, w, N, K, K, BN))) return rc;
@@ -938,5 +1017,38 @@ extern "C" int kgb_conv3x3_wgrad_bf16(const void* xT3, const void* gTr, float* d
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4 * sm_count()));
     wgrad_sum_kernel<<<grid, 256, 0, s>>>(work, dW, M, N, splits, C, Mky, ldw);
     KGB_CUDA_TRY(cudaGetLastError());
+    return KGB_OK;
+}
+
+extern "C" int kgb_conv3x3_s2_dgrad_bf16(const void* g, const void* wt, float* dx, int B, int Hg, int Wg, int C, int N,
+                                        int* err_dev, void* stream) {
+    if (!g || !wt || !dx) return set_error(KGB_ERR_VALUE, "s2 dgrad: null pointer");
+    if (B <= 0 || Hg <= 0 || Wg <= 0 || C <= 0 || N <= 0) return set_error(KGB_ERR_VALUE, "s2 dgrad: sizes must be positive");
+    if (C % 8) return set_error(KGB_ERR_VALUE, "s2 dgrad: channels must be a multiple of 8 (16-byte pixel rows)");
+    if (Wg % BM || N > 128 || N % 4)
+        return set_error(KGB_ERR_VALUE, "s2 dgrad: needs gradient rows of 128-pixel multiples and N <= 128, N %% 4 == 0");
+    if ((((uintptr_t)g | (uintptr_t)wt | (uintptr_t)dx) & 15) != 0)
+        return set_error(KGB_ERR_VALUE, "s2 dgrad: operands must be 16-byte aligned");
+    const int cblk = (C + BK - 1) / BK;
+    const int K = 9 * cblk * BK;
+    const int64_t M = (int64_t)B * Hg * Wg;
+    if (M > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "s2 dgrad: too many pixels");
+    const int BN = N <= 64 ? 64 : 128;
+    const int hstages = halo_stages(BN, cblk);
+    if (!hstages) return set_error(KGB_ERR_NOT_IMPLEMENTED, "s2 dgrad: weights do not fit in shared memory");
+    CUtensorMap ma, mb;
+    int rc;
+    if ((rc = make_map_halo(&ma, g, B, Hg, Wg, C))) return rc;
+    if ((rc = make_map(&mb, wt, N, K, K, BN))) return rc;
+    const int flags = vector_flag(dx, 2 * N, 0);
+    const ConvGeom hg{Hg, Wg, cblk, 1, B};
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) {
+            const HaloPlan plan = plan_s2_dgrad(a, b, 2 * Hg, 2 * Wg);
+            rc = BN == 64 ? halo_launch<64>(ma, mb, dx, (int)M, N, nullptr, flags, err_dev, hg, plan, hstages, s)
+                          : halo_launch<128>(ma, mb, dx, (int)M, N, nullptr, flags, err_dev, hg, plan, hstages, s);
+            if (rc) return rc;
+        }
     return KGB_OK;
 }

@@ -4,9 +4,11 @@ The convolutions (forward, weight gradient, data gradient) run on tcgen05
 tensor-core GEMMs: 3x3 stride-1 layers as implicit convolutions
 (``kgb_conv3x3_bf16``, one halo row per tap row for image rows of 128-pixel
 multiples) and implicit weight gradients (``kgb_conv3x3_wgrad_bf16`` on
-operands transposed per image row), the stride-2 layers as GEMMs
+operands transposed per image row); the stride-2 layers as GEMMs
 (``kgb_gemm_bf16_tn`` / ``kgb_gemm_bf16_tn_splitk``) on operands unfolded by
-``kgb_unet_unfold`` / ``kgb_unet_unfold_t``.  The two layers with one
+``kgb_unet_unfold`` / ``kgb_unet_unfold_t``, except their data gradient on
+rows of 128-pixel multiples, which runs as the four pixel-parity classes of
+implicit convolutions (``kgb_conv3x3_s2_dgrad_bf16``).  The two layers with one
 channel on a side -- the first 3x3 convolution of the one-channel input and
 the 1x1 head to one channel -- are direct kernels (a GEMM would be 1/8 or
 1/64 occupied).  ReLU masks, bias gradients, upsampling, skip concatenation,
@@ -43,6 +45,14 @@ def _rup(n: int, k: int = 8) -> int:
     return (n + k - 1) // k * k
 
 
+def _halo_weights_fit(C: int, N: int) -> bool:
+    """Do the 9-tap weights of an implicit convolution with C input and N
+    output channels stay in shared memory next to three halo rows (the
+    condition of kgb_conv3x3_s2_dgrad_bf16)?"""
+    cblk, bn = (C + 63) // 64, 64 if N <= 64 else 128
+    return 1024 + 9 * cblk * bn * 128 + 3 * 18 * 1024 + 8 * 12 + 16 <= 227 * 1024
+
+
 def _tileable(H: int, W: int) -> bool:
     """Can 128-pixel M tiles be TMA boxes of one image (kgb_conv3x3_bf16)?"""
     return (W >= 128 and W % 128 == 0) or (W < 128 and 128 % W == 0 and H % (128 // W) == 0)
@@ -64,6 +74,10 @@ class _Conv:
         # GEMMs (kgb_conv3x3_bf16) with weights in 64-channel blocks
         self.implicit = ks == 3 and stride == 1 and cin % 8 == 0
         self.implicit_dx = self.implicit and cout % 8 == 0
+        # 3x3 stride-2 layers: data gradient by pixel-parity classes on the
+        # tensor cores (kgb_conv3x3_s2_dgrad_bf16) when the gradient rows allow
+        self.s2_dx = (ks == 3 and stride == 2 and cout % 8 == 0 and cin % 4 == 0 and cin <= 128
+                      and _halo_weights_fit(cout, cin))
         self.Wi = None                      # bf16 (cout x 9 * rup(cin, 64))
         self.Wti = None                     # bf16 (cin x 9 * rup(cout, 64))
 
@@ -82,7 +96,8 @@ class _CountingLib:
     the others)."""
 
     _KERNELS = {"kgb_gemm_bf16_tn_splitk": 2, "kgb_unet_rowsum": 2, "kgb_unet_mse": 2, "kgb_conv3x3_wgrad_bf16": 2,
-                "kgb_unet_colsum": 2, "kgb_unet_conv3x3_c1_wgrad": 2}
+                "kgb_unet_colsum": 2, "kgb_unet_conv3x3_c1_wgrad": 2,
+                "kgb_conv3x3_s2_dgrad_bf16": 4}
 
     def __init__(self, owner):
         self._owner = owner
@@ -160,9 +175,9 @@ class UNet:
         for c in convs:
             c.Wb = torch.empty((c.cout, c.kpad), dtype=torch.bfloat16, device=dev)
             c.Wt = torch.empty((c.cin, c.kg), dtype=torch.bfloat16, device=dev)
-            if c.implicit:
+            if c.implicit or c.s2_dx:
                 c.Wi = torch.empty((c.cout, 9 * _rup(c.cin, 64)), dtype=torch.bfloat16, device=dev)
-                if c.implicit_dx:
+                if c.implicit_dx or c.s2_dx:
                     c.Wti = torch.empty((c.cin, 9 * _rup(c.cout, 64)), dtype=torch.bfloat16, device=dev)
         self._refresh_weights()
         self._ws = None
@@ -199,7 +214,7 @@ class UNet:
         for c in self.convs:
             _native.check(L.kgb_unet_weights(self._w(c).data_ptr(), c.Wb.data_ptr(), c.Wt.data_ptr(), c.cout, c.cin,
                                              c.ks, c.kpad, c.kg, s))
-            if c.implicit:
+            if c.Wi is not None:
                 _native.check(L.kgb_unet_weights_implicit(self._w(c).data_ptr(), c.Wi.data_ptr(),
                                                           c.Wti.data_ptr() if c.Wti is not None else None, c.cout,
                                                           c.cin, c.kpad, s))
@@ -424,6 +439,11 @@ class UNet:
             # the transposed convolution straight from g (no unfold)
             _native.check(L.kgb_conv3x3_bf16(g.data_ptr(), c.Wti.data_ptr(), dx.data_ptr(), B, H, W, c.cout, c.cin, 1,
                                              None, 0, self._err.data_ptr(), s))
+            return
+        if self.implicit and c.s2_dx and Wo % 128 == 0 and H == 2 * Ho and W == 2 * Wo:
+            # stride 2: the four pixel-parity classes straight from g (no unfold)
+            _native.check(L.kgb_conv3x3_s2_dgrad_bf16(g.data_ptr(), c.Wti.data_ptr(), dx.data_ptr(), B, Ho, Wo,
+                                                      c.cout, c.cin, self._err.data_ptr(), s))
             return
         _native.check(L.kgb_unet_unfold(g.data_ptr(), col.data_ptr(), B, Ho, Wo, c.cout, H, W, c.ks, c.stride, 1,
                                         c.kg, s))

@@ -202,3 +202,46 @@ def test_implicit_weight_gradient_matches_conv2d_weight(B, H, W, C, N):
     assert int(err.item()) == 0
     assert _rel(got[:, :9 * C].numpy(), ref.numpy()) < 1e-5
     assert torch.all(got[:, 9 * C:] == 5.0)
+
+
+@pytest.mark.parametrize("B,Hg,Wg,C,N", [(2, 4, 128, 64, 32), (1, 3, 256, 32, 64), (2, 2, 128, 128, 64),
+                                       (2, 2, 128, 64, 96)])
+def test_stride2_data_gradient_matches_conv2d_input(B, Hg, Wg, C, N):
+    """kgb_conv3x3_s2_dgrad_bf16 (four pixel-parity classes of implicit
+    stride-1 convolutions on g) against the input gradient of torch conv2d
+    (stride 2, padding 1) on the same bf16-rounded operands."""
+    from pylops_gb300 import _native
+
+    g = torch.Generator().manual_seed(B * 10 + C + N)
+    w = _bf(torch.randn(C, N, 3, 3, generator=g) / (3 * N ** 0.5))  # forward weights: C outputs, N inputs
+    gy = _bf(torch.randn(B, Hg, Wg, C, generator=g))
+    ref = torch.nn.grad.conv2d_input((B, N, 2 * Hg, 2 * Wg), w.double(), gy.permute(0, 3, 1, 2).double(), stride=2,
+                                     padding=1).permute(0, 2, 3, 1).float()
+    Cp = (C + 63) // 64 * 64
+    wt = torch.zeros(N, 9, Cp)
+    wt[:, :, :C] = w.permute(1, 2, 3, 0).reshape(N, 9, C)  # Wti[n][tap * Cp + c] = W[c][n][tap]
+    gd = gy.to(torch.bfloat16).cuda().contiguous()
+    wd = wt.reshape(N, 9 * Cp).to(torch.bfloat16).cuda().contiguous()
+    dx = torch.full((B, 2 * Hg, 2 * Wg, N), 3.0, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _native.check(_native.lib().kgb_conv3x3_s2_dgrad_bf16(gd.data_ptr(), wd.data_ptr(), dx.data_ptr(), B, Hg, Wg, C,
+                                                          N, err.data_ptr(),
+                                                          torch.cuda.current_stream().cuda_stream))
+    assert int(err.item()) == 0
+    assert _rel(dx.cpu().numpy(), ref.numpy()) < 1e-5
+
+
+def test_stride2_data_gradient_rejects_weights_that_do_not_fit():
+    """Two 64-channel blocks of gradient channels with 128 output columns
+    (288 KB of resident weights) are refused, and the network's layer check
+    agrees (it keeps the unfolded GEMM for such layers)."""
+    from pylops_gb300 import _native
+    from pylops_gb300.learned.unet import _halo_weights_fit
+
+    assert not _halo_weights_fit(128, 96) and _halo_weights_fit(128, 64) and _halo_weights_fit(64, 96)
+    g = torch.zeros(1, 2, 128, 128, dtype=torch.bfloat16, device="cuda")
+    wt = torch.zeros(96, 9 * 128, dtype=torch.bfloat16, device="cuda")
+    dx = torch.zeros(1, 4, 256, 96, device="cuda")
+    with pytest.raises(NotImplementedError):
+        _native.check(_native.lib().kgb_conv3x3_s2_dgrad_bf16(g.data_ptr(), wt.data_ptr(), dx.data_ptr(), 1, 2, 128,
+                                                              128, 96, None, torch.cuda.current_stream().cuda_stream))
