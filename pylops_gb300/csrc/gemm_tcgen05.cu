@@ -442,6 +442,7 @@ struct HaloPlan {
     int row_ntaps[3];              // taps per halo row (1..3)
     int tap_off[3][3], tap_w[3][3];  // per halo row and tap: row offset in the halo, kernel tap
     int out_rs, out_rb, out_cs, out_cb, Hout, Wout;
+    int ksteps_last;               // 16-channel k-steps of the last channel block that hold channels
 };
 
 template <int BN>
@@ -549,12 +550,14 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const int cb = st / plan.nrows, hr = st - cb * plan.nrows;
+                    const int nk = cb == cg.cblk - 1 ? plan.ksteps_last : BK / 16;
                     const uint32_t halo = sR + s * kHaloBytes;
                     for (int q = 0; q < plan.row_ntaps[hr]; ++q) {
                         const int off = plan.tap_off[hr][q];
                         const uint32_t wt = sW + (plan.tap_w[hr][q] * cg.cblk + cb) * W_TILE;
 #pragma unroll
                         for (int k = 0; k < BK / 16; ++k) {
+                            if (k >= nk) break;  // zero-filled channels past C contribute nothing
                             const uint64_t da = sw128_desc(halo + off * 128 + k * 32);
                             const uint64_t db = sw128_desc(wt + k * 32);
                             const uint32_t acc = (st > 0 || q > 0 || k > 0) ? 1u : 0u;
@@ -757,8 +760,14 @@ int halo_launch(const CUtensorMap& mx, const CUtensorMap& mw, void* y, int M, in
 // The 3x3 stride-1 convolution (sgn = +1) or its transposed form (sgn = -1):
 // halo rows ky = 0, 1, 2 at source row offset sgn (ky - 1), columns from
 // w0 - 1, taps kx at halo row offset kx (2 - kx transposed).
-HaloPlan plan_conv3x3(int sgn, int Hout, int Wout) {
+// k-steps of the last 64-channel block of C channels that hold channels
+int last_ksteps(int C) {
+    return (C - ((C - 1) / BK) * BK + 15) / 16;
+}
+
+HaloPlan plan_conv3x3(int sgn, int Hout, int Wout, int C) {
     HaloPlan p{};
+    p.ksteps_last = last_ksteps(C);
     p.nrows = 3;
     p.col0 = -1;
     for (int ky = 0; ky < 3; ++ky) {
@@ -784,8 +793,9 @@ HaloPlan plan_conv3x3(int sgn, int Hout, int Wout) {
 // di = 1 for ky = 0 and 0 otherwise (dj likewise): the halo rows are g rows
 // i + 1 and i, its columns start at j0, and a tap with dj = 1 starts one
 // row into the halo.
-HaloPlan plan_s2_dgrad(int a, int b, int Hout, int Wout) {
+HaloPlan plan_s2_dgrad(int a, int b, int Hout, int Wout, int C) {
     HaloPlan p{};
+    p.ksteps_last = last_ksteps(C);
     const int kys[2] = {a == 0 ? 1 : 0, 2}, nky = a == 0 ? 1 : 2;
     const int kxs[2] = {b == 0 ? 1 : 0, 2}, nkx = b == 0 ? 1 : 2;
     p.nrows = nky;
@@ -959,7 +969,7 @@ extern "C" int kgb_conv3x3_bf16(const void* x, const void* w, void* y, int B, in
         if ((rc = make_map(&mb, w, N, K, K, BN))) return rc;
         flags = (flags & 3) | vector_flag(y, N, flags);
         const ConvGeom hg{H, W, cblk, flip ? -1 : 1, B};
-        const HaloPlan plan = plan_conv3x3(flip ? -1 : 1, H, W);
+        const HaloPlan plan = plan_conv3x3(flip ? -1 : 1, H, W, C);
         cudaStream_t hs = (cudaStream_t)stream;
         if (BN == 64) return halo_launch<64>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, plan, hstages, hs);
         return halo_launch<128>(ma, mb, y, (int)M, N, bias, flags, err_dev, hg, plan, hstages, hs);
@@ -1045,7 +1055,7 @@ extern "C" int kgb_conv3x3_s2_dgrad_bf16(const void* g, const void* wt, float* d
     cudaStream_t s = (cudaStream_t)stream;
     for (int a = 0; a < 2; ++a)
         for (int b = 0; b < 2; ++b) {
-            const HaloPlan plan = plan_s2_dgrad(a, b, 2 * Hg, 2 * Wg);
+            const HaloPlan plan = plan_s2_dgrad(a, b, 2 * Hg, 2 * Wg, C);
             rc = BN == 64 ? halo_launch<64>(ma, mb, dx, (int)M, N, nullptr, flags, err_dev, hg, plan, hstages, s)
                           : halo_launch<128>(ma, mb, dx, (int)M, N, nullptr, flags, err_dev, hg, plan, hstages, s);
             if (rc) return rc;
