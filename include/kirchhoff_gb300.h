@@ -351,7 +351,9 @@ int kgb_conv3x3_bf16(const void* x_dev, const void* w_dev, void* y_dev, int B, i
  * weights wt (bf16, N x 9 Cp, as kgb_unet_weights_implicit writes Wti), as
  * four stride-1 implicit convolutions on g, one per output pixel parity
  * (1, 2, 2 and 4 taps), written 2 pixels apart: no unfolded copy.  Wg % 128
- * == 0, N <= 128, N % 4 == 0.  No reference counterpart. */
+ * == 0 (one halo box per kernel row), or Wg = 32 or 64 with Hg a multiple
+ * of 128 / Wg (one box of 128 / Wg rows per tap); N <= 128, N % 4 == 0.
+ * No reference counterpart. */
 int kgb_conv3x3_s2_dgrad_bf16(const void* g_dev, const void* wt_dev, float* dx_dev, int B, int Hg, int Wg, int C,
                               int N, int* err_dev, void* stream);
 

@@ -412,35 +412,40 @@ gemm_tn_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ 
     }
 }
 
-// Implicit convolutions with the input read once per image row of a tile:
-// tiles are 128 consecutive pixels of one row of the source grid (the
-// grid the A operand is read from; its width a multiple of 128).  A plan
-// lists, per channel block, up to three halo rows -- source row i +
-// row_dh[h], source columns w0 + col0 .. w0 + col0 + 135, 64 channels each
-// (a 136-row, 128-byte-row tile, zero fill outside the image) -- and per
-// halo row up to three taps: the A operand of a tap is that tile starting
-// `off` rows in (the descriptor's 128-byte swizzle follows the absolute
-// shared-memory address, so a start offset by whole rows reads the rows the
-// TMA wrote there), its B operand the weight tile of kernel tap `w`.  The
-// weights of all 9 taps (N <= BN rows) stay in shared memory for the whole
-// kernel.  Output pixel of source pixel (img, i, j): (img, out_rs i +
-// out_rb, out_cs j + out_cb) of an Hout x Wout image, so a tile's 128 output
-// rows are out_cs pixels apart.  Plans: the 3x3 stride-1 convolution and its
-// transposed form (3 halo rows, 3 taps each), and the four pixel-parity
-// classes of the data gradient of a 3x3 stride-2 convolution (1 or 2 halo
-// rows, 1, 2, 2 or 4 taps, outputs 2 pixels apart).  Same persistence,
-// accumulator double-buffering, epilogue and bounded waits as
-// gemm_tn_kernel.
+// Implicit convolutions with resident weights: tiles are 128 consecutive
+// pixels of the source grid (the grid the A operand is read from), either
+// part of one row (width a multiple of 128) or 128 / W whole rows (W
+// dividing 128).  A plan lists, per channel block, up to four boxes of 64
+// channels each -- the box of entry h starts at source row i + row_dh[h],
+// column w0 + row_dc[h] (zero fill outside the image) -- and per box up to
+// three taps: the A operand of a tap is that box starting `off` 128-byte rows
+// in (the descriptor's 128-byte swizzle follows the absolute shared-memory
+// address, so a start offset by whole rows reads the rows the TMA wrote
+// there), its B operand the weight tile of kernel tap `w`.  Row tiles use
+// halo boxes (136 pixels of one row, shared by the taps of one kernel row);
+// multi-row tiles use one box of the tile's own shape per tap.  The weights
+// of all 9 taps (N <= BN rows) stay in shared memory for the whole kernel.
+// Output pixel of source pixel (img, i, j): (img, out_rs i + out_rb, out_cs j
+// + out_cb) of an Hout x Wout image; the 32 rows of one epilogue warp lie in
+// one source row (W a multiple of 32), so they are out_cs pixels apart.
+// Plans: the 3x3 stride-1 convolution and its transposed form (3 halo rows,
+// 3 taps each), and the four pixel-parity classes of the data gradient of a
+// 3x3 stride-2 convolution (1, 2, 2 or 4 taps, outputs 2 pixels apart).
+// Same persistence, accumulator double-buffering, epilogue and bounded
+// waits as gemm_tn_kernel.
 constexpr int kHaloRows = 136;                  // 130 needed, 8-row multiple
 constexpr int kHaloBytes = 18 * 1024;           // 136 x 128 B, rounded to 1 KB
 constexpr int kHaloMaxStages = 8;
 
+constexpr int kPlanBoxes = 4;
+
 struct HaloPlan {
-    int nrows;                     // halo rows per channel block (1..3)
-    int row_dh[3];                 // source row offset of each halo row
-    int col0;                      // first source column of the halo, relative to the tile's
-    int row_ntaps[3];              // taps per halo row (1..3)
-    int tap_off[3][3], tap_w[3][3];  // per halo row and tap: row offset in the halo, kernel tap
+    int nrows;                     // boxes per channel block (1..4)
+    int row_dh[kPlanBoxes];        // source row offset of each box
+    int row_dc[kPlanBoxes];        // source column offset of each box, relative to the tile's
+    int row_ntaps[kPlanBoxes];     // taps per box (1..3)
+    int tap_off[kPlanBoxes][3], tap_w[kPlanBoxes][3];  // per box and tap: row offset in the box, kernel tap
+    int box_bytes;                 // bytes of one box
     int out_rs, out_rb, out_cs, out_cb, Hout, Wout;
     int ksteps_last;               // 16-channel k-steps of the last channel block that hold channels
 };
@@ -518,8 +523,8 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
                         break;
                     }
                     const int cb = st / plan.nrows, hr = st - cb * plan.nrows;
-                    mbar_expect_tx(bar_full + 8 * s, kHaloRows * BK * 2);
-                    tma_load_4d(sR + s * kHaloBytes, &tmX, bar_full + 8 * s, cb * BK, w0 + plan.col0,
+                    mbar_expect_tx(bar_full + 8 * s, (uint32_t)plan.box_bytes);
+                    tma_load_4d(sR + s * kHaloBytes, &tmX, bar_full + 8 * s, cb * BK, w0 + plan.row_dc[hr],
                                 h + plan.row_dh[hr], img);
                 }
             }
@@ -590,12 +595,15 @@ conv_halo_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant_
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // output row segment of this tile: 128 pixels, out_cs apart
+            // this warp's 32 rows: one source row segment, outputs out_cs
+            // apart; `opix` is the output pixel of tile row 0 on that line
+            // (tile rows q * 32 + lane), at least 0 since the output index
+            // grows with the source pixel
             const int m0 = t * BM;
-            const int img = m0 / hw, r = m0 - img * hw;
-            const int h = r / cg.W, w0 = r - h * cg.W;
-            const int64_t opix = ((int64_t)img * plan.Hout + (int64_t)plan.out_rs * h + plan.out_rb) * plan.Wout +
-                                 (int64_t)plan.out_cs * w0 + plan.out_cb;
+            const int img = m0 / hw, p = m0 - img * hw + q * 32;
+            const int hq = p / cg.W, wq = p - hq * cg.W;
+            const int64_t opix = ((int64_t)img * plan.Hout + (int64_t)plan.out_rs * hq + plan.out_rb) * plan.Wout +
+                                 (int64_t)plan.out_cs * wq + plan.out_cb - (int64_t)plan.out_cs * (q * 32);
             void* Ct = (flags & 2) ? static_cast<void*>(reinterpret_cast<__nv_bfloat16*>(C) + opix * N)
                                    : static_cast<void*>(reinterpret_cast<float*>(C) + opix * N);
             epilogue_store<BN>(tmem, q, a, lane, 0, 0, BM, N, plan.out_cs * N, Ct, bias, flags);
@@ -769,9 +777,10 @@ HaloPlan plan_conv3x3(int sgn, int Hout, int Wout, int C) {
     HaloPlan p{};
     p.ksteps_last = last_ksteps(C);
     p.nrows = 3;
-    p.col0 = -1;
+    p.box_bytes = kHaloRows * BK * 2;
     for (int ky = 0; ky < 3; ++ky) {
         p.row_dh[ky] = sgn * (ky - 1);
+        p.row_dc[ky] = -1;
         p.row_ntaps[ky] = 3;
         for (int kx = 0; kx < 3; ++kx) {
             p.tap_off[ky][kx] = sgn > 0 ? kx : 2 - kx;
@@ -793,21 +802,28 @@ HaloPlan plan_conv3x3(int sgn, int Hout, int Wout, int C) {
 // di = 1 for ky = 0 and 0 otherwise (dj likewise): the halo rows are g rows
 // i + 1 and i, its columns start at j0, and a tap with dj = 1 starts one
 // row into the halo.
-HaloPlan plan_s2_dgrad(int a, int b, int Hout, int Wout, int C) {
+// Class (a, b) of the data gradient of a 3x3 stride-2 convolution: input
+// pixel (2i + a, 2j + b) collects gradient pixel (i + dy, j + dx) through
+// kernel tap (ky, kx) for ky in {1} (a = 0) or {0, 2} (a = 1), dy = 1 for
+// ky = 0 else 0, and the same along columns.  halo: row tiles, one halo box
+// per kernel row shared by its column taps; otherwise one box per tap.
+HaloPlan plan_s2_dgrad(int a, int b, int Hout, int Wout, int C, bool halo) {
     HaloPlan p{};
     p.ksteps_last = last_ksteps(C);
     const int kys[2] = {a == 0 ? 1 : 0, 2}, nky = a == 0 ? 1 : 2;
     const int kxs[2] = {b == 0 ? 1 : 0, 2}, nkx = b == 0 ? 1 : 2;
-    p.nrows = nky;
-    p.col0 = 0;
+    p.nrows = halo ? nky : nky * nkx;
+    p.box_bytes = (halo ? kHaloRows : BM) * BK * 2;
     for (int r = 0; r < nky; ++r) {
         const int ky = kys[r];
-        p.row_dh[r] = ky == 0 ? 1 : 0;
-        p.row_ntaps[r] = nkx;
         for (int q = 0; q < nkx; ++q) {
             const int kx = kxs[q];
-            p.tap_off[r][q] = kx == 0 ? 1 : 0;
-            p.tap_w[r][q] = ky * 3 + kx;
+            const int e = halo ? r : r * nkx + q, t = halo ? q : 0;
+            p.row_dh[e] = ky == 0 ? 1 : 0;
+            p.row_dc[e] = halo ? 0 : (kx == 0 ? 1 : 0);
+            p.row_ntaps[e] = halo ? nkx : 1;
+            p.tap_off[e][t] = halo ? (kx == 0 ? 1 : 0) : 0;
+            p.tap_w[e][t] = ky * 3 + kx;
         }
     }
     p.out_rs = 2;
@@ -1035,8 +1051,12 @@ extern "C" int kgb_conv3x3_s2_dgrad_bf16(const void* g, const void* wt, float* d
     if (!g || !wt || !dx) return set_error(KGB_ERR_VALUE, "s2 dgrad: null pointer");
     if (B <= 0 || Hg <= 0 || Wg <= 0 || C <= 0 || N <= 0) return set_error(KGB_ERR_VALUE, "s2 dgrad: sizes must be positive");
     if (C % 8) return set_error(KGB_ERR_VALUE, "s2 dgrad: channels must be a multiple of 8 (16-byte pixel rows)");
-    if (Wg % BM || N > 128 || N % 4)
-        return set_error(KGB_ERR_VALUE, "s2 dgrad: needs gradient rows of 128-pixel multiples and N <= 128, N %% 4 == 0");
+    const bool halo = Wg % BM == 0;
+    const bool rows = !halo && Wg % 32 == 0 && BM % Wg == 0 && Hg % (BM / Wg) == 0;
+    if (!(halo || rows) || N > 128 || N % 4)
+        return set_error(KGB_ERR_VALUE,
+                         "s2 dgrad: needs gradient rows of 128-pixel multiples (or of 32 or 64 pixels with whole "
+                         "128-pixel tiles per image) and N <= 128, N %% 4 == 0");
     if ((((uintptr_t)g | (uintptr_t)wt | (uintptr_t)dx) & 15) != 0)
         return set_error(KGB_ERR_VALUE, "s2 dgrad: operands must be 16-byte aligned");
     const int cblk = (C + BK - 1) / BK;
@@ -1048,14 +1068,14 @@ extern "C" int kgb_conv3x3_s2_dgrad_bf16(const void* g, const void* wt, float* d
     if (!hstages) return set_error(KGB_ERR_NOT_IMPLEMENTED, "s2 dgrad: weights do not fit in shared memory");
     CUtensorMap ma, mb;
     int rc;
-    if ((rc = make_map_halo(&ma, g, B, Hg, Wg, C))) return rc;
+    if ((rc = halo ? make_map_halo(&ma, g, B, Hg, Wg, C) : make_map_nhwc(&ma, g, B, Hg, Wg, C, Wg, BM / Wg))) return rc;
     if ((rc = make_map(&mb, wt, N, K, K, BN))) return rc;
     const int flags = vector_flag(dx, 2 * N, 0);
     const ConvGeom hg{Hg, Wg, cblk, 1, B};
     cudaStream_t s = (cudaStream_t)stream;
     for (int a = 0; a < 2; ++a)
         for (int b = 0; b < 2; ++b) {
-            const HaloPlan plan = plan_s2_dgrad(a, b, 2 * Hg, 2 * Wg, C);
+            const HaloPlan plan = plan_s2_dgrad(a, b, 2 * Hg, 2 * Wg, C, halo);
             rc = BN == 64 ? halo_launch<64>(ma, mb, dx, (int)M, N, nullptr, flags, err_dev, hg, plan, hstages, s)
                           : halo_launch<128>(ma, mb, dx, (int)M, N, nullptr, flags, err_dev, hg, plan, hstages, s);
             if (rc) return rc;

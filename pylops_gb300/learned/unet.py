@@ -53,6 +53,13 @@ def _halo_weights_fit(C: int, N: int) -> bool:
     return 1024 + 9 * cblk * bn * 128 + 3 * 18 * 1024 + 8 * 12 + 16 <= 227 * 1024
 
 
+def _s2_tiles(Hg: int, Wg: int) -> bool:
+    """Does a Hg x Wg gradient grid split into 128-pixel tiles for
+    kgb_conv3x3_s2_dgrad_bf16 (parts of rows of 128-pixel multiples, or whole
+    rows of 32 or 64 pixels)?"""
+    return Wg % 128 == 0 or (Wg in (32, 64) and Hg % (128 // Wg) == 0)
+
+
 def _tileable(H: int, W: int) -> bool:
     """Can 128-pixel M tiles be TMA boxes of one image (kgb_conv3x3_bf16)?"""
     return (W >= 128 and W % 128 == 0) or (W < 128 and 128 % W == 0 and H % (128 // W) == 0)
@@ -440,7 +447,7 @@ class UNet:
             _native.check(L.kgb_conv3x3_bf16(g.data_ptr(), c.Wti.data_ptr(), dx.data_ptr(), B, H, W, c.cout, c.cin, 1,
                                              None, 0, self._err.data_ptr(), s))
             return
-        if self.implicit and c.s2_dx and Wo % 128 == 0 and H == 2 * Ho and W == 2 * Wo:
+        if self.implicit and c.s2_dx and _s2_tiles(Ho, Wo) and H == 2 * Ho and W == 2 * Wo:
             # stride 2: the four pixel-parity classes straight from g (no unfold)
             _native.check(L.kgb_conv3x3_s2_dgrad_bf16(g.data_ptr(), c.Wti.data_ptr(), dx.data_ptr(), B, Ho, Wo,
                                                       c.cout, c.cin, self._err.data_ptr(), s))

@@ -205,7 +205,8 @@ def test_implicit_weight_gradient_matches_conv2d_weight(B, H, W, C, N):
 
 
 @pytest.mark.parametrize("B,Hg,Wg,C,N", [(2, 4, 128, 64, 32), (1, 3, 256, 32, 64), (2, 2, 128, 128, 64),
-                                       (2, 2, 128, 64, 96)])
+                                       (2, 2, 128, 64, 96), (2, 4, 64, 64, 32), (1, 8, 32, 128, 64),
+                                       (3, 2, 64, 96, 64), (1, 4, 32, 40, 16)])
 def test_stride2_data_gradient_matches_conv2d_input(B, Hg, Wg, C, N):
     """kgb_conv3x3_s2_dgrad_bf16 (four pixel-parity classes of implicit
     stride-1 convolutions on g) against the input gradient of torch conv2d
@@ -245,3 +246,10 @@ def test_stride2_data_gradient_rejects_weights_that_do_not_fit():
     with pytest.raises(NotImplementedError):
         _native.check(_native.lib().kgb_conv3x3_s2_dgrad_bf16(g.data_ptr(), wt.data_ptr(), dx.data_ptr(), 1, 2, 128,
                                                               128, 96, None, torch.cuda.current_stream().cuda_stream))
+    # 64-pixel rows need an even number of them (whole 128-pixel tiles per image)
+    from pylops_gb300.learned.unet import _s2_tiles
+
+    assert not _s2_tiles(3, 64) and _s2_tiles(4, 64) and _s2_tiles(8, 32) and not _s2_tiles(4, 96)
+    with pytest.raises(ValueError):
+        _native.check(_native.lib().kgb_conv3x3_s2_dgrad_bf16(g.data_ptr(), wt.data_ptr(), dx.data_ptr(), 1, 3, 64,
+                                                              64, 32, None, torch.cuda.current_stream().cuda_stream))
