@@ -352,8 +352,11 @@ __global__ void head_dx_kernel(const bf16* __restrict__ g, const bf16* __restric
 // fp32 accumulation, one pixel per thread.
 __global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restrict__ w, const float* __restrict__ b,
                                uint4* __restrict__ y, int B, int H, int W, int N, int kpad, int relu) {
-    __shared__ float wsh[128 * 9], bsh[128];
-    for (int k = threadIdx.x; k < N * 9; k += blockDim.x) wsh[k] = __bfloat162float(w[(k / 9) * kpad + k % 9]);
+    // tap-major weights: the 8 output channels of one tap are two 16-byte loads
+    __shared__ __align__(16) float wsh[9 * 128];
+    __shared__ float bsh[128];
+    for (int k = threadIdx.x; k < N * 9; k += blockDim.x)
+        wsh[(k % 9) * 128 + k / 9] = __bfloat162float(w[(k / 9) * kpad + k % 9]);
     for (int k = threadIdx.x; k < N; k += blockDim.x) bsh[k] = b ? b[k] : 0.f;
     __syncthreads();
     const int64_t P = (int64_t)B * H * W;
@@ -374,12 +377,22 @@ __global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restric
         for (int n8 = 0; n8 < N; n8 += 8) {
             float o[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                float acc = bsh[n8 + j];
+            for (int j = 0; j < 8; ++j) o[j] = bsh[n8 + j];
 #pragma unroll
-                for (int k = 0; k < 9; ++k) acc += wsh[(n8 + j) * 9 + k] * v[k];
-                o[j] = relu ? fmaxf(acc, 0.f) : acc;
+            for (int k = 0; k < 9; ++k) {
+                const float4 a = *reinterpret_cast<const float4*>(wsh + k * 128 + n8);
+                const float4 c = *reinterpret_cast<const float4*>(wsh + k * 128 + n8 + 4);
+                o[0] += a.x * v[k];
+                o[1] += a.y * v[k];
+                o[2] += a.z * v[k];
+                o[3] += a.w * v[k];
+                o[4] += c.x * v[k];
+                o[5] += c.y * v[k];
+                o[6] += c.z * v[k];
+                o[7] += c.w * v[k];
             }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) o[j] = relu ? fmaxf(o[j], 0.f) : o[j];
             uint4 u;
             u.x = pack_bf16_pair(o[0], o[1]);
             u.y = pack_bf16_pair(o[2], o[3]);
@@ -393,10 +406,13 @@ __global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restric
 // Its weight gradient: dW[n][t] = sum_p g[p][n] x[p + off(t)].  Block k
 // takes image rows [k rpb, (k + 1) rpb); warp w of the block the rows k rpb
 // + w, + 4, ...; lane l the output channels l, l + 32, ... (N <= 128) with
-// nine tap accumulators each, walking the row with a sliding 3 x 3 window
-// of x.  The warps' sums are added in warp order into work[k][n * 9 + t];
+// nine tap accumulators each, walking the row kC1Span pixels at a time (the
+// span's gradient values and its 3 x (kC1Span + 2) window of x loaded
+// together, so the loads of a warp overlap).  The warps' sums are added in
+// warp order into work[k][n * 9 + t];
 // conv_c1_wgrad_final adds the blocks in a fixed order (warp per output).
 constexpr int kC1Warps = 4;
+constexpr int kC1Span = 8;  // pixels of a row whose loads are issued together
 __global__ void __launch_bounds__(32 * kC1Warps) conv_c1_wgrad_partial_kernel(const bf16* __restrict__ x,
                                                                              const bf16* __restrict__ g,
                                                                              float* __restrict__ work, int B, int H,
@@ -420,32 +436,32 @@ __global__ void __launch_bounds__(32 * kC1Warps) conv_c1_wgrad_partial_kernel(co
             if (w < 0 || w >= W || (dy < 0 && !up) || (dy > 0 && !dn)) return 0.f;
             return __bfloat162float(xr[(int64_t)dy * W + w]);
         };
-        // window v[dy][dx] = x at (h + dy - 1, w + dx - 1)
-        float v[3][3];
-#pragma unroll
-        for (int dy = 0; dy < 3; ++dy) {
-            v[dy][0] = 0.f;
-            v[dy][1] = xv(dy - 1, 0);
-            v[dy][2] = xv(dy - 1, 1);
-        }
-        for (int w = 0; w < W; ++w) {
+        // kC1Span pixels at a time: their gradients and the input window
+        // xw[dy][c] = x at (h + dy - 1, w0 + c - 1) are loaded together
+        // (independent loads in flight), then summed pixel by pixel
+        for (int w0 = 0; w0 < W; w0 += kC1Span) {
+            float gv[4][kC1Span];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int n = lane + 32 * q;
-                if (q < ng && n < N) {
-                    const float gv = __bfloat162float(g[(r * W + w) * N + n]);
 #pragma unroll
-                    for (int dy = 0; dy < 3; ++dy)
-#pragma unroll
-                        for (int dx = 0; dx < 3; ++dx) acc[q][dy * 3 + dx] += gv * v[dy][dx];
-                }
+                for (int j = 0; j < kC1Span; ++j)
+                    gv[q][j] = (q < ng && n < N && w0 + j < W) ? __bfloat162float(g[(r * W + w0 + j) * N + n]) : 0.f;
             }
+            float xw[3][kC1Span + 2];
 #pragma unroll
-            for (int dy = 0; dy < 3; ++dy) {
-                v[dy][0] = v[dy][1];
-                v[dy][1] = v[dy][2];
-                v[dy][2] = xv(dy - 1, w + 2);
-            }
+            for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                for (int c = 0; c < kC1Span + 2; ++c) xw[dy][c] = xv(dy - 1, w0 + c - 1);
+#pragma unroll
+            for (int j = 0; j < kC1Span; ++j)
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q < ng)
+#pragma unroll
+                        for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                            for (int dx = 0; dx < 3; ++dx) acc[q][dy * 3 + dx] += gv[q][j] * xw[dy][j + dx];
         }
     }
 #pragma unroll
