@@ -349,7 +349,7 @@ __global__ void head_dx_kernel(const bf16* __restrict__ g, const bf16* __restric
 // 3x3 convolution of a one-channel image (the network's first layer), zero
 // padding 1: y[p][n] = act(b[n] + sum_t w[n][t] x[p + off(t)]) as bf16, w
 // bf16 with row stride kpad (tap t = 3 ky + kx), N % 8 == 0, N <= 128;
-// fp32 accumulation, one pixel per thread.
+// fp32 accumulation, one pixel and 8 output channels per thread.
 __global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restrict__ w, const float* __restrict__ b,
                                uint4* __restrict__ y, int B, int H, int W, int N, int kpad, int relu) {
     // tap-major weights: the 8 output channels of one tap are two 16-byte loads
@@ -359,11 +359,15 @@ __global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restric
         wsh[(k % 9) * 128 + k / 9] = __bfloat162float(w[(k / 9) * kpad + k % 9]);
     for (int k = threadIdx.x; k < N; k += blockDim.x) bsh[k] = b ? b[k] : 0.f;
     __syncthreads();
-    const int64_t P = (int64_t)B * H * W;
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (int64_t)gridDim.x * blockDim.x) {
+    // thread = (pixel, group of 8 output channels): consecutive threads
+    // write consecutive 16-byte pieces of the NHWC output
+    const int G = N >> 3;
+    const int64_t T = (int64_t)B * H * W * G;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = i / G;
+        const int n8 = (int)(i - p * G) * 8;
         const int wi = (int)(p % W);
-        const int64_t t = p / W;
-        const int hi = (int)(t % H);
+        const int hi = (int)((p / W) % H);
         float v[9];
 #pragma unroll
         for (int ky = 0; ky < 3; ++ky)
@@ -374,32 +378,30 @@ __global__ void conv_c1_kernel(const bf16* __restrict__ x, const bf16* __restric
                                      ? __bfloat162float(x[p + (int64_t)(ky - 1) * W + (kx - 1)])
                                      : 0.f;
             }
-        for (int n8 = 0; n8 < N; n8 += 8) {
-            float o[8];
+        float o[8];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) o[j] = bsh[n8 + j];
+        for (int j = 0; j < 8; ++j) o[j] = bsh[n8 + j];
 #pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                const float4 a = *reinterpret_cast<const float4*>(wsh + k * 128 + n8);
-                const float4 c = *reinterpret_cast<const float4*>(wsh + k * 128 + n8 + 4);
-                o[0] += a.x * v[k];
-                o[1] += a.y * v[k];
-                o[2] += a.z * v[k];
-                o[3] += a.w * v[k];
-                o[4] += c.x * v[k];
-                o[5] += c.y * v[k];
-                o[6] += c.z * v[k];
-                o[7] += c.w * v[k];
-            }
-#pragma unroll
-            for (int j = 0; j < 8; ++j) o[j] = relu ? fmaxf(o[j], 0.f) : o[j];
-            uint4 u;
-            u.x = pack_bf16_pair(o[0], o[1]);
-            u.y = pack_bf16_pair(o[2], o[3]);
-            u.z = pack_bf16_pair(o[4], o[5]);
-            u.w = pack_bf16_pair(o[6], o[7]);
-            y[p * (N >> 3) + (n8 >> 3)] = u;
+        for (int k = 0; k < 9; ++k) {
+            const float4 a = *reinterpret_cast<const float4*>(wsh + k * 128 + n8);
+            const float4 c = *reinterpret_cast<const float4*>(wsh + k * 128 + n8 + 4);
+            o[0] += a.x * v[k];
+            o[1] += a.y * v[k];
+            o[2] += a.z * v[k];
+            o[3] += a.w * v[k];
+            o[4] += c.x * v[k];
+            o[5] += c.y * v[k];
+            o[6] += c.z * v[k];
+            o[7] += c.w * v[k];
         }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) o[j] = relu ? fmaxf(o[j], 0.f) : o[j];
+        uint4 u;
+        u.x = pack_bf16_pair(o[0], o[1]);
+        u.y = pack_bf16_pair(o[2], o[3]);
+        u.z = pack_bf16_pair(o[4], o[5]);
+        u.w = pack_bf16_pair(o[6], o[7]);
+        y[i] = u;
     }
 }
 
@@ -476,6 +478,80 @@ __global__ void __launch_bounds__(32 * kC1Warps) conv_c1_wgrad_partial_kernel(co
         float sum = 0.f;
         for (int k = 0; k < kC1Warps; ++k) sum += red[k][o];
         work[(int64_t)blockIdx.x * 9 * N + o] = sum;
+    }
+}
+
+// The same weight gradient, pixel-parallel: lane (slot, cg) of a warp takes
+// output channels 8 cg .. 8 cg + 7 (one 16-byte load of g) of pixel slot of
+// each group of 32 / G consecutive pixels (G = N / 8 lanes per pixel, so a
+// warp reads 512 contiguous bytes per load), two groups per step.  Each
+// lane sums its pixels in order, the slots sharing a channel group are
+// combined by a fixed xor-shuffle tree, the warps in warp order into
+// work[k][n * 9 + t].  Block k takes pixels [k ppb, (k + 1) ppb).
+template <int G>
+__global__ void __launch_bounds__(256) conv_c1_wgrad_px_kernel(const bf16* __restrict__ x, const uint4* __restrict__ g,
+                                                               float* __restrict__ work, int B, int H, int W) {
+    constexpr int PPW = 32 / G;  // pixels per warp and group
+    constexpr int NW = 8;        // warps per block
+    __shared__ float red[NW][9 * 8 * G];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int slot = lane / G, cg = lane - slot * G;
+    const int64_t P = (int64_t)B * H * W;
+    const int64_t ppb = (P + kColChunks - 1) / kColChunks;
+    const int64_t p0 = (int64_t)blockIdx.x * ppb, p1 = min(P, p0 + ppb);
+    float acc[8][9];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+#pragma unroll
+        for (int t = 0; t < 9; ++t) acc[j][t] = 0.f;
+    constexpr int64_t kStep = (int64_t)NW * PPW;
+    for (int64_t pb = p0 + warp * PPW + slot; pb < p1; pb += 2 * kStep) {
+        uint4 gv[2];
+        float xv[2][9];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int64_t p = pb + u * kStep;
+            const bool in = p < p1;
+            gv[u] = in ? __ldg(g + p * G + cg) : make_uint4(0u, 0u, 0u, 0u);
+            const int w = in ? (int)(p % W) : 0;
+            const int h = in ? (int)((p / W) % H) : 0;
+#pragma unroll
+            for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 3; ++dx) {
+                    const int hh = h + dy - 1, ww = w + dx - 1;
+                    xv[u][dy * 3 + dx] = (in && hh >= 0 && hh < H && ww >= 0 && ww < W)
+                                             ? __bfloat162float(x[p + (int64_t)(dy - 1) * W + (dx - 1)])
+                                             : 0.f;
+                }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const uint32_t wd[4] = {gv[u].x, gv[u].y, gv[u].z, gv[u].w};
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float gf = __uint_as_float((wd[j >> 1] >> (16 * (j & 1))) << 16);
+#pragma unroll
+                for (int t = 0; t < 9; ++t) acc[j][t] += gf * xv[u][t];
+            }
+        }
+    }
+#pragma unroll
+    for (int off = G; off < 32; off <<= 1)
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+#pragma unroll
+            for (int t = 0; t < 9; ++t) acc[j][t] += __shfl_xor_sync(0xffffffffu, acc[j][t], off);
+    if (slot == 0)
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+#pragma unroll
+            for (int t = 0; t < 9; ++t) red[warp][(cg * 8 + j) * 9 + t] = acc[j][t];
+    __syncthreads();
+    for (int o = threadIdx.x; o < 9 * 8 * G; o += blockDim.x) {
+        float sum = 0.f;
+        for (int k = 0; k < NW; ++k) sum += red[k][o];
+        work[(int64_t)blockIdx.x * 9 * 8 * G + o] = sum;
     }
 }
 
@@ -993,8 +1069,8 @@ int kgb_unet_conv3x3_c1(const void* x, const void* w, const void* bias, void* y,
         ((uintptr_t)y & 15))
         return set_error(KGB_ERR_VALUE, "unet_conv3x3_c1: bad arguments");
     const int64_t P = (int64_t)B * H * W;
-    conv_c1_kernel<<<grid_for(P), 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)w, (const float*)bias,
-                                                                  (uint4*)y, B, H, W, N, kpad, relu);
+    conv_c1_kernel<<<grid_for(P * (N / 8)), 256, 0, (cudaStream_t)stream>>>(
+        (const bf16*)x, (const bf16*)w, (const float*)bias, (uint4*)y, B, H, W, N, kpad, relu);
     KGB_CUDA_TRY(cudaGetLastError());
     return KGB_OK;
 }
@@ -1004,7 +1080,19 @@ int kgb_unet_conv3x3_c1_wgrad(const void* x, const void* g, float* dW, int B, in
     if (!x || !g || !dW || !work || B <= 0 || H <= 0 || W <= 0 || N <= 0 || N > 128 || kpad < 9)
         return set_error(KGB_ERR_VALUE, "unet_conv3x3_c1_wgrad: bad arguments (N <= 128)");
     cudaStream_t s = (cudaStream_t)stream;
-    conv_c1_wgrad_partial_kernel<<<kColChunks, 32 * kC1Warps, 0, s>>>((const bf16*)x, (const bf16*)g, work, B, H, W, N);
+    const bool px = ((uintptr_t)g & 15) == 0;
+    const bf16* xb = (const bf16*)x;
+    const uint4* g4 = (const uint4*)g;
+    if (px && N == 8)
+        conv_c1_wgrad_px_kernel<1><<<kColChunks, 256, 0, s>>>(xb, g4, work, B, H, W);
+    else if (px && N == 16)
+        conv_c1_wgrad_px_kernel<2><<<kColChunks, 256, 0, s>>>(xb, g4, work, B, H, W);
+    else if (px && N == 32)
+        conv_c1_wgrad_px_kernel<4><<<kColChunks, 256, 0, s>>>(xb, g4, work, B, H, W);
+    else if (px && N == 64)
+        conv_c1_wgrad_px_kernel<8><<<kColChunks, 256, 0, s>>>(xb, g4, work, B, H, W);
+    else
+        conv_c1_wgrad_partial_kernel<<<kColChunks, 32 * kC1Warps, 0, s>>>(xb, (const bf16*)g, work, B, H, W, N);
     KGB_CUDA_TRY(cudaGetLastError());
     conv_c1_wgrad_final_kernel<<<(9 * N + 7) / 8, 256, 0, s>>>(work, dW, N, kpad);
     KGB_CUDA_TRY(cudaGetLastError());
