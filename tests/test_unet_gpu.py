@@ -253,3 +253,50 @@ def test_stride2_data_gradient_rejects_weights_that_do_not_fit():
     with pytest.raises(ValueError):
         _native.check(_native.lib().kgb_conv3x3_s2_dgrad_bf16(g.data_ptr(), wt.data_ptr(), dx.data_ptr(), 1, 3, 64,
                                                               64, 32, None, torch.cuda.current_stream().cuda_stream))
+
+
+@pytest.mark.parametrize("B,H,W,N", [(2, 16, 32, 32), (1, 9, 40, 8), (2, 8, 64, 16), (1, 8, 16, 64), (1, 5, 24, 24),
+                                     (1, 4, 32, 128)])
+def test_first_layer_kernels_match_conv2d(B, H, W, N):
+    """kgb_unet_conv3x3_c1 (one input channel, N outputs, bias, ReLU, bf16
+    NHWC output) and kgb_unet_conv3x3_c1_wgrad (pixel-parallel reduction for
+    N = 8, 16, 32, 64; row-walking warps otherwise) against torch conv2d and
+    its weight gradient in float64 on the same bf16-rounded operands."""
+    from pylops_gb300 import _native
+
+    gen = torch.Generator().manual_seed(B * 1000 + H * 10 + N)
+    kpad = 16
+    x = _bf(torch.randn(B, H, W, generator=gen))
+    w = _bf(torch.randn(N, 9, generator=gen) / 3)
+    bias = torch.randn(N, generator=gen) / 4
+    gy = _bf(torch.randn(B, H, W, N, generator=gen))
+    L, s = _native.lib(), torch.cuda.current_stream().cuda_stream
+    xd = x.to(torch.bfloat16).cuda().contiguous()
+    wd = torch.zeros(N, kpad, dtype=torch.bfloat16)
+    wd[:, :9] = w.to(torch.bfloat16)
+    wd = wd.cuda()
+    bd = bias.cuda()
+    # forward: relu(b + sum_t w[n][t] x[p + off(t)]) rounded to bf16
+    y = torch.empty(B, H, W, N, dtype=torch.bfloat16, device="cuda")
+    _native.check(L.kgb_unet_conv3x3_c1(xd.data_ptr(), wd.data_ptr(), bd.data_ptr(), y.data_ptr(), B, H, W, N, kpad, 1,
+                                        s))
+    ref = torch.nn.functional.conv2d(x[:, None].double(), w.view(N, 1, 3, 3).double(), bias.double(), padding=1)
+    ref = torch.relu(ref).permute(0, 2, 3, 1).float()
+    got = y.float().cpu()
+    # float32 sums in tap order against float64, then bf16 rounding: at most one bf16 step apart
+    assert torch.all((got - ref).abs() <= ref.abs() * 2.0 ** -7 + 1e-6)
+    # weight gradient: dW[n][t] = sum over pixels of g[p][n] x[p + off(t)]; columns past 9 untouched
+    gd = gy.to(torch.bfloat16).cuda().contiguous()
+    dW = torch.full((N, kpad), 5.0, device="cuda")
+    work = torch.empty(1 << 21, device="cuda")
+    _native.check(L.kgb_unet_conv3x3_c1_wgrad(xd.data_ptr(), gd.data_ptr(), dW.data_ptr(), B, H, W, N, kpad,
+                                              work.data_ptr(), s))
+    refw = torch.nn.grad.conv2d_weight(x[:, None].double(), (N, 1, 3, 3), gy.permute(0, 3, 1, 2).double(), padding=1)
+    gotw = dW.cpu()
+    assert _rel(gotw[:, :9].numpy(), refw.view(N, 9).numpy()) < 1e-5
+    assert torch.all(gotw[:, 9:] == 5.0)
+    # deterministic: the same bits on a second call
+    dW2 = torch.full((N, kpad), 5.0, device="cuda")
+    _native.check(L.kgb_unet_conv3x3_c1_wgrad(xd.data_ptr(), gd.data_ptr(), dW2.data_ptr(), B, H, W, N, kpad,
+                                              work.data_ptr(), s))
+    assert torch.equal(dW2.cpu(), gotw)
