@@ -974,7 +974,9 @@ extern "C" int kgb_conv3x3_bf16(const void* x, const void* w, void* y, int B, in
     const int K = 9 * cblk * BK;
     const int64_t M = (int64_t)B * H * W;
     if (M > 0x7fffffffLL) return set_error(KGB_ERR_VALUE, "conv: too many pixels");
-    const int BN = N <= 64 ? 64 : 128;
+    // N > 128: 256-column tiles, so each input box serves twice the columns
+    // (the boxes per k-tile, not the MMAs, bound these small-image layers)
+    const int BN = N <= 64 ? 64 : N <= 128 ? 128 : 256;
     CUtensorMap ma, mb;
     int rc;
     // rows of whole 128-pixel segments, one N tile, weights resident: read
@@ -998,7 +1000,9 @@ extern "C" int kgb_conv3x3_bf16(const void* x, const void* w, void* y, int B, in
     const int ktiles = K / BK;
     if (BN == 64)
         return gemm_launch<64, kModeConv>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
-    return gemm_launch<128, kModeConv>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
+    if (BN == 128)
+        return gemm_launch<128, kModeConv>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
+    return gemm_launch<256, kModeConv>(ma, mb, y, (int)M, N, K, N, bias, flags, err_dev, 1, ktiles, 0, s, cg);
 }
 
 extern "C" int kgb_conv3x3_wgrad_bf16(const void* xT3, const void* gTr, float* dW, int B, int H, int W, int C, int N,

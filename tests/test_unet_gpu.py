@@ -114,7 +114,8 @@ def test_splitk_gemm_matches_fp32_reference():
 
 @pytest.mark.parametrize("B,H,W,C,N,flip", [(2, 16, 32, 32, 32, 0), (1, 8, 256, 96, 64, 0), (2, 32, 64, 64, 96, 1),
                                             (1, 64, 128, 40, 128, 1), (2, 6, 256, 32, 32, 1),
-                                            (3, 2, 128, 128, 64, 0)])
+                                            (3, 2, 128, 128, 64, 0), (2, 8, 64, 64, 192, 1), (1, 4, 32, 128, 256, 0),
+                                            (1, 8, 64, 64, 320, 0), (2, 2, 128, 64, 144, 1)])
 def test_implicit_conv3x3_matches_conv2d(B, H, W, C, N, flip):
     """kgb_conv3x3_bf16 (4-D TMA boxes shifted per tap, zero fill as padding;
     for W a multiple of 128 one halo row per ky shared by the three kx taps)
