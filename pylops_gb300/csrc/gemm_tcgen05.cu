@@ -857,12 +857,16 @@ template <int BN, int MODE = kModePlain>
 int gemm_launch(const CUtensorMap& ma, const CUtensorMap& mb, void* C, int M, int N, int K, int ldc, const float* bias,
                 int flags, int* err, int splits, int kt_per, int64_t split_stride, cudaStream_t s,
                 ConvGeom cg = ConvGeom{1, 1, 1, 1, 1}) {
-    static bool attr = false;
+    // the shared-memory limit is a per-device attribute of the kernel: set
+    // once per device
+    static bool attr[64] = {false};
+    int dev = 0;
+    KGB_CUDA_TRY(cudaGetDevice(&dev));
     const size_t smem = gemm_smem<BN>();
-    if (!attr) {
+    if (dev < 0 || dev >= 64 || !attr[dev]) {
         KGB_CUDA_TRY(cudaFuncSetAttribute(gemm_tn_kernel<BN, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)smem));
-        attr = true;
+        if (dev >= 0 && dev < 64) attr[dev] = true;
     }
     const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
     const int64_t ntiles = (int64_t)tiles_m * tiles_n * splits;
