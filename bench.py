@@ -853,6 +853,74 @@ def run_unet(args):
     }))
 
 
+def run_conv(args):
+    """One implicit 3x3 convolution of the U-Net through the C-ABI, on seeded
+    bf16 NHWC operands: --conv B,H,W,C,N,flip.  --conv-kind fwd: the
+    convolution (flip = 1: its transposed form, the data gradient;
+    kgb_conv3x3_bf16, bf16 output, bias-free with ReLU); wgrad: the weight
+    gradient (kgb_unet_row_transpose of x and g, then
+    kgb_conv3x3_wgrad_bf16).  A step is one such call (with its transposes).
+    value = algorithmic TFLOP/s, 2 B H W N 9 C flops per step.  Small cases
+    of the network's layers for ncu captures of one kernel."""
+    import torch
+
+    from pylops_gb300 import _native
+
+    B, H, W, C, N, flip = (int(v) for v in args.conv.split(","))
+    P = B * H * W
+    Cp = (C + 63) // 64 * 64
+    g = torch.Generator(device="cuda").manual_seed(0)
+    L, s = _native.lib(), torch.cuda.current_stream().cuda_stream
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    x = torch.randn(P * C, device="cuda", generator=g).to(torch.bfloat16)
+    if args.conv_kind == "fwd":
+        w = torch.randn(N * 9 * Cp, device="cuda", generator=g).to(torch.bfloat16)
+        y = torch.empty(P * N, dtype=torch.bfloat16, device="cuda")
+
+        def step():
+            _native.check(L.kgb_conv3x3_bf16(x.data_ptr(), w.data_ptr(), y.data_ptr(), B, H, W, C, N, flip, None, 3,
+                                             err.data_ptr(), s))
+
+        launches, kernel = 1, "conv_halo_kernel / gemm_tn_kernel (implicit convolution)"
+    else:
+        gy = torch.randn(P * N, device="cuda", generator=g).to(torch.bfloat16)
+        xT3 = torch.empty(3 * P * C, dtype=torch.bfloat16, device="cuda")
+        gTr = torch.empty(P * N, dtype=torch.bfloat16, device="cuda")
+        dW = torch.empty(N * 9 * C, device="cuda")
+        work = torch.empty(1 << 23, device="cuda")
+
+        def step():
+            _native.check(L.kgb_unet_row_transpose(x.data_ptr(), xT3.data_ptr(), B, H, W, C, 3, s))
+            _native.check(L.kgb_unet_row_transpose(gy.data_ptr(), gTr.data_ptr(), B, H, W, N, 1, s))
+            _native.check(L.kgb_conv3x3_wgrad_bf16(xT3.data_ptr(), gTr.data_ptr(), dW.data_ptr(), B, H, W, C, N,
+                                                   9 * C, work.data_ptr(), work.numel(), err.data_ptr(), s))
+
+        launches, kernel = 4, "gemm_tn_kernel (implicit weight gradient) with its row transposes and slice sum"
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = 2.0 * P * N * 9 * C
+    peak = _peaks().get("bf16_tflops") or 1900.0
+    ach = flops / (ms * 1e-3) / 1e12
+    print(json.dumps({
+        "metric": "implicit 3x3 convolution TFLOP/s", "value": round(ach, 2), "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": "conv3x3_%s_b%d_%dx%d_c%d_n%d_flip%d" % (args.conv_kind, B, H, W, C, N, flip)},
+        "roofline": {"bound": "tensor", "kernel": kernel, "achieved": round(ach, 2), "peak": peak,
+                     "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None},
+        "gpu_launches": launches * args.steps, "device_error": int(err.item()),
+    }))
+
+
 def run_nsconv(args):
     """Image-domain Hessian (NonStationaryConvolve2D): a 512 x 256 image (the
     learned-LSM grid) with 41 x 41 point-spread filters on a 16 x 8 coarse
@@ -1140,11 +1208,14 @@ def main():
     ap.add_argument("--variant", type=int, default=-1, help="force the forward kernel variant (0, 1, 2, 3)")
     ap.add_argument("--adjoint-variant", type=int, default=-1, help="force the adjoint kernel variant (0, 1, 2)")
     ap.add_argument("--workload", default="kirchhoff2d",
-                    choices=["kirchhoff2d", "batch", "lsm", "single", "unet", "nsconv", "kirchhoff3d"],
+                    choices=["kirchhoff2d", "batch", "lsm", "single", "unet", "nsconv", "kirchhoff3d", "conv3x3"],
                     help="kirchhoff2d: the headline fwd+adj workload; batch: 256 batched LSM problems; "
                          "lsm: learned vs plain LSQR time to a 1e-2 data residual (--steps held-out models); "
                          "single: the single-traveltime-table (HBM-streaming) mode; unet: U-Net training; "
-                         "nsconv: the non-stationary convolution (image-domain Hessian); kirchhoff3d: the 3-D workload")
+                         "nsconv: the non-stationary convolution (image-domain Hessian); kirchhoff3d: the 3-D workload; "
+                         "conv3x3: one implicit U-Net convolution or weight gradient (--conv, --conv-kind)")
+    ap.add_argument("--conv", default="2,512,256,32,32,0", help="conv3x3 workload: B,H,W,C,N,flip")
+    ap.add_argument("--conv-kind", default="fwd", choices=["fwd", "wgrad"])
     ap.add_argument("--weights", default="bfloat16", choices=["bfloat16", "float32"],
                     help="dynamic weight tables of the 3-D workload")
     ap.add_argument("--single-receivers", type=int, default=100)
@@ -1177,6 +1248,8 @@ def main():
         run_nsconv(args)
     elif args.workload == "kirchhoff3d":
         run_kirchhoff3d(args)
+    elif args.workload == "conv3x3":
+        run_conv(args)
     else:
         run_gpu(args)
 
