@@ -46,3 +46,20 @@ def test_illumination_diagonal_matches_oracle_column_norms():
     # exact up to the per-point spread of interpolation fractions (24 traces here)
     assert abs(np.median(ratio) - 1.0) < 0.02
     assert ratio.min() > 0.88 and ratio.max() < 1.12
+
+
+def test_unet_kernel_eligibility_rules():
+    """Host-side rules that route a U-Net layer to the resident-weight
+    implicit kernels (they mirror the C entry points' checks): the 9-tap
+    weights plus three halo rows fit in 227 KB of shared memory, and a
+    stride-2 gradient grid splits into 128-pixel tiles (parts of rows of
+    128-pixel multiples, or whole rows of 32 or 64 pixels)."""
+    from pylops_gb300.learned.unet import _halo_weights_fit, _s2_tiles
+
+    # (C, N): one or two 64-channel blocks with 64 columns, one with 128; not two with 128 or three with 64
+    assert _halo_weights_fit(32, 32) and _halo_weights_fit(64, 64) and _halo_weights_fit(128, 64)
+    assert _halo_weights_fit(64, 128) and _halo_weights_fit(96, 64)
+    assert not _halo_weights_fit(128, 96) and not _halo_weights_fit(192, 64) and not _halo_weights_fit(256, 128)
+    for Hg, Wg, ok in [(1, 128, True), (3, 256, True), (4, 64, True), (3, 64, False), (8, 32, True), (6, 32, False),
+                       (4, 96, False), (2, 16, False)]:
+        assert _s2_tiles(Hg, Wg) is ok, (Hg, Wg)
